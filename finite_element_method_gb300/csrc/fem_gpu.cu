@@ -1,0 +1,1628 @@
+// fem_gpu.cu -- GB300 (sm_103a) implementation of the C ABI in include/fem_gpu.h.
+//
+// Pipeline (one handle = one model = one CUDA stream):
+//   add_*      host registries (node numbers, duplicates) as in the reference's
+//              check_* functions, then a GPU validation kernel over the batch
+//              (Truss/Beam/Plate::create checks); first failure wins.
+//   symbolic   node-pair keys of every element in call order -> stable radix
+//              sort -> global blocks (unordered node pairs) with their
+//              contributors in element order; per-pair 36-bit non-zero masks
+//              (from the numeric element arithmetic) -> block masks -> CSR
+//              pattern, stiffness groups and the contribution map.
+//   numeric    element kernels write each node-pair 6x6 block to its
+//              destination-sorted slot (no atomics); the block reduction sums
+//              the slots of a block in element order (bit-exact with the
+//              reference's call-order accumulation) and scatters into CSR.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <cub/cub.cuh>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "../../include/fem_gpu.h"
+#include "element_math.cuh"
+
+using namespace femgpu;
+
+namespace {
+
+constexpr int kTruss = 0, kBeam = 1, kPlate = 2;
+constexpr int kPairs2 = 3;   // (1,1) (1,2) (2,2)
+constexpr int kPairs4 = 10;  // (1,1) (1,2) (1,3) (1,4) (2,2) (2,3) (2,4) (3,3) (3,4) (4,4)
+
+__host__ __device__ __forceinline__ void pair_nodes4(int p, int& i, int& j) {
+  const int I[10] = {0, 0, 0, 0, 1, 1, 1, 2, 2, 3};
+  const int J[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
+  i = I[p];
+  j = J[p];
+}
+__host__ __device__ __forceinline__ void pair_nodes2(int p, int& i, int& j) {
+  i = p == 2 ? 1 : 0;
+  j = p == 0 ? 0 : 1;
+}
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t cap = 0;
+  cudaError_t reserve(size_t n, cudaStream_t s, size_t keep = 0) {
+    if (n <= cap) return cudaSuccess;
+    size_t nc = std::max<size_t>(n, cap ? cap + cap / 2 : 256);
+    T* q = nullptr;
+    cudaError_t e = cudaMalloc((void**)&q, nc * sizeof(T));
+    if (e != cudaSuccess) return e;
+    if (p && keep) {
+      e = cudaMemcpyAsync(q, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return e;
+      e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) return e;
+    }
+    if (p) cudaFree(p);
+    p = q;
+    cap = nc;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// kernels: validation
+// ---------------------------------------------------------------------------
+struct NodesView {
+  const double *x, *y, *z;
+  __device__ __forceinline__ void get(int i, double o[3]) const {
+    o[0] = x[i];
+    o[1] = y[i];
+    o[2] = z[i];
+  }
+};
+
+__global__ void k_validate_truss(NodesView nd, const int32_t* __restrict__ n1, const int32_t* __restrict__ n2,
+                                 const double* __restrict__ E, const double* __restrict__ A,
+                                 const double* __restrict__ A2, size_t begin, size_t count, int* status,
+                                 unsigned long long* first) {
+  size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  size_t e = begin + k;
+  int st = 0;
+  if (E[e] <= 0.0) st = FEM_GPU_ERR_YOUNG;
+  else if (A[e] <= 0.0) st = FEM_GPU_ERR_AREA;
+  else if (A2[e] == A2[e] && A2[e] <= 0.0) st = FEM_GPU_ERR_AREA2;
+  else {
+    double x1[3], x2[3], R[9];
+    nd.get(n1[e], x1);
+    nd.get(n2[e], x2);
+    if (!truss_rotation(x1, x2, 0.0, R)) st = FEM_GPU_ERR_ZERO_LENGTH;
+  }
+  status[k] = st;
+  if (st) atomicMin(first, (unsigned long long)k);
+}
+
+struct BeamView {
+  const int32_t *n1, *n2;
+  const double *E, *nu, *A, *i11, *i22, *i12, *it, *ks, *ax, *ay, *az;
+};
+
+__global__ void k_validate_beam(NodesView nd, BeamView b, size_t begin, size_t count, int* status,
+                                unsigned long long* first) {
+  size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  size_t e = begin + k;
+  int st = 0;
+  if (b.E[e] <= 0.0) st = FEM_GPU_ERR_YOUNG;
+  else if (b.nu[e] <= 0.0) st = FEM_GPU_ERR_POISSON;
+  else if (b.A[e] <= 0.0) st = FEM_GPU_ERR_AREA;
+  else if (b.i11[e] <= 0.0) st = FEM_GPU_ERR_I11;
+  else if (b.i22[e] <= 0.0) st = FEM_GPU_ERR_I22;
+  else if (b.it[e] <= 0.0) st = FEM_GPU_ERR_IT;
+  else if (b.ks[e] <= 0.0) st = FEM_GPU_ERR_SHEAR_FACTOR;
+  else {
+    double x1[3], x2[3], d[3], p[3];
+    nd.get(b.n1[e], x1);
+    nd.get(b.n2[e], x2);
+    sub3(x2, x1, d);
+    double axis[3] = {b.ax[e], b.ay[e], b.az[e]};
+    project_perp(axis, d, p);
+    if (norm3(p) == 0.0) st = FEM_GPU_ERR_PARALLEL_AXIS;
+    else if (!(norm3(d) > 0.0)) st = FEM_GPU_ERR_ZERO_LENGTH;
+  }
+  status[k] = st;
+  if (st) atomicMin(first, (unsigned long long)k);
+}
+
+struct PlateView {
+  const int32_t *n1, *n2, *n3, *n4;
+  const double *E, *nu, *t, *ks;
+};
+
+__global__ void k_validate_plate(NodesView nd, PlateView pl, double abs_tol, size_t begin, size_t count, int* status,
+                                 unsigned long long* first) {
+  size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  size_t e = begin + k;
+  int st = 0;
+  if (pl.E[e] <= 0.0) st = FEM_GPU_ERR_YOUNG;
+  else if (pl.nu[e] <= 0.0) st = FEM_GPU_ERR_POISSON;
+  else if (pl.t[e] <= 0.0) st = FEM_GPU_ERR_THICKNESS;
+  else if (pl.ks[e] <= 0.0) st = FEM_GPU_ERR_SHEAR_FACTOR;
+  else {
+    double p1[3], p2[3], p3[3], p4[3];
+    nd.get(pl.n1[e], p1);
+    nd.get(pl.n2[e], p2);
+    nd.get(pl.n3[e], p3);
+    nd.get(pl.n4[e], p4);
+    if (quad_on_line(p1, p2, p3, p4)) st = FEM_GPU_ERR_NODES_ON_LINE;
+    else if (!quad_on_plane(p1, p2, p3, p4, abs_tol)) st = FEM_GPU_ERR_NOT_ON_PLANE;
+    else {
+      bool ok;
+      int hs = quad_hull_size(p1, p2, p3, p4, abs_tol, ok);
+      if (!ok) st = FEM_GPU_ERR_NODES_ON_LINE;
+      else if (hs != 4) st = FEM_GPU_ERR_NOT_CONVEX;
+    }
+  }
+  status[k] = st;
+  if (st) atomicMin(first, (unsigned long long)k);
+}
+
+// rotation getters (fem.rs:171-202)
+__global__ void k_rotation(int kind, NodesView nd, const int32_t* n1, const int32_t* n2, const int32_t* n3,
+                           const int32_t* n4, BeamView b, double rel_tol, double abs_tol, size_t e, double* out) {
+  double R[9];
+  for (int k = 0; k < 9; ++k) R[k] = 0.0;
+  if (kind == kTruss) {
+    double x1[3], x2[3];
+    nd.get(n1[e], x1);
+    nd.get(n2[e], x2);
+    truss_rotation(x1, x2, abs_tol, R);
+  } else if (kind == kBeam) {
+    double x1[3], x2[3], i11p, i22p;
+    nd.get(b.n1[e], x1);
+    nd.get(b.n2[e], x2);
+    double axis[3] = {b.ax[e], b.ay[e], b.az[e]};
+    beam_rotation(x1, x2, b.i11[e], b.i22[e], b.i12[e], axis, rel_tol, abs_tol, R, i11p, i22p);
+  } else {
+    double x2[3], x3[3], x4[3];
+    nd.get(n2[e], x2);
+    nd.get(n3[e], x3);
+    nd.get(n4[e], x4);
+    plate_rotation(x2, x3, x4, abs_tol, R);
+  }
+  for (int k = 0; k < 9; ++k) out[k] = R[k];
+}
+
+// ---------------------------------------------------------------------------
+// kernels: symbolic
+// ---------------------------------------------------------------------------
+__global__ void k_gen_pairs(int kind, const int32_t* __restrict__ n1, const int32_t* __restrict__ n2,
+                            const int32_t* __restrict__ n3, const int32_t* __restrict__ n4, size_t begin,
+                            size_t count, size_t pair_base, uint64_t* keys, uint32_t* vals) {
+  size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  size_t e = begin + k;
+  int ppe = kind == kPlate ? kPairs4 : kPairs2;
+  int32_t nodes[4];
+  nodes[0] = n1[e];
+  nodes[1] = n2[e];
+  if (kind == kPlate) {
+    nodes[2] = n3[e];
+    nodes[3] = n4[e];
+  }
+  for (int p = 0; p < ppe; ++p) {
+    int i, j;
+    if (kind == kPlate) pair_nodes4(p, i, j);
+    else pair_nodes2(p, i, j);
+    uint32_t I = (uint32_t)nodes[i], J = (uint32_t)nodes[j];
+    uint32_t lo = I < J ? I : J, hi = I < J ? J : I;
+    size_t pid = pair_base + k * ppe + p;
+    keys[pid] = ((uint64_t)lo << 32) | hi;
+    vals[pid] = ((uint32_t)kind << 30) | (uint32_t)(e * ppe + p);
+  }
+}
+
+// a 6x6 block in element orientation -> destination (mask bits or V slot),
+// transposed when the element's first node has the larger global index
+struct BlockSink {
+  uint64_t* mask;        // mask mode: per (element, pair)
+  double* V;             // numeric mode
+  const uint32_t* slot;  // numeric mode: per (element, pair)
+  __device__ __forceinline__ void put(size_t ep, bool transpose, const double blk[36]) const {
+    if (mask) {
+      uint64_t m = 0;
+#pragma unroll
+      for (int a = 0; a < 6; ++a)
+#pragma unroll
+        for (int b = 0; b < 6; ++b) {
+          int e = transpose ? 6 * b + a : 6 * a + b;
+          if (blk[6 * a + b] != 0.0) m |= 1ull << e;
+        }
+      mask[ep] = m;
+    } else {
+      double* dst = V + (size_t)slot[ep] * 36;
+      if (!transpose) {
+        double2* d2 = reinterpret_cast<double2*>(dst);
+#pragma unroll
+        for (int k = 0; k < 18; ++k) d2[k] = make_double2(blk[2 * k], blk[2 * k + 1]);
+      } else {
+        double2* d2 = reinterpret_cast<double2*>(dst);
+#pragma unroll
+        for (int k = 0; k < 18; ++k) {
+          int e0 = 2 * k, e1 = 2 * k + 1;
+          d2[k] = make_double2(blk[6 * (e0 % 6) + e0 / 6], blk[6 * (e1 % 6) + e1 / 6]);
+        }
+      }
+    }
+  }
+};
+
+__global__ void __launch_bounds__(128) k_truss(NodesView nd, const int32_t* __restrict__ n1,
+                                               const int32_t* __restrict__ n2, const double* __restrict__ E,
+                                               const double* __restrict__ A, const double* __restrict__ A2,
+                                               double abs_tol, size_t count, BlockSink sink) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= count) return;
+  int I = n1[e], J = n2[e];
+  double x1[3], x2[3], g[9];
+  nd.get(I, x1);
+  nd.get(J, x2);
+  if (!truss_block(x1, x2, E[e], A[e], A2[e], abs_tol, g)) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) g[k] = 0.0;
+  }
+  double blk[36];
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    double sg = s == 1 ? -1.0 : 1.0;
+#pragma unroll
+    for (int k = 0; k < 36; ++k) blk[k] = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) blk[6 * a + b] = s == 1 ? -g[3 * a + b] : g[3 * a + b];
+    (void)sg;
+    sink.put(e * kPairs2 + s, s == 1 && I > J, blk);
+  }
+}
+
+__global__ void __launch_bounds__(128) k_beam(NodesView nd, BeamView b, double rel_tol, double abs_tol, size_t count,
+                                              BlockSink sink) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= count) return;
+  int I = b.n1[e], J = b.n2[e];
+  double x1[3], x2[3];
+  nd.get(I, x1);
+  nd.get(J, x2);
+  double axis[3] = {b.ax[e], b.ay[e], b.az[e]};
+  BeamBlocks B;
+  if (!beam_blocks(x1, x2, b.E[e], b.nu[e], b.A[e], b.i11[e], b.i22[e], b.i12[e], b.it[e], b.ks[e], axis, rel_tol,
+                   abs_tol, B)) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) B.uu[k] = B.ut[k] = B.th[k] = B.tu[k] = B.thth2[k] = 0.0;
+  }
+  double blk[36];
+  // node block (1,1): [uu ut; ut^T th]
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      blk[6 * a + c] = B.uu[3 * a + c];
+      blk[6 * a + 3 + c] = B.ut[3 * a + c];
+      blk[6 * (3 + a) + c] = B.ut[3 * c + a];
+      blk[6 * (3 + a) + 3 + c] = B.th[3 * a + c];
+    }
+  sink.put(e * kPairs2 + 0, false, blk);
+  // node block (1,2): [-uu ut; tu thth2]
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      blk[6 * a + c] = -B.uu[3 * a + c];
+      blk[6 * a + 3 + c] = B.ut[3 * a + c];
+      blk[6 * (3 + a) + c] = B.tu[3 * a + c];
+      blk[6 * (3 + a) + 3 + c] = B.thth2[3 * a + c];
+    }
+  sink.put(e * kPairs2 + 1, I > J, blk);
+  // node block (2,2): [uu -ut; -ut^T th]
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      blk[6 * a + c] = B.uu[3 * a + c];
+      blk[6 * a + 3 + c] = -B.ut[3 * a + c];
+      blk[6 * (3 + a) + c] = -B.ut[3 * c + a];
+      blk[6 * (3 + a) + 3 + c] = B.th[3 * a + c];
+    }
+  sink.put(e * kPairs2 + 2, false, blk);
+}
+
+__global__ void __launch_bounds__(128) k_plate(NodesView nd, PlateView pl, double abs_tol, size_t count,
+                                               BlockSink sink) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= count) return;
+  int nidx[4] = {pl.n1[e], pl.n2[e], pl.n3[e], pl.n4[e]};
+  double X[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) nd.get(nidx[k], X[k]);
+  double R[9];
+  if (!plate_rotation(X[1], X[2], X[3], abs_tol, R)) set_identity(R);
+  double xl[4] = {0.0, 0.0, 0.0, 0.0}, yl[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (i == 2) continue;
+    double dd[3];
+    sub3(X[i], X[2], dd);
+    xl[i] = (R[0] * dd[0] + R[1] * dd[1]) + R[2] * dd[2];
+    yl[i] = (R[3] * dd[0] + R[4] * dd[1]) + R[5] * dd[2];
+  }
+  PlateCore C;
+  plate_core(xl, yl, pl.E[e], pl.nu[e], pl.t[e], pl.ks[e], C);
+  bool ident = is_identity(R);
+#pragma unroll 1
+  for (int p = 0; p < kPairs4; ++p) {
+    int i, j;
+    pair_nodes4(p, i, j);
+    double blk[36];
+    plate_local_block(C, i, j, blk);
+    if (!ident) {
+      double o[36];
+      plate_rotate_block(R, i == j, blk, o);
+#pragma unroll
+      for (int k = 0; k < 36; ++k) blk[k] = o[k];
+    }
+    sink.put(e * kPairs4 + p, i != j && nidx[i] > nidx[j], blk);
+  }
+}
+
+// sorted position k: record the element pair's slot and its mask
+__global__ void k_scatter_slots(const uint32_t* __restrict__ vals, size_t n, uint32_t* slot_t, uint32_t* slot_b,
+                                uint32_t* slot_p, const uint64_t* mask_t, const uint64_t* mask_b,
+                                const uint64_t* mask_p, uint64_t* sorted_mask) {
+  size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  uint32_t v = vals[k];
+  uint32_t kind = v >> 30, idx = v & 0x3fffffffu;
+  uint32_t* s = kind == kTruss ? slot_t : kind == kBeam ? slot_b : slot_p;
+  const uint64_t* m = kind == kTruss ? mask_t : kind == kBeam ? mask_b : mask_p;
+  s[idx] = (uint32_t)k;
+  sorted_mask[k] = m[idx];
+}
+
+__global__ void k_heads(const uint64_t* __restrict__ keys, size_t n, uint32_t* head) {
+  size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  head[k] = (k == 0 || keys[k] != keys[k - 1]) ? 1u : 0u;
+}
+
+// blk_id = inclusive scan of heads - 1
+__global__ void k_block_starts(const uint32_t* __restrict__ blk_incl, size_t n, uint32_t* blk_start) {
+  size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  if (k == 0 || blk_incl[k] != blk_incl[k - 1]) blk_start[blk_incl[k] - 1] = (uint32_t)k;
+}
+
+__device__ __forceinline__ uint64_t transpose36(uint64_t m) {
+  uint64_t t = 0;
+  for (int a = 0; a < 6; ++a)
+    for (int b = 0; b < 6; ++b)
+      if ((m >> (6 * a + b)) & 1ull) t |= 1ull << (6 * b + a);
+  return t;
+}
+
+__global__ void k_block_meta(const uint32_t* __restrict__ blk_start, size_t nb, size_t n_pairs,
+                             const uint64_t* __restrict__ keys, const uint64_t* __restrict__ sorted_mask,
+                             uint32_t* blk_count, uint64_t* blk_mask, uint64_t* blk_maskT, int32_t* blk_I,
+                             int32_t* blk_J, uint32_t* adj_n) {
+  size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  uint32_t s = blk_start[b];
+  uint32_t e = b + 1 < nb ? blk_start[b + 1] : (uint32_t)n_pairs;
+  uint64_t m = 0;
+  for (uint32_t k = s; k < e; ++k) m |= sorted_mask[k];
+  blk_count[b] = e - s;
+  blk_mask[b] = m;
+  blk_maskT[b] = transpose36(m);
+  uint64_t key = keys[s];
+  int32_t I = (int32_t)(key >> 32), J = (int32_t)(key & 0xffffffffu);
+  blk_I[b] = I;
+  blk_J[b] = J;
+  adj_n[b] = I == J ? 1u : 2u;
+}
+
+__global__ void k_adjacency(const uint32_t* __restrict__ adj_off, size_t nb, const int32_t* __restrict__ blk_I,
+                            const int32_t* __restrict__ blk_J, uint64_t* akeys, uint32_t* avals) {
+  size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  uint32_t o = adj_off[b];
+  uint32_t I = (uint32_t)blk_I[b], J = (uint32_t)blk_J[b];
+  akeys[o] = ((uint64_t)I << 32) | J;
+  avals[o] = (uint32_t)(b << 1);
+  if (I != J) {
+    akeys[o + 1] = ((uint64_t)J << 32) | I;
+    avals[o + 1] = (uint32_t)((b << 1) | 1u);
+  }
+}
+
+__global__ void k_row_segments(const uint64_t* __restrict__ akeys, size_t na, int32_t* seg_begin, int32_t* seg_end) {
+  size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= na) return;
+  uint32_t r = (uint32_t)(akeys[k] >> 32);
+  if (k == 0 || (uint32_t)(akeys[k - 1] >> 32) != r) seg_begin[r] = (int32_t)k;
+  if (k + 1 == na || (uint32_t)(akeys[k + 1] >> 32) != r) seg_end[r] = (int32_t)(k + 1);
+}
+
+__device__ __forceinline__ uint32_t kinds_of(uint64_t m) {
+  const uint64_t q0 = 0x1c71c7ull;        // rows 0-2, cols 0-2
+  const uint64_t q1 = q0 << 3;            // rows 0-2, cols 3-5
+  const uint64_t q2 = q0 << 18;           // rows 3-5, cols 0-2
+  const uint64_t q3 = q0 << 21;           // rows 3-5, cols 3-5
+  return ((m & q0) ? 1u : 0u) | ((m & q1) ? 2u : 0u) | ((m & q2) ? 4u : 0u) | ((m & q3) ? 8u : 0u);
+}
+
+// per row node: column positions of each adjacency entry in its 6 rows, row
+// lengths and group counts
+__global__ void k_row_counts(size_t n_nodes, const int32_t* __restrict__ seg_begin,
+                             const int32_t* __restrict__ seg_end, const uint32_t* __restrict__ avals,
+                             const uint64_t* __restrict__ blk_mask, const uint64_t* __restrict__ blk_maskT,
+                             int32_t* blk_colpos, int64_t* row_nnz, int64_t* gcount) {
+  size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (r >= n_nodes) return;
+  int32_t run[6] = {0, 0, 0, 0, 0, 0};
+  int64_t ng = 0;
+  int32_t s = seg_begin[r], e = seg_end[r];
+  for (int32_t k = s; k < e && s >= 0; ++k) {
+    uint32_t v = avals[k];
+    uint32_t b = v >> 1, t = v & 1u;
+    uint64_t m = t ? blk_maskT[b] : blk_mask[b];
+    for (int a = 0; a < 6; ++a) {
+      blk_colpos[(size_t)b * 12 + (t ? 6 : 0) + a] = run[a];
+      run[a] += __popcll((m >> (6 * a)) & 63ull);
+    }
+    ng += __popc(kinds_of(m));
+  }
+  for (int a = 0; a < 6; ++a) row_nnz[6 * r + a] = run[a];
+  gcount[r] = ng;
+}
+
+__global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin, const int32_t* __restrict__ seg_end,
+                           const uint64_t* __restrict__ akeys, const uint32_t* __restrict__ avals,
+                           const uint64_t* __restrict__ blk_mask, const uint64_t* __restrict__ blk_maskT,
+                           const int32_t* __restrict__ blk_colpos, const int64_t* __restrict__ row_ptr,
+                           const int64_t* __restrict__ gbase, int32_t* col_idx, int32_t* nnz_group, int32_t* g_row,
+                           int32_t* g_col, uint8_t* g_kind) {
+  size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (r >= n_nodes) return;
+  int32_t s = seg_begin[r], e = seg_end[r];
+  int64_t g = gbase[r];
+  for (int32_t k = s; k < e && s >= 0; ++k) {
+    uint32_t v = avals[k];
+    uint32_t b = v >> 1, t = v & 1u;
+    uint32_t J = (uint32_t)(akeys[k] & 0xffffffffu);
+    uint64_t m = t ? blk_maskT[b] : blk_mask[b];
+    uint32_t km = kinds_of(m);
+    int32_t kg[4] = {-1, -1, -1, -1};
+    for (int kd = 0; kd < 4; ++kd)
+      if (km & (1u << kd)) {
+        g_row[g] = (int32_t)r;
+        g_col[g] = (int32_t)J;
+        g_kind[g] = (uint8_t)kd;
+        kg[kd] = (int32_t)g;
+        ++g;
+      }
+    for (int a = 0; a < 6; ++a) {
+      int64_t pos = row_ptr[6 * r + a] + blk_colpos[(size_t)b * 12 + (t ? 6 : 0) + a];
+      uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
+      for (int c = 0; c < 6; ++c)
+        if (rowbits & (1u << c)) {
+          col_idx[pos] = (int32_t)(6 * J + c);
+          nnz_group[pos] = kg[2 * (a / 3) + c / 3];
+          ++pos;
+        }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// kernel: deterministic block reduction into CSR
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(288) k_reduce(size_t nb, const uint32_t* __restrict__ blk_start,
+                                                const uint32_t* __restrict__ blk_count,
+                                                const uint64_t* __restrict__ blk_mask,
+                                                const int32_t* __restrict__ blk_I, const int32_t* __restrict__ blk_J,
+                                                const int32_t* __restrict__ blk_colpos,
+                                                const int64_t* __restrict__ row_ptr, const double* __restrict__ V,
+                                                double* values, int* flag) {
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= nb * 36) return;
+  size_t b = t / 36;
+  int en = (int)(t - b * 36);
+  int a = en / 6, c = en - 6 * (en / 6);
+  uint32_t s = blk_start[b], n = blk_count[b];
+  const double* src = V + (size_t)s * 36 + en;
+  double sum = src[0];
+  bool nz = sum != 0.0;
+  for (uint32_t k = 1; k < n; ++k) {
+    double v = src[(size_t)k * 36];
+    nz |= v != 0.0;
+    sum = sum + v;
+  }
+  uint64_t m = blk_mask[b];
+  bool inpat = (m >> en) & 1ull;
+  if (nz != inpat) atomicOr(flag, 1);
+  if (!inpat) return;
+  int32_t I = blk_I[b], J = blk_J[b];
+  uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
+  int64_t pos = row_ptr[6 * (int64_t)I + a] + blk_colpos[b * 12 + a] + __popc(rowbits & ((1u << c) - 1u));
+  values[pos] = sum;
+  if (I != J) {
+    uint32_t colbits = 0;
+#pragma unroll
+    for (int r = 0; r < 6; ++r) colbits |= (uint32_t)((m >> (6 * r + c)) & 1ull) << r;
+    int64_t pos2 = row_ptr[6 * (int64_t)J + c] + blk_colpos[b * 12 + 6 + c] + __popc(colbits & ((1u << a) - 1u));
+    values[pos2] = sum;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------
+// Rust's {:?} for f64 (shortest round-trip digits; plain notation for
+// 1e-4 <= |v| < 1e16, else d.ddde[-]x)
+std::string rust_f64(double v) {
+  if (v != v) return "NaN";
+  if (std::isinf(v)) return v > 0 ? "inf" : "-inf";
+  if (v == 0.0) return std::signbit(v) ? "-0.0" : "0.0";
+  char buf[64];
+  for (int prec = 1; prec <= 17; ++prec) {
+    snprintf(buf, sizeof buf, "%.*e", prec - 1, v);
+    if (strtod(buf, nullptr) == v) break;
+  }
+  std::string s(buf);
+  size_t epos = s.find('e');
+  int ex = atoi(s.c_str() + epos + 1);
+  std::string mant = s.substr(0, epos);
+  bool neg = mant[0] == '-';
+  std::string digs;
+  for (char c : mant)
+    if (c >= '0' && c <= '9') digs.push_back(c);
+  double av = std::fabs(v);
+  std::string out = neg ? "-" : "";
+  if (av >= 1e-4 && av < 1e16) {
+    if (ex >= 0) {
+      for (int i = 0; i <= ex; ++i) out.push_back(i < (int)digs.size() ? digs[i] : '0');
+      out.push_back('.');
+      if (ex + 1 < (int)digs.size()) out += digs.substr(ex + 1);
+      else out.push_back('0');
+    } else {
+      out += "0.";
+      for (int i = 0; i < -ex - 1; ++i) out.push_back('0');
+      out += digs;
+    }
+  } else {
+    while (digs.size() > 1 && digs.back() == '0') digs.pop_back();
+    out.push_back(digs[0]);
+    if (digs.size() > 1) {
+      out.push_back('.');
+      out += digs.substr(1);
+    }
+    out += "e" + std::to_string(ex);
+  }
+  return out;
+}
+
+struct CoordKey {
+  uint64_t a, b, c;
+  bool operator==(const CoordKey& o) const { return a == o.a && b == o.b && c == o.c; }
+};
+struct CoordHash {
+  size_t operator()(const CoordKey& k) const {
+    uint64_t h = k.a * 0x9E3779B97F4A7C15ull ^ (k.b + 0x632BE59BD9B4E019ull) * 0xC2B2AE3D27D4EB4Full ^
+                 (k.c + 0x165667B19E3779F9ull) * 0xD6E8FEB86659FD93ull;
+    return (size_t)(h ^ (h >> 31));
+  }
+};
+CoordKey coord_key(double x, double y, double z) {
+  if (x == 0.0) x = 0.0;
+  if (y == 0.0) y = 0.0;
+  if (z == 0.0) z = 0.0;
+  CoordKey k;
+  memcpy(&k.a, &x, 8);
+  memcpy(&k.b, &y, 8);
+  memcpy(&k.c, &z, 8);
+  return k;
+}
+
+uint64_t pair_key(uint32_t a, uint32_t b) {
+  uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
+  return ((uint64_t)lo << 32) | hi;
+}
+
+struct Set4 {
+  uint32_t s[4];
+  bool operator==(const Set4& o) const { return !memcmp(s, o.s, sizeof s); }
+};
+struct Set4Hash {
+  size_t operator()(const Set4& k) const {
+    uint64_t h = 1469598103934665603ull;
+    for (int i = 0; i < 4; ++i) h = (h ^ k.s[i]) * 1099511628211ull;
+    return (size_t)h;
+  }
+};
+Set4 sorted4(const uint32_t n[4]) {
+  Set4 k;
+  memcpy(k.s, n, sizeof k.s);
+  std::sort(k.s, k.s + 4);
+  return k;
+}
+
+struct Run {
+  int kind;
+  size_t begin, count, pair_base;
+};
+
+unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// the handle
+// ---------------------------------------------------------------------------
+struct fem_gpu {
+  double rel_tol = 0, abs_tol = 0;
+  uint32_t nodes_number = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // nodes
+  size_t n_nodes = 0;
+  std::vector<uint32_t> idx_number;
+  std::unordered_map<uint32_t, int32_t> node_idx;
+  std::unordered_map<CoordKey, int32_t, CoordHash> node_coords;
+  DevBuf<double> dx, dy, dz;
+  // elements
+  std::vector<Run> runs;
+  size_t n_pairs = 0;
+  // truss
+  size_t nt = 0;
+  std::vector<uint32_t> t_num;
+  std::unordered_map<uint32_t, size_t> t_by_num;
+  std::unordered_set<uint64_t> t_pairs;
+  DevBuf<int32_t> t_n1, t_n2;
+  DevBuf<double> t_E, t_A, t_A2;
+  // beam
+  size_t nbm = 0;
+  std::vector<uint32_t> b_num;
+  std::unordered_map<uint32_t, size_t> b_by_num;
+  std::unordered_set<uint64_t> b_pairs;
+  DevBuf<int32_t> b_n1, b_n2;
+  DevBuf<double> b_E, b_nu, b_A, b_i11, b_i22, b_i12, b_it, b_ks, b_ax, b_ay, b_az;
+  // plate
+  size_t np = 0;
+  std::vector<uint32_t> p_num, p_nodes;
+  std::unordered_map<uint32_t, size_t> p_by_num;
+  std::unordered_map<Set4, int, Set4Hash> p_sets;
+  DevBuf<int32_t> p_n1, p_n2, p_n3, p_n4;
+  DevBuf<double> p_E, p_nu, p_t, p_ks;
+  // validation scratch
+  DevBuf<int> vstatus;
+  DevBuf<unsigned long long> vfirst;
+  // symbolic results
+  bool pattern_valid = false;
+  size_t n_blocks = 0;
+  DevBuf<uint32_t> slot_t, slot_b, slot_p;
+  DevBuf<uint64_t> mask_t, mask_b, mask_p;
+  DevBuf<double> V;
+  DevBuf<uint32_t> blk_start, blk_count;
+  DevBuf<uint64_t> blk_mask, blk_maskT;
+  DevBuf<int32_t> blk_I, blk_J, blk_colpos;
+  DevBuf<int64_t> row_ptr;
+  DevBuf<int32_t> col_idx;
+  DevBuf<double> values;
+  int64_t nnz = 0, n_groups = 0;
+  DevBuf<int32_t> g_row, g_col, nnz_group;
+  DevBuf<uint8_t> g_kind;
+  DevBuf<int> flag;
+  DevBuf<uint8_t> cub_tmp;
+  bool numeric_done = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  float t_elem_ms = 0, t_reduce_ms = 0;
+
+  int fail(int code, const char* fmt, ...) {
+    char b[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(b, sizeof b, fmt, ap);
+    va_end(ap);
+    err = b;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    cudaGetLastError();
+    return fail(e == cudaErrorMemoryAllocation ? FEM_GPU_ERR_OUT_OF_MEMORY : FEM_GPU_ERR_CUDA, "CUDA error in %s: %s",
+                what, cudaGetErrorString(e));
+  }
+  NodesView nodes() const { return NodesView{dx.p, dy.p, dz.p}; }
+  BeamView beams() const {
+    return BeamView{b_n1.p, b_n2.p, b_E.p, b_nu.p, b_A.p, b_i11.p, b_i22.p, b_i12.p, b_it.p, b_ks.p, b_ax.p, b_ay.p, b_az.p};
+  }
+  PlateView plates() const { return PlateView{p_n1.p, p_n2.p, p_n3.p, p_n4.p, p_E.p, p_nu.p, p_t.p, p_ks.p}; }
+  void append_run(int kind, size_t begin, size_t count) {
+    if (!count) return;
+    size_t ppe = kind == kPlate ? kPairs4 : kPairs2;
+    runs.push_back(Run{kind, begin, count, n_pairs});
+    n_pairs += count * ppe;
+    pattern_valid = false;
+    numeric_done = false;
+  }
+};
+
+#define CK(call)                                         \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return h->cuda_fail(e_, #call); \
+  } while (0)
+
+namespace {
+
+template <class T>
+cudaError_t upload(DevBuf<T>& buf, size_t at, const T* src, size_t n, cudaStream_t s) {
+  cudaError_t e = buf.reserve(at + n, s, at);
+  if (e != cudaSuccess) return e;
+  if (!n) return cudaSuccess;
+  return cudaMemcpyAsync(buf.p + at, src, n * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+// runs the validation kernel over [begin, begin+count) and returns the first
+// failing offset (or count) and its status code
+template <class Launch>
+int first_failure(fem_gpu* h, size_t count, Launch launch, size_t* first_bad, int* code) {
+  *first_bad = count;
+  *code = 0;
+  if (!count) return FEM_GPU_OK;
+  CK(h->vstatus.reserve(count, h->stream));
+  CK(h->vfirst.reserve(1, h->stream));
+  unsigned long long init = ~0ull;
+  CK(cudaMemcpyAsync(h->vfirst.p, &init, sizeof init, cudaMemcpyHostToDevice, h->stream));
+  launch(h->vstatus.p, h->vfirst.p);
+  CK(cudaGetLastError());
+  unsigned long long first = 0;
+  CK(cudaMemcpyAsync(&first, h->vfirst.p, sizeof first, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (first != ~0ull) {
+    int c = 0;
+    CK(cudaMemcpy(&c, h->vstatus.p + first, sizeof c, cudaMemcpyDeviceToHost));
+    *first_bad = (size_t)first;
+    *code = c;
+  }
+  return FEM_GPU_OK;
+}
+
+int ensure_ready(fem_gpu* h) {
+  if (!h) return FEM_GPU_ERR_ARGUMENT;
+  if (h->stream) return FEM_GPU_OK;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return h->cuda_fail(e, "cudaGetDevice");
+  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  for (auto& ev : h->ev) CK(cudaEventCreate(&ev));
+  size_t nn = h->nodes_number ? h->nodes_number : 1;
+  CK(h->dx.reserve(nn, h->stream));
+  CK(h->dy.reserve(nn, h->stream));
+  CK(h->dz.reserve(nn, h->stream));
+  CK(h->flag.reserve(1, h->stream));
+  return FEM_GPU_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" int fem_gpu_create(double rel_tol, double abs_tol, uint32_t nodes_number, fem_gpu_t** out) {
+  if (!out) return FEM_GPU_ERR_ARGUMENT;
+  fem_gpu* h = new fem_gpu();
+  h->rel_tol = rel_tol;
+  h->abs_tol = abs_tol;
+  h->nodes_number = nodes_number;
+  h->idx_number.reserve(nodes_number);
+  *out = h;
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
+  if (!h) return FEM_GPU_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  DevBuf<double>* d[] = {&h->dx, &h->dy, &h->dz, &h->t_E, &h->t_A, &h->t_A2, &h->b_E, &h->b_nu, &h->b_A,
+                         &h->b_i11, &h->b_i22, &h->b_i12, &h->b_it, &h->b_ks, &h->b_ax, &h->b_ay, &h->b_az,
+                         &h->p_E, &h->p_nu, &h->p_t, &h->p_ks, &h->V, &h->values};
+  for (auto* b : d) b->release();
+  DevBuf<int32_t>* i[] = {&h->t_n1, &h->t_n2, &h->b_n1, &h->b_n2, &h->p_n1, &h->p_n2, &h->p_n3, &h->p_n4,
+                          &h->blk_I, &h->blk_J, &h->blk_colpos, &h->col_idx, &h->g_row, &h->g_col, &h->nnz_group};
+  for (auto* b : i) b->release();
+  h->slot_t.release();
+  h->slot_b.release();
+  h->slot_p.release();
+  h->mask_t.release();
+  h->mask_b.release();
+  h->mask_p.release();
+  h->blk_start.release();
+  h->blk_count.release();
+  h->blk_mask.release();
+  h->blk_maskT.release();
+  h->row_ptr.release();
+  h->g_kind.release();
+  h->flag.release();
+  h->cub_tmp.release();
+  h->vstatus.release();
+  h->vfirst.release();
+  for (auto& ev : h->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return FEM_GPU_OK;
+}
+
+extern "C" const char* fem_gpu_last_error(const fem_gpu_t* h) { return h ? h->err.c_str() : "null handle"; }
+
+// add_node, methods_for_node_data_handle.rs:39-79
+extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const double* xyz, size_t n,
+                                 size_t* n_added) {
+  if (n_added) *n_added = 0;
+  if (!h || (n && (!numbers || !xyz))) return FEM_GPU_ERR_ARGUMENT;
+  int st = ensure_ready(h);
+  if (st) return st;
+  size_t start = h->n_nodes, k = 0;
+  int code = FEM_GPU_OK;
+  std::vector<double> xs, ys, zs;
+  xs.reserve(n);
+  ys.reserve(n);
+  zs.reserve(n);
+  for (; k < n; ++k) {
+    uint32_t num = numbers[k];
+    double x = xyz[3 * k], y = xyz[3 * k + 1], z = xyz[3 * k + 2];
+    size_t index = h->n_nodes;
+    if (h->nodes_number == 0 || index > (size_t)h->nodes_number - 1) {
+      code = h->fail(FEM_GPU_ERR_NODE_LIMIT, "Nodes number could not be greater than %u!", h->nodes_number);
+      break;
+    }
+    if (h->node_idx.count(num)) {
+      code = h->fail(FEM_GPU_ERR_NODE_NUMBER, "Node with number %u already exists!", num);
+      break;
+    }
+    if (x == x && y == y && z == z) {
+      CoordKey ck = coord_key(x, y, z);
+      if (h->node_coords.count(ck)) {
+        code = h->fail(FEM_GPU_ERR_NODE_COORDS, "Node with coordinates x: %s, y: %s, z: %s already exists!",
+                       rust_f64(x).c_str(), rust_f64(y).c_str(), rust_f64(z).c_str());
+        break;
+      }
+      h->node_coords.emplace(ck, (int32_t)index);
+    }
+    h->node_idx.emplace(num, (int32_t)index);
+    h->idx_number.push_back(num);
+    xs.push_back(x);
+    ys.push_back(y);
+    zs.push_back(z);
+    h->n_nodes++;
+  }
+  if (n_added) *n_added = k;
+  size_t m = h->n_nodes - start;
+  if (m) {
+    CK(cudaMemcpyAsync(h->dx.p + start, xs.data(), m * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->dy.p + start, ys.data(), m * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->dz.p + start, zs.data(), m * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->pattern_valid = false;
+    h->numeric_done = false;
+  }
+  return code;
+}
+
+namespace {
+int lookup_node(fem_gpu* h, uint32_t num, int32_t* idx) {
+  auto it = h->node_idx.find(num);
+  if (it == h->node_idx.end()) return h->fail(FEM_GPU_ERR_NODE_NOT_EXIST, "Node with number %u does not exist!", num);
+  *idx = it->second;
+  return FEM_GPU_OK;
+}
+}  // namespace
+
+// add_truss, methods_for_truss_data_handle.rs:32-128 and structs/truss.rs:44-64
+extern "C" int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const uint32_t* nodes, const double* young,
+                                   const double* area, const double* area2, size_t n, size_t* n_added) {
+  if (n_added) *n_added = 0;
+  if (!h || (n && (!numbers || !nodes || !young || !area))) return FEM_GPU_ERR_ARGUMENT;
+  int st = ensure_ready(h);
+  if (st) return st;
+  std::vector<int32_t> i1, i2;
+  std::vector<double> a2v;
+  i1.reserve(n);
+  i2.reserve(n);
+  a2v.reserve(n);
+  int host_code = FEM_GPU_OK;
+  std::string host_err;
+  size_t k = 0;
+  for (; k < n; ++k) {
+    uint32_t num = numbers[k], u = nodes[2 * k], v = nodes[2 * k + 1];
+    int32_t a, b;
+    if ((host_code = lookup_node(h, u, &a)) || (host_code = lookup_node(h, v, &b))) break;
+    if (h->t_by_num.count(num)) {
+      host_code = h->fail(FEM_GPU_ERR_ELEM_NUMBER, "Truss element with number %u already exists!", num);
+      break;
+    }
+    if (h->t_pairs.count(pair_key(u, v))) {
+      host_code = h->fail(FEM_GPU_ERR_ELEM_SAME_NODES, "Truss element with node number %u and %u already exists!", u, v);
+      break;
+    }
+    h->t_by_num.emplace(num, h->nt + k);
+    h->t_pairs.insert(pair_key(u, v));
+    i1.push_back(a);
+    i2.push_back(b);
+    a2v.push_back(area2 ? area2[k] : NAN);
+  }
+  if (host_code) host_err = h->err;
+  size_t m = k, base = h->nt;
+  CK(upload(h->t_n1, base, i1.data(), m, h->stream));
+  CK(upload(h->t_n2, base, i2.data(), m, h->stream));
+  CK(upload(h->t_E, base, young, m, h->stream));
+  CK(upload(h->t_A, base, area, m, h->stream));
+  CK(upload(h->t_A2, base, a2v.data(), m, h->stream));
+  size_t bad;
+  int code;
+  NodesView nd = h->nodes();
+  int32_t *n1 = h->t_n1.p, *n2 = h->t_n2.p;
+  double *E = h->t_E.p, *A = h->t_A.p, *A2 = h->t_A2.p;
+  st = first_failure(h, m, [&](int* s, unsigned long long* f) {
+    k_validate_truss<<<grid_for(m, 128), 128, 0, h->stream>>>(nd, n1, n2, E, A, A2, base, m, s, f);
+  }, &bad, &code);
+  if (st) return st;
+  size_t accepted = std::min(m, bad);
+  for (size_t j = accepted; j < m; ++j) {  // roll back registry entries past the failure
+    h->t_by_num.erase(numbers[j]);
+    h->t_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]));
+  }
+  for (size_t j = 0; j < accepted; ++j) h->t_num.push_back(numbers[j]);
+  h->nt += accepted;
+  h->append_run(kTruss, base, accepted);
+  if (n_added) *n_added = accepted;
+  if (bad < m) {
+    char b[48];
+    switch (code) {
+      case FEM_GPU_ERR_YOUNG:
+        return h->fail(code, "Young's modulus %s is less or equal to zero!", rust_f64(young[bad]).c_str());
+      case FEM_GPU_ERR_AREA: return h->fail(code, "Area %s is less or equal to zero!", rust_f64(area[bad]).c_str());
+      case FEM_GPU_ERR_AREA2:
+        return h->fail(code, "Area2 %s is less or equal to zero!", rust_f64(area2[bad]).c_str());
+      default:
+        snprintf(b, sizeof b, "%u", numbers[bad]);
+        return h->fail(code, "Truss element %s has coincident nodes %u and %u!", b, nodes[2 * bad], nodes[2 * bad + 1]);
+    }
+  }
+  if (host_code) {
+    h->err = host_err;
+    return host_code;
+  }
+  return FEM_GPU_OK;
+}
+
+// add_beam, methods_for_beam_data_handle.rs:32-142 and structs/beam.rs:63-117
+extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const uint32_t* nodes, const double* young,
+                                 const double* poisson, const double* area, const double* i11, const double* i22,
+                                 const double* i12, const double* it, const double* shear_factor,
+                                 const double* local_axis, size_t n, size_t* n_added) {
+  if (n_added) *n_added = 0;
+  if (!h || (n && (!numbers || !nodes || !young || !poisson || !area || !i11 || !i22 || !i12 || !it ||
+                   !shear_factor || !local_axis)))
+    return FEM_GPU_ERR_ARGUMENT;
+  int st = ensure_ready(h);
+  if (st) return st;
+  std::vector<int32_t> i1, i2;
+  std::vector<double> ax, ay, az;
+  int host_code = FEM_GPU_OK;
+  std::string host_err;
+  size_t k = 0;
+  for (; k < n; ++k) {
+    uint32_t num = numbers[k], u = nodes[2 * k], v = nodes[2 * k + 1];
+    int32_t a, b;
+    if ((host_code = lookup_node(h, u, &a)) || (host_code = lookup_node(h, v, &b))) break;
+    if (h->b_by_num.count(num)) {
+      host_code = h->fail(FEM_GPU_ERR_ELEM_NUMBER, "Beam element with number %u already exists!", num);
+      break;
+    }
+    if (h->b_pairs.count(pair_key(u, v))) {
+      host_code = h->fail(FEM_GPU_ERR_ELEM_SAME_NODES, "Beam element with node number %u and %u already exists!", u, v);
+      break;
+    }
+    h->b_by_num.emplace(num, h->nbm + k);
+    h->b_pairs.insert(pair_key(u, v));
+    i1.push_back(a);
+    i2.push_back(b);
+    ax.push_back(local_axis[3 * k]);
+    ay.push_back(local_axis[3 * k + 1]);
+    az.push_back(local_axis[3 * k + 2]);
+  }
+  if (host_code) host_err = h->err;
+  size_t m = k, base = h->nbm;
+  CK(upload(h->b_n1, base, i1.data(), m, h->stream));
+  CK(upload(h->b_n2, base, i2.data(), m, h->stream));
+  CK(upload(h->b_E, base, young, m, h->stream));
+  CK(upload(h->b_nu, base, poisson, m, h->stream));
+  CK(upload(h->b_A, base, area, m, h->stream));
+  CK(upload(h->b_i11, base, i11, m, h->stream));
+  CK(upload(h->b_i22, base, i22, m, h->stream));
+  CK(upload(h->b_i12, base, i12, m, h->stream));
+  CK(upload(h->b_it, base, it, m, h->stream));
+  CK(upload(h->b_ks, base, shear_factor, m, h->stream));
+  CK(upload(h->b_ax, base, ax.data(), m, h->stream));
+  CK(upload(h->b_ay, base, ay.data(), m, h->stream));
+  CK(upload(h->b_az, base, az.data(), m, h->stream));
+  size_t bad;
+  int code;
+  NodesView nd = h->nodes();
+  BeamView bv = h->beams();
+  st = first_failure(h, m, [&](int* s, unsigned long long* f) {
+    k_validate_beam<<<grid_for(m, 128), 128, 0, h->stream>>>(nd, bv, base, m, s, f);
+  }, &bad, &code);
+  if (st) return st;
+  size_t accepted = std::min(m, bad);
+  for (size_t j = accepted; j < m; ++j) {
+    h->b_by_num.erase(numbers[j]);
+    h->b_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]));
+  }
+  for (size_t j = 0; j < accepted; ++j) h->b_num.push_back(numbers[j]);
+  h->nbm += accepted;
+  h->append_run(kBeam, base, accepted);
+  if (n_added) *n_added = accepted;
+  if (bad < m) {
+    switch (code) {
+      case FEM_GPU_ERR_YOUNG:
+        return h->fail(code, "Young's modulus %s is less or equal to zero!", rust_f64(young[bad]).c_str());
+      case FEM_GPU_ERR_POISSON:  // beam.rs:84 reports the Young's modulus value
+        return h->fail(code, "Poisson's ratio %s is less or equal to zero!", rust_f64(young[bad]).c_str());
+      case FEM_GPU_ERR_AREA: return h->fail(code, "Area %s is less or equal to zero!", rust_f64(area[bad]).c_str());
+      case FEM_GPU_ERR_I11: return h->fail(code, "I11 %s is less or equal to zero!", rust_f64(i11[bad]).c_str());
+      case FEM_GPU_ERR_I22: return h->fail(code, "I22 %s is less or equal to zero!", rust_f64(i22[bad]).c_str());
+      case FEM_GPU_ERR_IT: return h->fail(code, "It %s is less or equal to zero!", rust_f64(it[bad]).c_str());
+      case FEM_GPU_ERR_SHEAR_FACTOR:
+        return h->fail(code, "Shear factor %s is less or equal to zero!", rust_f64(shear_factor[bad]).c_str());
+      case FEM_GPU_ERR_PARALLEL_AXIS:
+        return h->fail(code, "Local axis 1 direction [%s, %s, %s] parallel to element %u!",
+                       rust_f64(local_axis[3 * bad]).c_str(), rust_f64(local_axis[3 * bad + 1]).c_str(),
+                       rust_f64(local_axis[3 * bad + 2]).c_str(), numbers[bad]);
+      default:
+        return h->fail(code, "Beam element %u has coincident nodes %u and %u!", numbers[bad], nodes[2 * bad],
+                       nodes[2 * bad + 1]);
+    }
+  }
+  if (host_code) {
+    h->err = host_err;
+    return host_code;
+  }
+  return FEM_GPU_OK;
+}
+
+// add_plate, methods_for_plate_data_handle.rs:33-217 and structs/plate.rs:58-158
+extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const uint32_t* nodes, const double* young,
+                                  const double* poisson, const double* thickness, const double* shear_factor,
+                                  size_t n, size_t* n_added) {
+  if (n_added) *n_added = 0;
+  if (!h || (n && (!numbers || !nodes || !young || !poisson || !thickness || !shear_factor)))
+    return FEM_GPU_ERR_ARGUMENT;
+  int st = ensure_ready(h);
+  if (st) return st;
+  std::vector<int32_t> id[4];
+  for (auto& v : id) v.reserve(n);
+  int host_code = FEM_GPU_OK;
+  std::string host_err;
+  size_t k = 0;
+  for (; k < n; ++k) {
+    uint32_t num = numbers[k];
+    const uint32_t* nn = nodes + 4 * k;
+    int32_t ix[4];
+    bool okn = true;
+    for (int q = 0; q < 4 && okn; ++q)
+      if ((host_code = lookup_node(h, nn[q], &ix[q]))) okn = false;
+    if (!okn) break;
+    if (h->p_by_num.count(num)) {
+      host_code = h->fail(FEM_GPU_ERR_ELEM_NUMBER, "Plate element with number %u already exists!", num);
+      break;
+    }
+    // Plate::is_nodes_numbers_same (plate.rs:1107-1118): every given number belongs to an existing plate
+    bool distinct = nn[0] != nn[1] && nn[0] != nn[2] && nn[0] != nn[3] && nn[1] != nn[2] && nn[1] != nn[3] &&
+                    nn[2] != nn[3];
+    bool same = false;
+    if (distinct) {
+      same = h->p_sets.count(sorted4(nn)) > 0;
+    } else {
+      for (size_t e = 0; e < h->p_num.size() + k && !same; ++e) {
+        const uint32_t* mm = e < h->p_num.size() ? &h->p_nodes[4 * e] : nodes + 4 * (e - h->p_num.size());
+        bool all = true;
+        for (int q = 0; q < 4 && all; ++q) all = nn[q] == mm[0] || nn[q] == mm[1] || nn[q] == mm[2] || nn[q] == mm[3];
+        same = all;
+      }
+    }
+    if (same) {
+      host_code = h->fail(FEM_GPU_ERR_ELEM_SAME_NODES, "Plate element with nodes numbers [%u, %u, %u, %u] already exists!",
+                          nn[0], nn[1], nn[2], nn[3]);
+      break;
+    }
+    h->p_by_num.emplace(num, h->np + k);
+    h->p_sets[sorted4(nn)] += 1;
+    for (int q = 0; q < 4; ++q) id[q].push_back(ix[q]);
+  }
+  if (host_code) host_err = h->err;
+  size_t m = k, base = h->np;
+  CK(upload(h->p_n1, base, id[0].data(), m, h->stream));
+  CK(upload(h->p_n2, base, id[1].data(), m, h->stream));
+  CK(upload(h->p_n3, base, id[2].data(), m, h->stream));
+  CK(upload(h->p_n4, base, id[3].data(), m, h->stream));
+  CK(upload(h->p_E, base, young, m, h->stream));
+  CK(upload(h->p_nu, base, poisson, m, h->stream));
+  CK(upload(h->p_t, base, thickness, m, h->stream));
+  CK(upload(h->p_ks, base, shear_factor, m, h->stream));
+  size_t bad;
+  int code;
+  NodesView nd = h->nodes();
+  PlateView pv = h->plates();
+  double abs_tol = h->abs_tol;
+  st = first_failure(h, m, [&](int* s, unsigned long long* f) {
+    k_validate_plate<<<grid_for(m, 128), 128, 0, h->stream>>>(nd, pv, abs_tol, base, m, s, f);
+  }, &bad, &code);
+  if (st) return st;
+  size_t accepted = std::min(m, bad);
+  for (size_t j = accepted; j < m; ++j) {
+    h->p_by_num.erase(numbers[j]);
+    auto it2 = h->p_sets.find(sorted4(nodes + 4 * j));
+    if (it2 != h->p_sets.end() && --it2->second == 0) h->p_sets.erase(it2);
+  }
+  for (size_t j = 0; j < accepted; ++j) {
+    h->p_num.push_back(numbers[j]);
+    for (int q = 0; q < 4; ++q) h->p_nodes.push_back(nodes[4 * j + q]);
+  }
+  h->np += accepted;
+  h->append_run(kPlate, base, accepted);
+  if (n_added) *n_added = accepted;
+  if (bad < m) {
+    switch (code) {
+      case FEM_GPU_ERR_YOUNG:
+        return h->fail(code, "Young's modulus %s is less or equal to zero!", rust_f64(young[bad]).c_str());
+      case FEM_GPU_ERR_POISSON:  // plate.rs:79 reports the Young's modulus value
+        return h->fail(code, "Poisson's ratio %s is less or equal to zero!", rust_f64(young[bad]).c_str());
+      case FEM_GPU_ERR_THICKNESS:  // plate.rs:82 reports the Young's modulus value
+        return h->fail(code, "Thickness %s is less or equal to zero!", rust_f64(young[bad]).c_str());
+      case FEM_GPU_ERR_SHEAR_FACTOR:
+        return h->fail(code, "Shear factor %s is less or equal to zero!", rust_f64(shear_factor[bad]).c_str());
+      case FEM_GPU_ERR_NODES_ON_LINE: return h->fail(code, "Some nodes of %u element lie on the line!", numbers[bad]);
+      case FEM_GPU_ERR_NOT_ON_PLANE: return h->fail(code, "Not all nodes of element %u lie on the plane!", numbers[bad]);
+      default: return h->fail(code, "Element %u non-convex!", numbers[bad]);
+    }
+  }
+  if (host_code) {
+    h->err = host_err;
+    return host_code;
+  }
+  return FEM_GPU_OK;
+}
+
+namespace {
+
+int launch_elements(fem_gpu* h, BlockSink sink_t, BlockSink sink_b, BlockSink sink_p) {
+  NodesView nd = h->nodes();
+  if (h->nt)
+    k_truss<<<grid_for(h->nt, 128), 128, 0, h->stream>>>(nd, h->t_n1.p, h->t_n2.p, h->t_E.p, h->t_A.p, h->t_A2.p,
+                                                         h->abs_tol, h->nt, sink_t);
+  if (h->nbm)
+    k_beam<<<grid_for(h->nbm, 128), 128, 0, h->stream>>>(nd, h->beams(), h->rel_tol, h->abs_tol, h->nbm, sink_b);
+  if (h->np) k_plate<<<grid_for(h->np, 128), 128, 0, h->stream>>>(nd, h->plates(), h->abs_tol, h->np, sink_p);
+  CK(cudaGetLastError());
+  return FEM_GPU_OK;
+}
+
+int numeric_launch(fem_gpu* h) {
+  CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->stream));
+  CK(cudaEventRecord(h->ev[0], h->stream));
+  BlockSink st{nullptr, h->V.p, h->slot_t.p}, sb{nullptr, h->V.p, h->slot_b.p}, sp{nullptr, h->V.p, h->slot_p.p};
+  int r = launch_elements(h, st, sb, sp);
+  if (r) return r;
+  CK(cudaEventRecord(h->ev[1], h->stream));
+  if (h->n_blocks)
+    k_reduce<<<grid_for(h->n_blocks * 36, 288), 288, 0, h->stream>>>(
+        h->n_blocks, h->blk_start.p, h->blk_count.p, h->blk_mask.p, h->blk_I.p, h->blk_J.p, h->blk_colpos.p,
+        h->row_ptr.p, h->V.p, h->values.p, h->flag.p);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(h->ev[2], h->stream));
+  h->numeric_done = true;
+  return FEM_GPU_OK;
+}
+
+template <class F>
+int cub_call(fem_gpu* h, F f) {
+  size_t bytes = 0;
+  CK(f((void*)nullptr, bytes));
+  CK(h->cub_tmp.reserve(bytes ? bytes : 1, h->stream));
+  CK(f((void*)h->cub_tmp.p, bytes));
+  return FEM_GPU_OK;
+}
+
+int symbolic(fem_gpu* h) {
+  cudaStream_t s = h->stream;
+  size_t np = h->n_pairs;
+  const size_t nrows = (size_t)h->nodes_number * 6;
+  CK(h->row_ptr.reserve(nrows + 1, s));
+  h->n_blocks = 0;
+  h->nnz = 0;
+  h->n_groups = 0;
+  if (np == 0) {
+    CK(cudaMemsetAsync(h->row_ptr.p, 0, (nrows + 1) * sizeof(int64_t), s));
+    CK(cudaStreamSynchronize(s));
+    h->pattern_valid = true;
+    return FEM_GPU_OK;
+  }
+  // 1. pair keys in call order
+  DevBuf<uint64_t> keys, skeys;
+  DevBuf<uint32_t> vals, svals;
+  CK(keys.reserve(np, s));
+  CK(skeys.reserve(np, s));
+  CK(vals.reserve(np, s));
+  CK(svals.reserve(np, s));
+  for (const Run& r : h->runs) {
+    if (r.kind == kTruss)
+      k_gen_pairs<<<grid_for(r.count, 256), 256, 0, s>>>(kTruss, h->t_n1.p, h->t_n2.p, nullptr, nullptr, r.begin,
+                                                         r.count, r.pair_base, keys.p, vals.p);
+    else if (r.kind == kBeam)
+      k_gen_pairs<<<grid_for(r.count, 256), 256, 0, s>>>(kBeam, h->b_n1.p, h->b_n2.p, nullptr, nullptr, r.begin,
+                                                         r.count, r.pair_base, keys.p, vals.p);
+    else
+      k_gen_pairs<<<grid_for(r.count, 256), 256, 0, s>>>(kPlate, h->p_n1.p, h->p_n2.p, h->p_n3.p, h->p_n4.p,
+                                                         r.begin, r.count, r.pair_base, keys.p, vals.p);
+  }
+  CK(cudaGetLastError());
+  // 2. per-pair non-zero masks from the element arithmetic
+  CK(h->mask_t.reserve(h->nt * kPairs2 + 1, s));
+  CK(h->mask_b.reserve(h->nbm * kPairs2 + 1, s));
+  CK(h->mask_p.reserve(h->np * kPairs4 + 1, s));
+  {
+    BlockSink st{h->mask_t.p, nullptr, nullptr}, sb{h->mask_b.p, nullptr, nullptr}, sp{h->mask_p.p, nullptr, nullptr};
+    int r = launch_elements(h, st, sb, sp);
+    if (r) return r;
+  }
+  // 3. stable sort by node-pair key (call order preserved within a block)
+  int st = cub_call(h, [&](void* tmp, size_t& bytes) {
+    return cub::DeviceRadixSort::SortPairs(tmp, bytes, keys.p, skeys.p, vals.p, svals.p, (int64_t)np, 0, 64, s);
+  });
+  if (st) return st;
+  // 4. slots and sorted masks
+  CK(h->slot_t.reserve(h->nt * kPairs2 + 1, s));
+  CK(h->slot_b.reserve(h->nbm * kPairs2 + 1, s));
+  CK(h->slot_p.reserve(h->np * kPairs4 + 1, s));
+  DevBuf<uint64_t> smask;
+  CK(smask.reserve(np, s));
+  k_scatter_slots<<<grid_for(np, 256), 256, 0, s>>>(svals.p, np, h->slot_t.p, h->slot_b.p, h->slot_p.p, h->mask_t.p,
+                                                     h->mask_b.p, h->mask_p.p, smask.p);
+  // 5. blocks
+  DevBuf<uint32_t> head, incl;
+  CK(head.reserve(np, s));
+  CK(incl.reserve(np, s));
+  k_heads<<<grid_for(np, 256), 256, 0, s>>>(skeys.p, np, head.p);
+  st = cub_call(h, [&](void* tmp, size_t& bytes) {
+    return cub::DeviceScan::InclusiveSum(tmp, bytes, head.p, incl.p, (int64_t)np, s);
+  });
+  if (st) return st;
+  uint32_t nb32 = 0;
+  CK(cudaMemcpyAsync(&nb32, incl.p + np - 1, sizeof nb32, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  size_t nb = nb32;
+  h->n_blocks = nb;
+  CK(h->blk_start.reserve(nb, s));
+  CK(h->blk_count.reserve(nb, s));
+  CK(h->blk_mask.reserve(nb, s));
+  CK(h->blk_maskT.reserve(nb, s));
+  CK(h->blk_I.reserve(nb, s));
+  CK(h->blk_J.reserve(nb, s));
+  CK(h->blk_colpos.reserve(nb * 12, s));
+  k_block_starts<<<grid_for(np, 256), 256, 0, s>>>(incl.p, np, h->blk_start.p);
+  DevBuf<uint32_t> adj_n, adj_off;
+  CK(adj_n.reserve(nb, s));
+  CK(adj_off.reserve(nb, s));
+  k_block_meta<<<grid_for(nb, 256), 256, 0, s>>>(h->blk_start.p, nb, np, skeys.p, smask.p, h->blk_count.p,
+                                                 h->blk_mask.p, h->blk_maskT.p, h->blk_I.p, h->blk_J.p, adj_n.p);
+  st = cub_call(h, [&](void* tmp, size_t& bytes) {
+    return cub::DeviceScan::ExclusiveSum(tmp, bytes, adj_n.p, adj_off.p, (int64_t)nb, s);
+  });
+  if (st) return st;
+  uint32_t last_off = 0, last_n = 0;
+  CK(cudaMemcpyAsync(&last_off, adj_off.p + nb - 1, sizeof last_off, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&last_n, adj_n.p + nb - 1, sizeof last_n, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  size_t na = (size_t)last_off + last_n;
+  // 6. row-node adjacency sorted by (row node, col node)
+  DevBuf<uint64_t> akeys, sakeys;
+  DevBuf<uint32_t> avals, savals;
+  CK(akeys.reserve(na, s));
+  CK(sakeys.reserve(na, s));
+  CK(avals.reserve(na, s));
+  CK(savals.reserve(na, s));
+  k_adjacency<<<grid_for(nb, 256), 256, 0, s>>>(adj_off.p, nb, h->blk_I.p, h->blk_J.p, akeys.p, avals.p);
+  st = cub_call(h, [&](void* tmp, size_t& bytes) {
+    return cub::DeviceRadixSort::SortPairs(tmp, bytes, akeys.p, sakeys.p, avals.p, savals.p, (int64_t)na, 0, 64, s);
+  });
+  if (st) return st;
+  size_t nn = h->nodes_number;
+  DevBuf<int32_t> seg_b, seg_e;
+  DevBuf<int64_t> row_nnz, gcount, gbase;
+  CK(seg_b.reserve(nn, s));
+  CK(seg_e.reserve(nn, s));
+  CK(row_nnz.reserve(nrows + 1, s));
+  CK(gcount.reserve(nn + 1, s));
+  CK(gbase.reserve(nn + 1, s));
+  CK(cudaMemsetAsync(seg_b.p, 0xff, nn * sizeof(int32_t), s));
+  CK(cudaMemsetAsync(seg_e.p, 0xff, nn * sizeof(int32_t), s));
+  CK(cudaMemsetAsync(row_nnz.p, 0, (nrows + 1) * sizeof(int64_t), s));
+  CK(cudaMemsetAsync(gcount.p, 0, (nn + 1) * sizeof(int64_t), s));
+  k_row_segments<<<grid_for(na, 256), 256, 0, s>>>(sakeys.p, na, seg_b.p, seg_e.p);
+  k_row_counts<<<grid_for(nn, 128), 128, 0, s>>>(nn, seg_b.p, seg_e.p, savals.p, h->blk_mask.p, h->blk_maskT.p,
+                                                 h->blk_colpos.p, row_nnz.p, gcount.p);
+  st = cub_call(h, [&](void* tmp, size_t& bytes) {
+    return cub::DeviceScan::ExclusiveSum(tmp, bytes, row_nnz.p, h->row_ptr.p, (int64_t)(nrows + 1), s);
+  });
+  if (st) return st;
+  st = cub_call(h, [&](void* tmp, size_t& bytes) {
+    return cub::DeviceScan::ExclusiveSum(tmp, bytes, gcount.p, gbase.p, (int64_t)(nn + 1), s);
+  });
+  if (st) return st;
+  int64_t nnz = 0, ng = 0;
+  CK(cudaMemcpyAsync(&nnz, h->row_ptr.p + nrows, sizeof nnz, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&ng, gbase.p + nn, sizeof ng, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  h->nnz = nnz;
+  h->n_groups = ng;
+  CK(h->col_idx.reserve(nnz + 1, s));
+  CK(h->values.reserve(nnz + 1, s));
+  CK(h->nnz_group.reserve(nnz + 1, s));
+  CK(h->g_row.reserve(ng + 1, s));
+  CK(h->g_col.reserve(ng + 1, s));
+  CK(h->g_kind.reserve(ng + 1, s));
+  k_row_fill<<<grid_for(nn, 128), 128, 0, s>>>(nn, seg_b.p, seg_e.p, sakeys.p, savals.p, h->blk_mask.p,
+                                               h->blk_maskT.p, h->blk_colpos.p, h->row_ptr.p, gbase.p, h->col_idx.p,
+                                               h->nnz_group.p, h->g_row.p, h->g_col.p, h->g_kind.p);
+  CK(cudaGetLastError());
+  CK(h->V.reserve(np * 36, s));
+  CK(cudaStreamSynchronize(s));
+  // temporaries
+  keys.release();
+  skeys.release();
+  vals.release();
+  svals.release();
+  smask.release();
+  head.release();
+  incl.release();
+  adj_n.release();
+  adj_off.release();
+  akeys.release();
+  sakeys.release();
+  avals.release();
+  savals.release();
+  seg_b.release();
+  seg_e.release();
+  row_nnz.release();
+  gcount.release();
+  gbase.release();
+  h->pattern_valid = true;
+  return FEM_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" int fem_gpu_assemble(fem_gpu_t* h) {
+  int st = ensure_ready(h);
+  if (st) return st;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    if (!h->pattern_valid) {
+      st = symbolic(h);
+      if (st) return st;
+    }
+    st = numeric_launch(h);
+    if (st) return st;
+    int flag = 0;
+    CK(cudaMemcpyAsync(&flag, h->flag.p, sizeof flag, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaEventElapsedTime(&h->t_elem_ms, h->ev[0], h->ev[1]));
+    CK(cudaEventElapsedTime(&h->t_reduce_ms, h->ev[1], h->ev[2]));
+    if (!flag) return FEM_GPU_OK;
+    h->pattern_valid = false;  // a coordinate/property update changed the exact-zero pattern
+  }
+  return h->fail(FEM_GPU_ERR_PATTERN_CHANGED, "pattern changed twice in one assemble");
+}
+
+extern "C" int fem_gpu_assemble_numeric_async(fem_gpu_t* h) {
+  if (!h) return FEM_GPU_ERR_ARGUMENT;
+  if (!h->pattern_valid) return h->fail(FEM_GPU_ERR_STATE, "no valid pattern: call fem_gpu_assemble first");
+  return numeric_launch(h);
+}
+
+extern "C" int fem_gpu_check_pattern(fem_gpu_t* h) {
+  if (!h || !h->stream) return FEM_GPU_ERR_ARGUMENT;
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, h->flag.p, sizeof flag, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (flag) {
+    h->pattern_valid = false;
+    return h->fail(FEM_GPU_ERR_PATTERN_CHANGED, "the exact-zero pattern changed; call fem_gpu_assemble");
+  }
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_set_node_coordinates(fem_gpu_t* h, const double* xyz, size_t n_nodes) {
+  if (!h || !xyz || n_nodes != h->n_nodes) return FEM_GPU_ERR_ARGUMENT;
+  int st = ensure_ready(h);
+  if (st) return st;
+  std::vector<double> a(n_nodes), b(n_nodes), c(n_nodes);
+  for (size_t i = 0; i < n_nodes; ++i) {
+    a[i] = xyz[3 * i];
+    b[i] = xyz[3 * i + 1];
+    c[i] = xyz[3 * i + 2];
+  }
+  CK(cudaMemcpyAsync(h->dx.p, a.data(), n_nodes * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->dy.p, b.data(), n_nodes * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->dz.p, c.data(), n_nodes * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->numeric_done = false;
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_set_plate_properties(fem_gpu_t* h, const double* young, const double* poisson,
+                                            const double* thickness, const double* shear_factor, size_t n) {
+  if (!h || n != h->np || !young || !poisson || !thickness || !shear_factor) return FEM_GPU_ERR_ARGUMENT;
+  CK(cudaMemcpyAsync(h->p_E.p, young, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->p_nu.p, poisson, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->p_t.p, thickness, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->p_ks.p, shear_factor, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->numeric_done = false;
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_get_csr_sizes(fem_gpu_t* h, int64_t* n_rows, int64_t* nnz) {
+  if (!h) return FEM_GPU_ERR_ARGUMENT;
+  if (!h->numeric_done || !h->pattern_valid) return h->fail(FEM_GPU_ERR_STATE, "call fem_gpu_assemble first");
+  if (n_rows) *n_rows = (int64_t)h->nodes_number * 6;
+  if (nnz) *nnz = h->nnz;
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_get_csr(fem_gpu_t* h, int64_t* row_ptr, int32_t* col_idx, double* values) {
+  int st = fem_gpu_get_csr_sizes(h, nullptr, nullptr);
+  if (st) return st;
+  size_t nrows = (size_t)h->nodes_number * 6;
+  if (row_ptr) CK(cudaMemcpyAsync(row_ptr, h->row_ptr.p, (nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
+  if (col_idx && h->nnz)
+    CK(cudaMemcpyAsync(col_idx, h->col_idx.p, h->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  if (values && h->nnz)
+    CK(cudaMemcpyAsync(values, h->values.p, h->nnz * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_get_csr_values(fem_gpu_t* h, double* values) { return fem_gpu_get_csr(h, nullptr, nullptr, values); }
+
+extern "C" int fem_gpu_get_csr_device(fem_gpu_t* h, const int64_t** row_ptr, const int32_t** col_idx,
+                                      const double** values) {
+  int st = fem_gpu_get_csr_sizes(h, nullptr, nullptr);
+  if (st) return st;
+  if (row_ptr) *row_ptr = h->row_ptr.p;
+  if (col_idx) *col_idx = h->col_idx.p;
+  if (values) *values = h->values.p;
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_get_node_count(fem_gpu_t* h, int64_t* n_nodes) {
+  if (!h || !n_nodes) return FEM_GPU_ERR_ARGUMENT;
+  *n_nodes = (int64_t)h->n_nodes;
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_get_index_node_numbers(fem_gpu_t* h, uint32_t* numbers) {
+  if (!h || (!numbers && h->n_nodes)) return FEM_GPU_ERR_ARGUMENT;
+  if (h->n_nodes) memcpy(numbers, h->idx_number.data(), h->n_nodes * sizeof(uint32_t));
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_get_group_count(fem_gpu_t* h, int64_t* n_groups) {
+  if (!h || !n_groups) return FEM_GPU_ERR_ARGUMENT;
+  if (!h->pattern_valid) return h->fail(FEM_GPU_ERR_STATE, "call fem_gpu_assemble first");
+  *n_groups = h->n_groups;
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_get_groups(fem_gpu_t* h, int32_t* row_node, int32_t* col_node, uint8_t* kind,
+                                  int32_t* nnz_group) {
+  if (!h) return FEM_GPU_ERR_ARGUMENT;
+  if (!h->pattern_valid) return h->fail(FEM_GPU_ERR_STATE, "call fem_gpu_assemble first");
+  size_t ng = (size_t)h->n_groups, nz = (size_t)h->nnz;
+  if (row_node && ng) CK(cudaMemcpyAsync(row_node, h->g_row.p, ng * 4, cudaMemcpyDeviceToHost, h->stream));
+  if (col_node && ng) CK(cudaMemcpyAsync(col_node, h->g_col.p, ng * 4, cudaMemcpyDeviceToHost, h->stream));
+  if (kind && ng) CK(cudaMemcpyAsync(kind, h->g_kind.p, ng, cudaMemcpyDeviceToHost, h->stream));
+  if (nnz_group && nz) CK(cudaMemcpyAsync(nnz_group, h->nnz_group.p, nz * 4, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return FEM_GPU_OK;
+}
+
+namespace {
+int rotation_of(fem_gpu* h, int kind, uint32_t number, double* r9) {
+  if (!h || !r9) return FEM_GPU_ERR_ARGUMENT;
+  const std::unordered_map<uint32_t, size_t>& m = kind == kTruss ? h->t_by_num : kind == kBeam ? h->b_by_num : h->p_by_num;
+  auto it = m.find(number);
+  const char* nm = kind == kTruss ? "Truss" : kind == kBeam ? "Beam" : "Plate";
+  if (it == m.end()) return h->fail(FEM_GPU_ERR_ARGUMENT, "%s element with number %u does not exist!", nm, number);
+  DevBuf<double> out;
+  CK(out.reserve(9, h->stream));
+  if (kind == kTruss)
+    k_rotation<<<1, 1, 0, h->stream>>>(kind, h->nodes(), h->t_n1.p, h->t_n2.p, nullptr, nullptr, h->beams(), h->rel_tol,
+                                       h->abs_tol, it->second, out.p);
+  else if (kind == kBeam)
+    k_rotation<<<1, 1, 0, h->stream>>>(kind, h->nodes(), nullptr, nullptr, nullptr, nullptr, h->beams(), h->rel_tol,
+                                       h->abs_tol, it->second, out.p);
+  else
+    k_rotation<<<1, 1, 0, h->stream>>>(kind, h->nodes(), h->p_n1.p, h->p_n2.p, h->p_n3.p, h->p_n4.p, h->beams(),
+                                       h->rel_tol, h->abs_tol, it->second, out.p);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(r9, out.p, 9 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  out.release();
+  return FEM_GPU_OK;
+}
+}  // namespace
+
+extern "C" int fem_gpu_get_truss_rotation(fem_gpu_t* h, uint32_t number, double* r9) {
+  return rotation_of(h, kTruss, number, r9);
+}
+extern "C" int fem_gpu_get_beam_rotation(fem_gpu_t* h, uint32_t number, double* r9) {
+  return rotation_of(h, kBeam, number, r9);
+}
+extern "C" int fem_gpu_get_plate_rotation(fem_gpu_t* h, uint32_t number, double* r9) {
+  return rotation_of(h, kPlate, number, r9);
+}
+
+extern "C" int fem_gpu_get_element_counts(fem_gpu_t* h, int64_t* n_truss, int64_t* n_beam, int64_t* n_plate) {
+  if (!h) return FEM_GPU_ERR_ARGUMENT;
+  if (n_truss) *n_truss = (int64_t)h->nt;
+  if (n_beam) *n_beam = (int64_t)h->nbm;
+  if (n_plate) *n_plate = (int64_t)h->np;
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_get_stream(fem_gpu_t* h, void** stream) {
+  if (!h || !stream) return FEM_GPU_ERR_ARGUMENT;
+  int st = ensure_ready(h);
+  if (st) return st;
+  *stream = (void*)h->stream;
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_numeric_launch_count(fem_gpu_t* h, int* n_launches) {
+  if (!h || !n_launches) return FEM_GPU_ERR_ARGUMENT;
+  *n_launches = (h->nt ? 1 : 0) + (h->nbm ? 1 : 0) + (h->np ? 1 : 0) + (h->n_blocks ? 1 : 0);
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_last_numeric_timing(fem_gpu_t* h, float* element_ms, float* reduce_ms) {
+  if (!h) return FEM_GPU_ERR_ARGUMENT;
+  if (!h->numeric_done) return h->fail(FEM_GPU_ERR_STATE, "no numeric pass yet");
+  CK(cudaEventSynchronize(h->ev[2]));
+  CK(cudaEventElapsedTime(&h->t_elem_ms, h->ev[0], h->ev[1]));
+  CK(cudaEventElapsedTime(&h->t_reduce_ms, h->ev[1], h->ev[2]));
+  if (element_ms) *element_ms = h->t_elem_ms;
+  if (reduce_ms) *reduce_ms = h->t_reduce_ms;
+  return FEM_GPU_OK;
+}

@@ -1,0 +1,153 @@
+/*
+ * fem_gpu.h -- C ABI of the GB300 (sm_103a) element-stiffness-and-assembly
+ * library.  Drop-in for the eager assembly path of the Rust crate
+ * `finite_element_method` 0.9.12:
+ *
+ *   FEM::create(rel_tol, abs_tol, nodes_number)   src/fem/fem.rs:34-65
+ *   FEM::add_node                                  src/fem/methods_for_node_data_handle.rs:66-79
+ *   FEM::add_truss                                 src/fem/methods_for_truss_data_handle.rs:49-128
+ *   FEM::add_beam                                  src/fem/methods_for_beam_data_handle.rs:49-142
+ *   FEM::add_plate                                 src/fem/methods_for_plate_data_handle.rs:62-217
+ *   FEM.stiffness_matrix (read by the separation)  src/fem/fem.rs:17, :71-73
+ *   get_{truss,beam,plate}_rotation_matrix_elements src/fem/fem.rs:171-202
+ *
+ * The reference assembles eagerly inside each add_*; here add_* validates the
+ * element on the GPU (same checks, same messages, same "first failure wins,
+ * model unchanged by the failing element" behaviour) and records it, and
+ * fem_gpu_assemble() builds the CSR global stiffness in one pass.  Results are
+ * the reference's: the CSR pattern is the set of (row, col) that received a
+ * non-zero element contribution, values are summed per entry in element call
+ * order.  Everything is FP64.
+ *
+ * Conventions: every function returns 0 on success or a FEM_GPU_* code; the
+ * message of the last failure is fem_gpu_last_error(h).  A handle owns its
+ * device buffers and one CUDA stream; it is not thread-safe.  Host pointers are
+ * plain host memory (pinned or pageable); *_device getters return device
+ * pointers owned by the handle, valid until the next call that changes the
+ * model.  No CPU fallback exists: without a CUDA device every call that needs
+ * one returns FEM_GPU_ERR_CUDA.
+ */
+#ifndef FEM_GPU_H
+#define FEM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fem_gpu fem_gpu_t;
+
+enum {
+  FEM_GPU_OK = 0,
+  FEM_GPU_ERR_NODE_LIMIT = 1,      /* "Nodes number could not be greater than N!" */
+  FEM_GPU_ERR_NODE_NUMBER = 2,     /* "Node with number N already exists!" */
+  FEM_GPU_ERR_NODE_INDEX = 3,
+  FEM_GPU_ERR_NODE_COORDS = 4,     /* "Node with coordinates x: .., y: .., z: .. already exists!" */
+  FEM_GPU_ERR_NODE_NOT_EXIST = 5,  /* "Node with number N does not exist!" */
+  FEM_GPU_ERR_ELEM_NUMBER = 6,     /* "<Kind> element with number N already exists!" */
+  FEM_GPU_ERR_ELEM_SAME_NODES = 7,
+  FEM_GPU_ERR_YOUNG = 8,
+  FEM_GPU_ERR_POISSON = 9,
+  FEM_GPU_ERR_AREA = 10,
+  FEM_GPU_ERR_AREA2 = 11,
+  FEM_GPU_ERR_I11 = 12,
+  FEM_GPU_ERR_I22 = 13,
+  FEM_GPU_ERR_IT = 14,
+  FEM_GPU_ERR_SHEAR_FACTOR = 15,
+  FEM_GPU_ERR_PARALLEL_AXIS = 16,
+  FEM_GPU_ERR_THICKNESS = 17,
+  FEM_GPU_ERR_NODES_ON_LINE = 18,
+  FEM_GPU_ERR_NOT_ON_PLANE = 19,
+  FEM_GPU_ERR_NOT_CONVEX = 20,
+  FEM_GPU_ERR_ZERO_LENGTH = 21,    /* two-node element whose nodes coincide */
+  FEM_GPU_ERR_ARGUMENT = 30,       /* null pointer / size out of range */
+  FEM_GPU_ERR_STATE = 31,          /* e.g. CSR requested before fem_gpu_assemble */
+  FEM_GPU_ERR_CUDA = 40,           /* CUDA runtime failure or no device */
+  FEM_GPU_ERR_OUT_OF_MEMORY = 41,
+  FEM_GPU_ERR_PATTERN_CHANGED = 42 /* numeric pass saw a non-zero outside the stored pattern */
+};
+
+/* FEM::create (fem.rs:34).  Allocates nothing on the device until the first add. */
+int fem_gpu_create(double rel_tol, double abs_tol, uint32_t nodes_number, fem_gpu_t** out);
+int fem_gpu_destroy(fem_gpu_t* h);
+const char* fem_gpu_last_error(const fem_gpu_t* h);
+
+/* FEM::add_node (methods_for_node_data_handle.rs:66), n of them in order.
+ * xyz is n x 3 row-major.  Stops at the first failure; *n_added (optional)
+ * receives how many were added before it. */
+int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const double* xyz, size_t n, size_t* n_added);
+
+/* FEM::add_truss (methods_for_truss_data_handle.rs:49).  nodes is n x 2 node
+ * numbers; area2 may be NULL, or hold NaN for "None" per element. */
+int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const uint32_t* nodes, const double* young,
+                        const double* area, const double* area2, size_t n, size_t* n_added);
+
+/* FEM::add_beam (methods_for_beam_data_handle.rs:49); local_axis is n x 3. */
+int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const uint32_t* nodes, const double* young,
+                      const double* poisson, const double* area, const double* i11, const double* i22,
+                      const double* i12, const double* it, const double* shear_factor, const double* local_axis,
+                      size_t n, size_t* n_added);
+
+/* FEM::add_plate (methods_for_plate_data_handle.rs:62); nodes is n x 4. */
+int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const uint32_t* nodes, const double* young,
+                       const double* poisson, const double* thickness, const double* shear_factor, size_t n,
+                       size_t* n_added);
+
+/* Build the global stiffness: the symbolic phase (pattern, DOF map, groups and
+ * the destination map) when the element set changed, then the numeric phase.
+ * Synchronous; returns after the CSR is complete on the device. */
+int fem_gpu_assemble(fem_gpu_t* h);
+
+/* Numeric phase only, enqueued on the handle's stream without synchronising
+ * (requires a prior fem_gpu_assemble).  For timing loops and graph capture.
+ * fem_gpu_check_pattern() synchronises and reports whether the last numeric
+ * pass found the stored pattern still exact (0) or changed (PATTERN_CHANGED). */
+int fem_gpu_assemble_numeric_async(fem_gpu_t* h);
+int fem_gpu_check_pattern(fem_gpu_t* h);
+
+/* Replace all node coordinates (index order, n_nodes x 3) / plate properties
+ * (element order) without changing the topology; the next assemble reuses the
+ * pattern.  Host pointers. */
+int fem_gpu_set_node_coordinates(fem_gpu_t* h, const double* xyz, size_t n_nodes);
+int fem_gpu_set_plate_properties(fem_gpu_t* h, const double* young, const double* poisson, const double* thickness,
+                                 const double* shear_factor, size_t n);
+
+/* CSR read-out.  n_rows = 6 * nodes_number (the reference's SquareMatrix size). */
+int fem_gpu_get_csr_sizes(fem_gpu_t* h, int64_t* n_rows, int64_t* nnz);
+int fem_gpu_get_csr(fem_gpu_t* h, int64_t* row_ptr, int32_t* col_idx, double* values);
+int fem_gpu_get_csr_values(fem_gpu_t* h, double* values);
+int fem_gpu_get_csr_device(fem_gpu_t* h, const int64_t** row_ptr, const int32_t** col_idx, const double** values);
+
+/* DOF map: node index (insertion order) -> node number; global DOF of
+ * (node, DOFParameter p) is 6 * index + p (methods_for_bc_data_handle.rs:7-14). */
+int fem_gpu_get_node_count(fem_gpu_t* h, int64_t* n_nodes);
+int fem_gpu_get_index_node_numbers(fem_gpu_t* h, uint32_t* numbers);
+
+/* Stiffness groups (docs/Stiffness_groups.md): every non-empty 3x3 region
+ * (kind 0 Kuu, 1 Kuth, 2 Kthu, 3 Kthth) of every node-pair block, sorted by
+ * (row node, col node, kind); nnz_group[k] is the group of CSR entry k. */
+int fem_gpu_get_group_count(fem_gpu_t* h, int64_t* n_groups);
+int fem_gpu_get_groups(fem_gpu_t* h, int32_t* row_node, int32_t* col_node, uint8_t* kind, int32_t* nnz_group);
+
+/* get_{truss,beam,plate}_rotation_matrix_elements (fem.rs:171-202): the 3x3
+ * rotation (row-major) of element `number` of that kind. */
+int fem_gpu_get_truss_rotation(fem_gpu_t* h, uint32_t number, double* r9);
+int fem_gpu_get_beam_rotation(fem_gpu_t* h, uint32_t number, double* r9);
+int fem_gpu_get_plate_rotation(fem_gpu_t* h, uint32_t number, double* r9);
+
+/* Element counts, the handle's CUDA stream (cudaStream_t) and the number of
+ * kernels one numeric pass launches. */
+int fem_gpu_get_element_counts(fem_gpu_t* h, int64_t* n_truss, int64_t* n_beam, int64_t* n_plate);
+int fem_gpu_get_stream(fem_gpu_t* h, void** stream);
+int fem_gpu_numeric_launch_count(fem_gpu_t* h, int* n_launches);
+
+/* Per-kernel timing of the last numeric pass, measured with CUDA events on the
+ * handle's stream (milliseconds): element kernels (all types) and the reduction. */
+int fem_gpu_last_numeric_timing(fem_gpu_t* h, float* element_ms, float* reduce_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,144 @@
+/*
+ * fem_oracle.h -- CPU oracle for the element-stiffness-and-assembly path of the
+ * Rust crate `finite_element_method` (v0.9.12).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity checker and the timed
+ * CPU baseline.  Only tests/, __graft_entry__.smoke() and bench.py's CPU legs
+ * may load it; the product (finite_element_method_gb300/) never does.
+ *
+ * It restates, in FP64 C, the reference's eager assembly:
+ *   FEM::create                 src/fem/fem.rs:34-65
+ *   FEM::add_node               src/fem/methods_for_node_data_handle.rs:66-79
+ *   FEM::add_truss              src/fem/methods_for_truss_data_handle.rs:49-128
+ *   FEM::add_beam               src/fem/methods_for_beam_data_handle.rs:49-142
+ *   FEM::add_plate              src/fem/methods_for_plate_data_handle.rs:62-217
+ * with the element routines of src/fem/structs/{truss,beam,plate}.rs,
+ * src/fem/bar_2n_element_functions.rs and
+ * src/fem/quadrilateral_4n_element_functions.rs.  The global stiffness is kept,
+ * like the reference's SquareMatrix, as a (row, col) -> value hash map filled
+ * in element call order with exact zeros skipped; it is read out as CSR.
+ *
+ * Parity status: the truss path is pinned by the reference's own known answer
+ * (src/tests/fem/test_fem.rs:5-64: 2-node truss, E=1e6, A=2, L=30).  Beam and
+ * plate values are pinned only by closed-form answers derived from the
+ * reference formulas and by a literal dense restatement (oracle/literal.py);
+ * the reference's own tests hold no golden data for them.
+ */
+#ifndef FEM_ORACLE_H
+#define FEM_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_fem orc_fem_t;
+
+/* status codes, shared meaning with the GPU library's FEM_GPU_* codes */
+enum {
+  ORC_OK = 0,
+  ORC_ERR_NODE_LIMIT = 1,        /* methods_for_node_data_handle.rs:47-51 */
+  ORC_ERR_NODE_NUMBER = 2,       /* :53-55 */
+  ORC_ERR_NODE_INDEX = 3,        /* :56-58 */
+  ORC_ERR_NODE_COORDS = 4,       /* :59-61 */
+  ORC_ERR_NODE_NOT_EXIST = 5,    /* :81-86 */
+  ORC_ERR_ELEM_NUMBER = 6,       /* e.g. methods_for_truss_data_handle.rs:39-41 */
+  ORC_ERR_ELEM_SAME_NODES = 7,   /* e.g. methods_for_truss_data_handle.rs:42-44 */
+  ORC_ERR_YOUNG = 8,
+  ORC_ERR_POISSON = 9,
+  ORC_ERR_AREA = 10,
+  ORC_ERR_AREA2 = 11,
+  ORC_ERR_I11 = 12,
+  ORC_ERR_I22 = 13,
+  ORC_ERR_IT = 14,
+  ORC_ERR_SHEAR_FACTOR = 15,
+  ORC_ERR_PARALLEL_AXIS = 16,    /* structs/beam.rs:104-114 */
+  ORC_ERR_THICKNESS = 17,
+  ORC_ERR_NODES_ON_LINE = 18,    /* structs/plate.rs:87-106 */
+  ORC_ERR_NOT_ON_PLANE = 19,     /* structs/plate.rs:107-127 */
+  ORC_ERR_NOT_CONVEX = 20,       /* structs/plate.rs:128-155 */
+  ORC_ERR_ZERO_LENGTH = 21,      /* two-node element whose nodes coincide */
+  ORC_ERR_INTERNAL = 99
+};
+
+orc_fem_t* orc_create(double rel_tol, double abs_tol, uint32_t nodes_number);
+void orc_destroy(orc_fem_t* h);
+const char* orc_last_error(const orc_fem_t* h);
+
+int orc_add_node(orc_fem_t* h, uint32_t number, double x, double y, double z);
+int orc_add_truss(orc_fem_t* h, uint32_t number, uint32_t n1, uint32_t n2, double young, double area,
+                  int has_area2, double area2);
+int orc_add_beam(orc_fem_t* h, uint32_t number, uint32_t n1, uint32_t n2, double young, double poisson,
+                 double area, double i11, double i22, double i12, double it, double shear_factor,
+                 const double local_axis_1_direction[3]);
+int orc_add_plate(orc_fem_t* h, uint32_t number, uint32_t n1, uint32_t n2, uint32_t n3, uint32_t n4,
+                  double young, double poisson, double thickness, double shear_factor);
+
+/* Batched forms: loop over add_* in array order; stop at the first failure.
+ * *n_added receives the number of elements accepted before it. */
+int orc_add_nodes(orc_fem_t* h, const uint32_t* numbers, const double* xyz, size_t n, size_t* n_added);
+int orc_add_trusses(orc_fem_t* h, const uint32_t* numbers, const uint32_t* nodes2, const double* young,
+                    const double* area, const double* area2_or_nan, size_t n, size_t* n_added);
+int orc_add_beams(orc_fem_t* h, const uint32_t* numbers, const uint32_t* nodes2, const double* young,
+                  const double* poisson, const double* area, const double* i11, const double* i22,
+                  const double* i12, const double* it, const double* shear_factor, const double* axis3,
+                  size_t n, size_t* n_added);
+int orc_add_plates(orc_fem_t* h, const uint32_t* numbers, const uint32_t* nodes4, const double* young,
+                   const double* poisson, const double* thickness, const double* shear_factor, size_t n,
+                   size_t* n_added);
+
+/* Global stiffness as CSR (rows = 6 * nodes_number). */
+int64_t orc_n_rows(const orc_fem_t* h);
+int64_t orc_nnz(const orc_fem_t* h);
+int orc_get_csr(const orc_fem_t* h, int64_t* row_ptr, int32_t* col_idx, double* values);
+/* DOF map: index -> node number (insertion order), length = nodes added. */
+int64_t orc_n_nodes(const orc_fem_t* h);
+int orc_get_index_node_numbers(const orc_fem_t* h, uint32_t* numbers);
+/* Stiffness groups (docs/Stiffness_groups.md): every non-empty 3x3 region
+ * (Kuu, Kuth, Kthu, Kthth) of every node-pair block, sorted by (row node, col
+ * node, kind); and per CSR entry the index of its group. */
+int64_t orc_n_groups(const orc_fem_t* h);
+int orc_get_groups(const orc_fem_t* h, int32_t* row_node, int32_t* col_node, uint8_t* kind,
+                   int32_t* nnz_group);
+
+/* Element-level matrices in global axes (exactly what add_* scatters).
+ * truss: 6x6 (3 DOF per node), beam: 12x12, plate: 24x24, row-major.
+ * Return a status code (validation is NOT run here, only the arithmetic). */
+int orc_truss_global_matrix(const double x1[3], const double x2[3], double young, double area,
+                            int has_area2, double area2, double rel_tol, double abs_tol, double* out36);
+int orc_beam_global_matrix(const double x1[3], const double x2[3], double young, double poisson,
+                           double area, double i11, double i22, double i12, double it, double shear_factor,
+                           const double axis[3], double rel_tol, double abs_tol, double* out144);
+int orc_plate_global_matrix(const double x1[3], const double x2[3], const double x3[3], const double x4[3],
+                            double young, double poisson, double thickness, double shear_factor,
+                            double rel_tol, double abs_tol, double* out576);
+/* rotation matrices as stored by Truss/Beam/Plate::create (row-major 3x3) */
+int orc_truss_rotation(const double x1[3], const double x2[3], double rel_tol, double abs_tol, double* r9);
+int orc_beam_rotation(const double x1[3], const double x2[3], double i11, double i22, double i12,
+                      const double axis[3], double rel_tol, double abs_tol, double* r9,
+                      double* i11_p, double* i22_p);
+int orc_plate_rotation(const double x2[3], const double x3[3], const double x4[3], double rel_tol,
+                       double abs_tol, double* r9);
+
+/* the transcendental kernels shared (by algorithm, not by code) with the GPU */
+double orc_sin(double x);
+double orc_cos(double x);
+double orc_atan(double x);
+double orc_acos(double x);
+
+/* Multi-threaded numeric assembly of a whole mesh into a given CSR pattern,
+ * used as the reference arm of the benchmark: element matrices are formed in
+ * parallel and summed per entry in element order (bit-identical to the eager
+ * path).  Elements are given in call order; kinds: 0 truss, 1 beam, 2 plate.
+ * Returns elapsed seconds in *seconds. */
+int orc_parallel_plates_assemble(const double* xyz, const int32_t* nodes4_idx, const double* young,
+                                 const double* poisson, const double* thickness, const double* shear,
+                                 size_t n_elems, double rel_tol, double abs_tol, int n_threads,
+                                 double* element_out /* n_elems*576 or NULL */, double* seconds);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
