@@ -1,0 +1,309 @@
+"""Benchmark of the FP64 element-stiffness-and-assembly path on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload plate|beam|truss]
+
+A step is one numeric assembly pass over the whole mesh into the FP64 CSR
+global stiffness (element kernels + deterministic block reduction), with the
+CSR pattern built once before timing.  `value` is elements/s of that pass with
+the mesh resident in HBM (CUDA events on the library's stream, L2 flushed
+between steps); `e2e` is elements/s of the full drop-in call sequence from
+host arrays (create, add_nodes, add_plates/beams, assemble, CSR read-back to
+host); `roofline` reports the dominant kernel against the measured HBM copy
+bandwidth and the measured FP64 FMA rate; `cpu_baseline` times the CPU oracle
+(the reference algorithm restated in C, one thread, eager insertion order) on
+a bounded sample.  `--impl reference` times the multi-threaded CPU port of the
+reference algorithm on all host cores instead.  The path does not shard across
+GPUs: `--gpus N` under torchrun runs N independent replicas (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from finite_element_method_gb300 import FEM, meshes  # noqa: E402
+
+# FP64 FMA throughput of a GB300 measured with a dependent-chain DFMA loop on all
+# 152 SMs at 2070 MHz (1.6 DFMA/clk/SM): 504.6e9 DFMA/s = 1.009e12 FP64 flop/s.
+FP64_PEAK_FLOPS = 1.009e12
+
+# Algorithmic work per element of the numeric pass (counted from the kernels'
+# formulation: one FMA = 2 flops; bytes = compulsory HBM traffic of each kernel).
+WORK = {
+    # plate, R = I (flat mesh in z = 0): core 552 flops + 10 node-pair blocks x 68 flops
+    "plate": dict(elem_flops=1232, pairs=10),
+    "beam": dict(elem_flops=1100, pairs=3),
+    "truss": dict(elem_flops=60, pairs=3),
+}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index=0, period_ms=100):
+        self.samples, self.max_mhz, self.reasons = [], None, set()
+        self._stop = threading.Event()
+        self._idx, self._period = gpu_index, period_ms
+        self._t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self._idx), f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                f = [x.strip() for x in out.stdout.strip().split(",")]
+                if len(f) >= 6:
+                    self.samples.append(float(f[0]))
+                    self.max_mhz = float(f[1])
+                    for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                        "sw_power_cap"), f[2:6]):
+                        if v.lower().startswith("active"):
+                            self.reasons.add(name)
+            except Exception:
+                pass
+            self._stop.wait(self._period / 1000.0)
+
+    def __enter__(self):
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        return {"sm_mhz": float(np.median(self.samples)) if self.samples else None, "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(self.reasons), "samples": len(self.samples)}
+
+
+def make_mesh(workload, nx=1000):
+    if workload == "plate":
+        n = nx
+        return meshes.plate_mesh(n, n), (f"plate_mesh_{n}x{n} ({n * n:,} 4-node plates, {(n + 1) ** 2:,} nodes, "
+                                         "6 DOF/node)")
+    if workload == "beam":
+        return meshes.beam_frame(), "beam_frame_101x101x21 (628,220 2-node beams, 214,221 nodes)"
+    if workload == "truss":
+        return meshes.truss_lattice(), "truss_lattice_11x11x11 (4,630 bars, 1,331 nodes)"
+    raise SystemExit(f"unknown workload {workload}")
+
+
+def sample_mesh(workload):
+    """bounded sample of the same workload for the CPU legs (~10 s of one-thread work)."""
+    if workload == "plate":
+        return meshes.plate_mesh(400, 400), "plate_mesh 400x400 (160,000 plates), same generator"
+    if workload == "beam":
+        return meshes.beam_frame(41, 41, 21), "beam_frame 41x41x21 (104,140 beams), same generator"
+    return meshes.truss_lattice(), "full truss lattice"
+
+
+def cpu_oracle_eager(mesh):
+    """one-thread eager assembly (the reference algorithm: element matrix, T^T K T, zero-skip, hash accumulate
+    in call order), from host arrays to CSR; returns elements/s."""
+    from oracle.fem_oracle import OracleFEM
+
+    t0 = time.perf_counter()
+    o = OracleFEM(meshes.REL_TOL, meshes.ABS_TOL, mesh.nodes_number)
+    meshes.load(o, mesh)
+    o.csr()
+    dt = time.perf_counter() - t0
+    return mesh.n_elements / dt, dt
+
+
+def run_reference(args):
+    """--impl reference: the multi-threaded CPU port of the reference algorithm on all host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import fem_oracle
+
+    fem_oracle.lib()
+    mesh, sample_desc = sample_mesh(args.workload)
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        fem_oracle.assemble_parallel(mesh, cores)
+    times = []
+    for _ in range(args.steps):
+        sec, nnz, _ = fem_oracle.assemble_parallel(mesh, cores)
+        times.append(sec)
+    t = float(np.mean(times))
+    v = mesh.n_elements / t
+    line = {"impl": "reference", "metric": "elements/s assembled to FP64 CSR", "value": v, "unit": "elements/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "sample": sample_desc, "nnz": nnz},
+            "cpu_baseline": {"value": v, "unit": "elements/s", "cores": cores, "kind": "port",
+                             "sample": sample_desc},
+            "e2e": {"value": v, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="plate", choices=["plate", "beam", "truss"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--nx", type=int, default=1000, help="plate mesh size (nx x nx); 1000 is the full workload")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    mesh, desc = make_mesh(args.workload, args.nx)
+    n_el = mesh.n_elements
+    fem = FEM(meshes.REL_TOL, meshes.ABS_TOL, mesh.nodes_number)
+    t0 = time.perf_counter()
+    meshes.load(fem, mesh)
+    fem.assemble()  # symbolic (pattern, groups, destination map) + first numeric pass
+    setup_s = time.perf_counter() - t0
+    n_rows, nnz = fem.csr_sizes()
+
+    stream = torch.cuda.ExternalStream(fem.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+    for _ in range(args.warmup):
+        fem.assemble_numeric_async()
+    torch.cuda.synchronize()
+    fem.check_pattern()
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    step_ms, elem_ms, red_ms = [], [], []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            fem.assemble_numeric_async()
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            a, b = fem.last_numeric_timing()
+            elem_ms.append(a)
+            red_ms.append(b)
+    torch.cuda.synchronize()
+    fem.check_pattern()
+    t_step = float(np.sum(step_ms)) / args.steps
+    if world > 1:
+        tt = torch.tensor([t_step], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = n_el * world / (t_step * 1e-3)
+
+    # roofline of the dominant kernel
+    hbm_gbs, peak_src = measured_peaks()
+    w = WORK[args.workload]
+    pairs = w["pairs"] * n_el
+    # element kernels: write 36 doubles per node-pair block + read inputs (conn, coords, props)
+    in_bytes = {"plate": 16 + 4 * 24 + 32, "beam": 8 + 2 * 24 + 13 * 8, "truss": 8 + 2 * 24 + 24}[args.workload]
+    elem_bytes = pairs * 36 * 8 + n_el * in_bytes
+    # reduction: read every slot once + block metadata, write CSR values
+    red_bytes = pairs * 36 * 8 + nnz * 8
+    t_e, t_r = float(np.mean(elem_ms)), float(np.mean(red_ms))
+    kern = {"element": dict(ms=t_e, bytes=elem_bytes, flops=w["elem_flops"] * n_el),
+            "reduce": dict(ms=t_r, bytes=red_bytes, flops=0)}
+    dom = max(kern, key=lambda k: kern[k]["ms"])
+    kd = kern[dom]
+    gbs = kd["bytes"] / (kd["ms"] * 1e-3) / 1e9
+    fl = kd["flops"] / (kd["ms"] * 1e-3)
+    frac_hbm, frac_fp64 = gbs / hbm_gbs, fl / FP64_PEAK_FLOPS
+    if frac_fp64 > frac_hbm:
+        roof = {"bound": "fp64", "achieved": fl / 1e12, "peak": FP64_PEAK_FLOPS / 1e12, "unit": "TFLOP/s",
+                "frac": frac_fp64}
+    else:
+        roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_gbs, "unit": "GB/s", "frac": frac_hbm}
+    roof.update({"kernel": dom, "traffic": None, "peak_source": f"{peak_src} (hbm); FP64 FMA loop (fp64)",
+                 "per_kernel_ms": {k: v["ms"] for k, v in kern.items()},
+                 "per_kernel_frac": {k: {"hbm": v["bytes"] / (v["ms"] * 1e-3) / 1e9 / hbm_gbs,
+                                         "fp64": v["flops"] / (v["ms"] * 1e-3) / FP64_PEAK_FLOPS}
+                                     for k, v in kern.items()}})
+
+    # e2e: the drop-in call sequence from host arrays to a host CSR
+    e2e_ms = []
+    h2d = mesh.xyz.nbytes + mesh.node_numbers.nbytes
+    for d in (mesh.trusses, mesh.beams, mesh.plates):
+        if d is not None:
+            h2d += sum(np.asarray(v).nbytes for k, v in d.items() if v is not None and k != "numbers")
+    d2h = (n_rows + 1) * 8 + nnz * (4 + 8)
+    rp = np.empty(n_rows + 1, np.int64)
+    ci = np.empty(nnz, np.int32)
+    va = np.empty(nnz, np.float64)
+    for _ in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        f2 = FEM(meshes.REL_TOL, meshes.ABS_TOL, mesh.nodes_number)
+        meshes.load(f2, mesh)
+        f2.assemble()
+        from finite_element_method_gb300._lib import ptr
+        import ctypes
+
+        st = f2._L.fem_gpu_get_csr(f2.handle, ptr(rp, ctypes.c_int64), ptr(ci, ctypes.c_int32),
+                                   ptr(va, ctypes.c_double))
+        assert st == 0
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        f2.close()
+    e2e_t = float(np.median(e2e_ms))
+    e2e = {"value": n_el * world / (e2e_t * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t,
+           "what": "create + add_nodes + add_* + assemble (symbolic + numeric) + CSR to host"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        smesh, sdesc = sample_mesh(args.workload)
+        v, dt = cpu_oracle_eager(smesh)
+        cpu = {"value": v, "unit": "elements/s", "cores": 1, "kind": "port", "sample": sdesc + f", {dt:.1f} s"}
+
+    launches = fem.numeric_launch_count() * args.steps
+    line = {"metric": "elements/s assembled to FP64 CSR", "value": value, "unit": "elements/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc, "nnz": int(nnz), "n_rows": int(n_rows), "l2": "flushed (256 MB write) "
+                       "between steps", "parallelism": f"replicas x{world}", "setup_s": setup_s},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clocks.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    fem.close()
+
+
+if __name__ == "__main__":
+    main()

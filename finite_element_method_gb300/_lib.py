@@ -1,0 +1,81 @@
+"""ctypes binding of the C ABI declared in include/fem_gpu.h.
+
+The shared library is the product: every call goes to CUDA kernels.  There
+is no CPU path behind this module; when the library is missing it is built
+with nvcc, and when no CUDA device is present the library's own calls fail
+with FEM_GPU_ERR_CUDA.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_int32, c_int64, c_size_t, c_uint8, c_uint32, c_void_p
+
+from . import build as _build
+
+dp, fp = POINTER(c_double), POINTER(c_float)
+i32p, i64p, u32p, u8p, szp = POINTER(c_int32), POINTER(c_int64), POINTER(c_uint32), POINTER(c_uint8), POINTER(c_size_t)
+hp = c_void_p
+
+# name -> (restype, argtypes); the complete exported surface of include/fem_gpu.h
+SIGNATURES = {
+    "fem_gpu_create": (c_int, [c_double, c_double, c_uint32, POINTER(c_void_p)]),
+    "fem_gpu_destroy": (c_int, [hp]),
+    "fem_gpu_last_error": (c_char_p, [hp]),
+    "fem_gpu_add_nodes": (c_int, [hp, u32p, dp, c_size_t, szp]),
+    "fem_gpu_add_trusses": (c_int, [hp, u32p, u32p, dp, dp, dp, c_size_t, szp]),
+    "fem_gpu_add_beams": (c_int, [hp, u32p, u32p] + [dp] * 9 + [c_size_t, szp]),
+    "fem_gpu_add_plates": (c_int, [hp, u32p, u32p, dp, dp, dp, dp, c_size_t, szp]),
+    "fem_gpu_assemble": (c_int, [hp]),
+    "fem_gpu_assemble_numeric_async": (c_int, [hp]),
+    "fem_gpu_check_pattern": (c_int, [hp]),
+    "fem_gpu_set_node_coordinates": (c_int, [hp, dp, c_size_t]),
+    "fem_gpu_set_plate_properties": (c_int, [hp, dp, dp, dp, dp, c_size_t]),
+    "fem_gpu_get_csr_sizes": (c_int, [hp, i64p, i64p]),
+    "fem_gpu_get_csr": (c_int, [hp, i64p, i32p, dp]),
+    "fem_gpu_get_csr_values": (c_int, [hp, dp]),
+    "fem_gpu_get_csr_device": (c_int, [hp, POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p)]),
+    "fem_gpu_get_node_count": (c_int, [hp, i64p]),
+    "fem_gpu_get_index_node_numbers": (c_int, [hp, u32p]),
+    "fem_gpu_get_group_count": (c_int, [hp, i64p]),
+    "fem_gpu_get_groups": (c_int, [hp, i32p, i32p, u8p, i32p]),
+    "fem_gpu_get_truss_rotation": (c_int, [hp, c_uint32, dp]),
+    "fem_gpu_get_beam_rotation": (c_int, [hp, c_uint32, dp]),
+    "fem_gpu_get_plate_rotation": (c_int, [hp, c_uint32, dp]),
+    "fem_gpu_get_element_counts": (c_int, [hp, i64p, i64p, i64p]),
+    "fem_gpu_get_stream": (c_int, [hp, POINTER(c_void_p)]),
+    "fem_gpu_numeric_launch_count": (c_int, [hp, POINTER(c_int)]),
+    "fem_gpu_last_numeric_timing": (c_int, [hp, fp, fp]),
+}
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load libfem_gpu.so (building it first when absent or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB_PATH
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA assembly library not found at {path}; build it with finite_element_method_gb300.build")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def ptr(a, ct):
+    """ctypes pointer to a contiguous numpy array (None passes NULL)."""
+    if a is None:
+        return None
+    return a.ctypes.data_as(POINTER(ct))

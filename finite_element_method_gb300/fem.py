@@ -1,0 +1,252 @@
+"""Host-side mirror of the reference crate's `FEM` assembly API over the C ABI.
+
+Reference interface (Rust crate finite_element_method 0.9.12):
+  FEM::create(rel_tol, abs_tol, nodes_number)          src/fem/fem.rs:34
+  FEM::add_node(number, x, y, z)                        src/fem/methods_for_node_data_handle.rs:66
+  FEM::add_truss(number, n1, n2, E, A, Option<A2>)      src/fem/methods_for_truss_data_handle.rs:49
+  FEM::add_beam(number, n1, n2, E, nu, A, I11, I22, I12, It, k, axis)
+                                                        src/fem/methods_for_beam_data_handle.rs:49
+  FEM::add_plate(number, n1, n2, n3, n4, E, nu, t, k)   src/fem/methods_for_plate_data_handle.rs:62
+  FEM::get_{truss,beam,plate}_rotation_matrix_elements  src/fem/fem.rs:171-202
+  FEM.stiffness_matrix (SquareMatrix, read by the separation step, fem.rs:71)
+
+Each add_* raises `FEMError` with the reference's message where the reference
+returns Err(String); the failing element leaves the model unchanged.  The
+reference assembles eagerly inside add_*; here the stiffness is built by
+`assemble()` (one symbolic + numeric pass on the GPU), after which
+`stiffness_csr()` returns the same matrix as CSR (row = 6 * node index + DOF,
+DOFParameter order X, Y, Z, ThX, ThY, ThZ).  The bulk forms add many elements
+of one kind in one call, in array order, stopping at the first failure.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import c_double, c_float, c_int, c_int32, c_int64, c_size_t, c_uint8, c_uint32, c_void_p
+
+import numpy as np
+
+from . import _lib
+from ._lib import ptr
+
+FEM_GPU_ERR_CUDA = 40
+
+
+class FEMError(RuntimeError):
+    """A failed C-ABI call: `code` is the FEM_GPU_* status, the message the reference's."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+def _f64(v, m):
+    return np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), (m,)))
+
+
+def _u32(v, shape):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.uint32).reshape(shape))
+
+
+class FEM:
+    """FEM::create(rel_tol, abs_tol, nodes_number) with the GPU assembly behind it."""
+
+    def __init__(self, rel_tol: float, abs_tol: float, nodes_number: int):
+        self._L = _lib.load()
+        h = c_void_p()
+        self._check(self._L.fem_gpu_create(rel_tol, abs_tol, nodes_number, ctypes.byref(h)), None)
+        self._h = h
+        self.rel_tol, self.abs_tol, self.nodes_number = rel_tol, abs_tol, nodes_number
+
+    # -- plumbing ---------------------------------------------------------
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._L.fem_gpu_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, st: int, h=-1):
+        if st:
+            hh = self._h if h == -1 else h
+            msg = self._L.fem_gpu_last_error(hh).decode() if hh else f"status {st}"
+            raise FEMError(st, msg)
+
+    # -- node / element API (reference names) ------------------------------
+    def add_node(self, number: int, x: float, y: float, z: float) -> None:
+        self.add_nodes([number], [[x, y, z]])
+
+    def add_nodes(self, numbers, xyz) -> int:
+        numbers = _u32(numbers, (-1,))
+        xyz = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64).reshape(len(numbers), 3))
+        n = c_size_t(0)
+        st = self._L.fem_gpu_add_nodes(self._h, ptr(numbers, c_uint32), ptr(xyz, c_double), len(numbers),
+                                       ctypes.byref(n))
+        self._check(st)
+        return n.value
+
+    def add_truss(self, number, node_1_number, node_2_number, young_modulus, area, area_2=None) -> None:
+        self.add_trusses([number], [[node_1_number, node_2_number]], young_modulus, area,
+                         None if area_2 is None else [area_2])
+
+    def add_trusses(self, numbers, nodes, young_modulus, area, area_2=None) -> int:
+        m = len(numbers)
+        numbers, nodes = _u32(numbers, (m,)), _u32(nodes, (m, 2))
+        E, A = _f64(young_modulus, m), _f64(area, m)
+        A2 = None if area_2 is None else _f64(area_2, m)
+        n = c_size_t(0)
+        st = self._L.fem_gpu_add_trusses(self._h, ptr(numbers, c_uint32), ptr(nodes, c_uint32), ptr(E, c_double),
+                                         ptr(A, c_double), ptr(A2, c_double), m, ctypes.byref(n))
+        self._check(st)
+        return n.value
+
+    def add_beam(self, number, node_1_number, node_2_number, young_modulus, poisson_ratio, area, i11, i22, i12, it,
+                 shear_factor, local_axis_1_direction) -> None:
+        self.add_beams([number], [[node_1_number, node_2_number]], young_modulus, poisson_ratio, area, i11, i22, i12,
+                       it, shear_factor, [local_axis_1_direction])
+
+    def add_beams(self, numbers, nodes, young_modulus, poisson_ratio, area, i11, i22, i12, it, shear_factor,
+                  local_axis_1_direction) -> int:
+        m = len(numbers)
+        numbers, nodes = _u32(numbers, (m,)), _u32(nodes, (m, 2))
+        arrs = [_f64(v, m) for v in (young_modulus, poisson_ratio, area, i11, i22, i12, it, shear_factor)]
+        axis = np.ascontiguousarray(np.broadcast_to(np.asarray(local_axis_1_direction, dtype=np.float64), (m, 3)))
+        n = c_size_t(0)
+        st = self._L.fem_gpu_add_beams(self._h, ptr(numbers, c_uint32), ptr(nodes, c_uint32),
+                                       *[ptr(a, c_double) for a in arrs], ptr(axis, c_double), m, ctypes.byref(n))
+        self._check(st)
+        return n.value
+
+    def add_plate(self, number, node_1_number, node_2_number, node_3_number, node_4_number, young_modulus,
+                  poisson_ratio, thickness, shear_factor) -> None:
+        self.add_plates([number], [[node_1_number, node_2_number, node_3_number, node_4_number]], young_modulus,
+                        poisson_ratio, thickness, shear_factor)
+
+    def add_plates(self, numbers, nodes, young_modulus, poisson_ratio, thickness, shear_factor) -> int:
+        m = len(numbers)
+        numbers, nodes = _u32(numbers, (m,)), _u32(nodes, (m, 4))
+        arrs = [_f64(v, m) for v in (young_modulus, poisson_ratio, thickness, shear_factor)]
+        n = c_size_t(0)
+        st = self._L.fem_gpu_add_plates(self._h, ptr(numbers, c_uint32), ptr(nodes, c_uint32),
+                                        *[ptr(a, c_double) for a in arrs], m, ctypes.byref(n))
+        self._check(st)
+        return n.value
+
+    # -- assembly ----------------------------------------------------------
+    def assemble(self) -> None:
+        self._check(self._L.fem_gpu_assemble(self._h))
+
+    def assemble_numeric_async(self) -> None:
+        self._check(self._L.fem_gpu_assemble_numeric_async(self._h))
+
+    def check_pattern(self) -> None:
+        self._check(self._L.fem_gpu_check_pattern(self._h))
+
+    def set_node_coordinates(self, xyz) -> None:
+        xyz = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64).reshape(-1, 3))
+        self._check(self._L.fem_gpu_set_node_coordinates(self._h, ptr(xyz, c_double), len(xyz)))
+
+    def set_plate_properties(self, young_modulus, poisson_ratio, thickness, shear_factor) -> None:
+        m = self.element_counts()[2]
+        arrs = [_f64(v, m) for v in (young_modulus, poisson_ratio, thickness, shear_factor)]
+        self._check(self._L.fem_gpu_set_plate_properties(self._h, *[ptr(a, c_double) for a in arrs], m))
+
+    # -- read-out ----------------------------------------------------------
+    def csr_sizes(self):
+        nr, nnz = c_int64(0), c_int64(0)
+        self._check(self._L.fem_gpu_get_csr_sizes(self._h, ctypes.byref(nr), ctypes.byref(nnz)))
+        return nr.value, nnz.value
+
+    def stiffness_csr(self):
+        """(row_ptr int64[n_rows+1], col_idx int32[nnz], values float64[nnz]) of the global stiffness."""
+        nr, nnz = self.csr_sizes()
+        rp = np.zeros(nr + 1, np.int64)
+        ci = np.zeros(max(nnz, 1), np.int32)
+        va = np.zeros(max(nnz, 1), np.float64)
+        self._check(self._L.fem_gpu_get_csr(self._h, ptr(rp, c_int64), ptr(ci, c_int32), ptr(va, c_double)))
+        return rp, ci[:nnz], va[:nnz]
+
+    def stiffness_values(self, out=None):
+        _, nnz = self.csr_sizes()
+        if out is None:
+            out = np.zeros(max(nnz, 1), np.float64)
+        self._check(self._L.fem_gpu_get_csr_values(self._h, ptr(out, c_double)))
+        return out[:nnz]
+
+    def stiffness_device_pointers(self):
+        a, b, c = c_void_p(), c_void_p(), c_void_p()
+        self._check(self._L.fem_gpu_get_csr_device(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def node_count(self) -> int:
+        n = c_int64(0)
+        self._check(self._L.fem_gpu_get_node_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def index_node_numbers(self):
+        """DOF map: node index (insertion order) -> node number; DOF = 6 * index + DOFParameter."""
+        n = self.node_count()
+        out = np.zeros(max(n, 1), np.uint32)
+        self._check(self._L.fem_gpu_get_index_node_numbers(self._h, ptr(out, c_uint32)))
+        return out[:n]
+
+    def groups(self):
+        """Stiffness groups: (row_node, col_node, kind, nnz_group); kind 0 Kuu, 1 Kuth, 2 Kthu, 3 Kthth."""
+        ng = c_int64(0)
+        self._check(self._L.fem_gpu_get_group_count(self._h, ctypes.byref(ng)))
+        ng = ng.value
+        _, nnz = self.csr_sizes()
+        rn, cn = np.zeros(max(ng, 1), np.int32), np.zeros(max(ng, 1), np.int32)
+        kd, gi = np.zeros(max(ng, 1), np.uint8), np.zeros(max(nnz, 1), np.int32)
+        self._check(self._L.fem_gpu_get_groups(self._h, ptr(rn, c_int32), ptr(cn, c_int32), ptr(kd, c_uint8),
+                                               ptr(gi, c_int32)))
+        return rn[:ng], cn[:ng], kd[:ng], gi[:nnz]
+
+    def _rotation(self, fn, number):
+        r = np.zeros(9)
+        self._check(fn(self._h, number, ptr(r, c_double)))
+        return r
+
+    def get_truss_rotation_matrix_elements(self, number):
+        return self._rotation(self._L.fem_gpu_get_truss_rotation, number)
+
+    def get_beam_rotation_matrix_elements(self, number):
+        return self._rotation(self._L.fem_gpu_get_beam_rotation, number)
+
+    def get_plate_rotation_matrix_elements(self, number):
+        return self._rotation(self._L.fem_gpu_get_plate_rotation, number)
+
+    def element_counts(self):
+        a, b, c = c_int64(0), c_int64(0), c_int64(0)
+        self._check(self._L.fem_gpu_get_element_counts(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def stream(self) -> int:
+        s = c_void_p()
+        self._check(self._L.fem_gpu_get_stream(self._h, ctypes.byref(s)))
+        return s.value or 0
+
+    def numeric_launch_count(self) -> int:
+        n = c_int(0)
+        self._check(self._L.fem_gpu_numeric_launch_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def last_numeric_timing(self):
+        """(element kernels ms, reduction ms) of the last numeric pass, CUDA events on the handle's stream."""
+        a, b = c_float(0), c_float(0)
+        self._check(self._L.fem_gpu_last_numeric_timing(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value

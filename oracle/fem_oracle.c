@@ -1405,17 +1405,33 @@ static int kv_cmp(const void* a, const void* b) {
   return x < y ? -1 : x > y ? 1 : 0;
 }
 
+/* entries sorted by (row, col): counting sort by row, then a small sort per row */
 static kv* sorted_entries(const orc_fem_t* h) {
-  kv* e = (kv*)malloc(sizeof(kv) * (h->K.len ? h->K.len : 1));
-  size_t k = 0;
+  uint64_t nrows = (uint64_t)h->nodes_number * 6u;
+  size_t n = h->K.len;
+  kv* e = (kv*)malloc(sizeof(kv) * (n ? n : 1));
+  int64_t* off = (int64_t*)calloc(nrows + 2, sizeof(int64_t));
+  for (size_t i = 0; i < h->K.cap; ++i)
+    if (h->K.keys[i]) off[(h->K.keys[i] - 1) / nrows + 2]++;
+  for (uint64_t r = 0; r < nrows; ++r) off[r + 2] += off[r + 1];
   for (size_t i = 0; i < h->K.cap; ++i)
     if (h->K.keys[i]) {
-      e[k].key = h->K.keys[i] - 1;
-      memcpy(&e[k].val, &h->K.vals[i], 8);
-      ++k;
+      uint64_t key = h->K.keys[i] - 1;
+      int64_t at = off[key / nrows + 1]++;
+      e[at].key = key;
+      memcpy(&e[at].val, &h->K.vals[i], 8);
     }
-  qsort(e, k, sizeof(kv), kv_cmp);
+  for (uint64_t r = 0; r < nrows; ++r) {
+    int64_t b = off[r], m = off[r + 1] - off[r];
+    if (m > 1) qsort(e + b, (size_t)m, sizeof(kv), kv_cmp);
+  }
+  free(off);
   return e;
+}
+
+static int u64_cmp(const void* a, const void* b) {
+  uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+  return x < y ? -1 : x > y ? 1 : 0;
 }
 
 int orc_get_csr(const orc_fem_t* h, int64_t* row_ptr, int32_t* col_idx, double* values) {
@@ -1434,49 +1450,52 @@ int orc_get_csr(const orc_fem_t* h, int64_t* row_ptr, int32_t* col_idx, double* 
   return ORC_OK;
 }
 
-/* groups = distinct (row node, col node, kind) over the pattern, in sorted order */
+/* groups = distinct (row node, col node, kind) over the pattern, in sorted
+ * order (docs/Stiffness_groups.md: every node-pair 6x6 block splits into the
+ * 3x3 groups Kuu, Kuth, Kthu, Kthth) */
 static int64_t groups_impl(const orc_fem_t* h, int32_t* row_node, int32_t* col_node, uint8_t* kind,
                            int32_t* nnz_group) {
   uint64_t nrows = (uint64_t)h->nodes_number * 6u;
   kv* e = sorted_entries(h);
   size_t n = h->K.len;
-  /* group key = (row_node, col_node, kind); collect, sort, unique */
   uint64_t* gk = (uint64_t*)malloc(sizeof(uint64_t) * (n ? n : 1));
   for (size_t i = 0; i < n; ++i) {
     uint64_t r = e[i].key / nrows, c = e[i].key % nrows;
     uint64_t kd = 2u * ((r % 6u) / 3u) + (c % 6u) / 3u;
     gk[i] = ((r / 6u) << 34) | ((c / 6u) << 2) | kd; /* node indices < 2^30 */
   }
+  /* entries are sorted by row, so each row node's entries are contiguous:
+   * sort and unique its group keys locally */
   uint64_t* sk = (uint64_t*)malloc(sizeof(uint64_t) * (n ? n : 1));
-  memcpy(sk, gk, sizeof(uint64_t) * n);
-  /* sort unique */
-  {
-    kv* tmp = (kv*)malloc(sizeof(kv) * (n ? n : 1));
-    for (size_t i = 0; i < n; ++i) {
-      tmp[i].key = sk[i];
-      tmp[i].val = 0;
-    }
-    qsort(tmp, n, sizeof(kv), kv_cmp);
-    for (size_t i = 0; i < n; ++i) sk[i] = tmp[i].key;
-    free(tmp);
+  size_t ng = 0, i = 0;
+  while (i < n) {
+    uint64_t rn = gk[i] >> 34;
+    size_t j = i;
+    while (j < n && (gk[j] >> 34) == rn) ++j;
+    size_t g0 = ng;
+    memcpy(sk + ng, gk + i, sizeof(uint64_t) * (j - i));
+    qsort(sk + ng, j - i, sizeof(uint64_t), u64_cmp);
+    size_t w = g0;
+    for (size_t k = g0; k < g0 + (j - i); ++k)
+      if (k == g0 || sk[k] != sk[k - 1]) sk[w++] = sk[k];
+    if (nnz_group)
+      for (size_t k = i; k < j; ++k) {
+        size_t lo = g0, hi = w;
+        while (lo < hi) {
+          size_t mid = (lo + hi) / 2;
+          if (sk[mid] < gk[k]) lo = mid + 1;
+          else hi = mid;
+        }
+        nnz_group[k] = (int32_t)lo;
+      }
+    ng = w;
+    i = j;
   }
-  size_t ng = 0;
-  for (size_t i = 0; i < n; ++i)
-    if (i == 0 || sk[i] != sk[i - 1]) sk[ng++] = sk[i];
   if (row_node) {
     for (size_t g = 0; g < ng; ++g) {
       row_node[g] = (int32_t)(sk[g] >> 34);
       col_node[g] = (int32_t)((sk[g] >> 2) & ((1ull << 32) - 1));
       kind[g] = (uint8_t)(sk[g] & 3u);
-    }
-    for (size_t i = 0; i < n; ++i) {
-      size_t lo = 0, hi = ng;
-      while (lo < hi) {
-        size_t mid = (lo + hi) / 2;
-        if (sk[mid] < gk[i]) lo = mid + 1;
-        else hi = mid;
-      }
-      nnz_group[i] = (int32_t)lo;
     }
   }
   free(gk);
@@ -1492,61 +1511,150 @@ int orc_get_groups(const orc_fem_t* h, int32_t* row_node, int32_t* col_node, uin
 }
 
 /* ------------------------------------------------------------------------ */
-/* multi-threaded plate element matrices (reference arm of the benchmark)    */
+/* multi-threaded assembly of a whole mesh (the timed CPU reference arm)     */
 /* ------------------------------------------------------------------------ */
 
+/* Row-partitioned port of the eager assembly: thread t owns the node range
+ * [n0, n1) and walks every element in call order, forming the element matrix
+ * (element routines above) whenever the element touches its range and adding
+ * the non-zero entries of its own rows to a private hash map.  Each entry is
+ * therefore summed in element call order exactly as in orc_add_* (results
+ * are bit-identical), and threads share nothing but the read-only inputs. */
 typedef struct {
-  const double* xyz;
-  const int32_t* nodes4;
-  const double *young, *poisson, *thickness, *shear;
-  size_t begin, end;
+  const orc_mesh_t* m;
   double rel_tol, abs_tol;
-  double* out;
-  double checksum;
-} plate_job;
+  size_t n0, n1;
+  u64map K;
+  int status;
+} asm_job;
 
-static void* plate_worker(void* p) {
-  plate_job* j = (plate_job*)p;
-  double kg[576];
-  double cs = 0.0;
-  for (size_t e = j->begin; e < j->end; ++e) {
-    const int32_t* n = j->nodes4 + 4 * e;
-    double* dst = j->out ? j->out + 576 * e : kg;
-    orc_plate_global_matrix(j->xyz + 3 * (size_t)n[0], j->xyz + 3 * (size_t)n[1], j->xyz + 3 * (size_t)n[2],
-                            j->xyz + 3 * (size_t)n[3], j->young[e], j->poisson[e], j->thickness[e], j->shear[e],
-                            j->rel_tol, j->abs_tol, dst);
-    cs += dst[0] + dst[575];
+static int touches(const int32_t* nd, int k, size_t n0, size_t n1) {
+  for (int i = 0; i < k; ++i)
+    if ((size_t)nd[i] >= n0 && (size_t)nd[i] < n1) return 1;
+  return 0;
+}
+
+static void scatter_rows(u64map* K, uint64_t nrows, const int32_t* idx, int nn, int ndof, const double* kg, size_t n0,
+                         size_t n1) {
+  int w = nn * ndof;
+  for (int bi = 0; bi < nn; ++bi) {
+    if ((size_t)idx[bi] < n0 || (size_t)idx[bi] >= n1) continue;
+    for (int bj = 0; bj < nn; ++bj)
+      for (int a = 0; a < ndof; ++a)
+        for (int b = 0; b < ndof; ++b) {
+          double v = kg[w * (bi * ndof + a) + bj * ndof + b];
+          if (v != 0.0) {
+            uint64_t row = (uint64_t)idx[bi] * 6u + (uint64_t)a, col = (uint64_t)idx[bj] * 6u + (uint64_t)b;
+            kadd(K, row * nrows + col, v);
+          }
+        }
   }
-  j->checksum = cs;
+}
+
+static void* asm_worker(void* p) {
+  asm_job* j = (asm_job*)p;
+  const orc_mesh_t* m = j->m;
+  uint64_t nrows = (uint64_t)m->nodes_number * 6u;
+  double kg[576];
+  const double* X = m->xyz;
+  for (size_t e = 0; e < m->n_truss; ++e) {
+    const int32_t* nd = m->t_nodes + 2 * e;
+    if (!touches(nd, 2, j->n0, j->n1)) continue;
+    double a2 = m->t_area2 ? m->t_area2[e] : NAN;
+    if (orc_truss_global_matrix(X + 3 * (size_t)nd[0], X + 3 * (size_t)nd[1], m->t_young[e], m->t_area[e], a2 == a2,
+                                a2 == a2 ? a2 : 0.0, j->rel_tol, j->abs_tol, kg)) {
+      j->status = ORC_ERR_ZERO_LENGTH;
+      continue;
+    }
+    scatter_rows(&j->K, nrows, nd, 2, 3, kg, j->n0, j->n1);
+  }
+  for (size_t e = 0; e < m->n_beam; ++e) {
+    const int32_t* nd = m->b_nodes + 2 * e;
+    if (!touches(nd, 2, j->n0, j->n1)) continue;
+    if (orc_beam_global_matrix(X + 3 * (size_t)nd[0], X + 3 * (size_t)nd[1], m->b_young[e], m->b_poisson[e],
+                               m->b_area[e], m->b_i11[e], m->b_i22[e], m->b_i12[e], m->b_it[e], m->b_shear[e],
+                               m->b_axis + 3 * e, j->rel_tol, j->abs_tol, kg)) {
+      j->status = ORC_ERR_ZERO_LENGTH;
+      continue;
+    }
+    scatter_rows(&j->K, nrows, nd, 2, 6, kg, j->n0, j->n1);
+  }
+  for (size_t e = 0; e < m->n_plate; ++e) {
+    const int32_t* nd = m->p_nodes + 4 * e;
+    if (!touches(nd, 4, j->n0, j->n1)) continue;
+    if (orc_plate_global_matrix(X + 3 * (size_t)nd[0], X + 3 * (size_t)nd[1], X + 3 * (size_t)nd[2],
+                                X + 3 * (size_t)nd[3], m->p_young[e], m->p_poisson[e], m->p_thickness[e],
+                                m->p_shear[e], j->rel_tol, j->abs_tol, kg)) {
+      j->status = ORC_ERR_NODES_ON_LINE;
+      continue;
+    }
+    scatter_rows(&j->K, nrows, nd, 4, 6, kg, j->n0, j->n1);
+  }
   return NULL;
 }
 
-int orc_parallel_plates_assemble(const double* xyz, const int32_t* nodes4_idx, const double* young,
-                                 const double* poisson, const double* thickness, const double* shear, size_t n_elems,
-                                 double rel_tol, double abs_tol, int n_threads, double* element_out, double* seconds) {
+int orc_assemble_parallel(const orc_mesh_t* mesh, double rel_tol, double abs_tol, int n_threads, int64_t* row_ptr,
+                          int32_t* col_idx, double* values, int64_t values_cap, int64_t* nnz_out, double* seconds) {
   if (n_threads < 1) n_threads = 1;
+  uint64_t nrows = (uint64_t)mesh->nodes_number * 6u;
   pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)n_threads);
-  plate_job* jobs = (plate_job*)malloc(sizeof(plate_job) * (size_t)n_threads);
+  asm_job* jobs = (asm_job*)calloc((size_t)n_threads, sizeof(asm_job));
   struct timespec t0, t1;
   clock_gettime(CLOCK_MONOTONIC, &t0);
   for (int t = 0; t < n_threads; ++t) {
-    jobs[t].xyz = xyz;
-    jobs[t].nodes4 = nodes4_idx;
-    jobs[t].young = young;
-    jobs[t].poisson = poisson;
-    jobs[t].thickness = thickness;
-    jobs[t].shear = shear;
-    jobs[t].begin = n_elems * (size_t)t / (size_t)n_threads;
-    jobs[t].end = n_elems * (size_t)(t + 1) / (size_t)n_threads;
+    jobs[t].m = mesh;
     jobs[t].rel_tol = rel_tol;
     jobs[t].abs_tol = abs_tol;
-    jobs[t].out = element_out;
-    pthread_create(&th[t], NULL, plate_worker, &jobs[t]);
+    jobs[t].n0 = (size_t)mesh->nodes_number * (size_t)t / (size_t)n_threads;
+    jobs[t].n1 = (size_t)mesh->nodes_number * (size_t)(t + 1) / (size_t)n_threads;
+    u64map_init(&jobs[t].K, 4096);
+    pthread_create(&th[t], NULL, asm_worker, &jobs[t]);
   }
-  for (int t = 0; t < n_threads; ++t) pthread_join(th[t], NULL);
+  int st = ORC_OK;
+  for (int t = 0; t < n_threads; ++t) {
+    pthread_join(th[t], NULL);
+    if (jobs[t].status) st = jobs[t].status;
+  }
+  /* CSR: each thread's rows are a contiguous row range; count, then fill */
+  int64_t nnz = 0;
+  for (int t = 0; t < n_threads; ++t) nnz += (int64_t)jobs[t].K.len;
+  if (nnz_out) *nnz_out = nnz;
+  if (row_ptr && nnz <= values_cap) {
+    for (uint64_t r = 0; r <= nrows; ++r) row_ptr[r] = 0;
+    for (int t = 0; t < n_threads; ++t) {
+      u64map* K = &jobs[t].K;
+      for (size_t i = 0; i < K->cap; ++i)
+        if (K->keys[i]) row_ptr[(K->keys[i] - 1) / nrows + 1]++;
+    }
+    for (uint64_t r = 0; r < nrows; ++r) row_ptr[r + 1] += row_ptr[r];
+    int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (nrows + 1));
+    memcpy(fill, row_ptr, sizeof(int64_t) * (nrows + 1));
+    kv* e = (kv*)malloc(sizeof(kv) * (size_t)(nnz ? nnz : 1));
+    for (int t = 0; t < n_threads; ++t) {
+      u64map* K = &jobs[t].K;
+      for (size_t i = 0; i < K->cap; ++i)
+        if (K->keys[i]) {
+          uint64_t key = K->keys[i] - 1;
+          int64_t at = fill[key / nrows]++;
+          e[at].key = key;
+          memcpy(&e[at].val, &K->vals[i], 8);
+        }
+    }
+    for (uint64_t r = 0; r < nrows; ++r) {
+      int64_t b = row_ptr[r], n = row_ptr[r + 1] - b;
+      if (n > 1) qsort(e + b, (size_t)n, sizeof(kv), kv_cmp);
+      for (int64_t k = b; k < b + n; ++k) {
+        col_idx[k] = (int32_t)(e[k].key % nrows);
+        values[k] = e[k].val;
+      }
+    }
+    free(e);
+    free(fill);
+  }
   clock_gettime(CLOCK_MONOTONIC, &t1);
   *seconds = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+  for (int t = 0; t < n_threads; ++t) u64map_free(&jobs[t].K);
   free(th);
   free(jobs);
-  return ORC_OK;
+  return st;
 }

@@ -128,15 +128,29 @@ double orc_cos(double x);
 double orc_atan(double x);
 double orc_acos(double x);
 
-/* Multi-threaded numeric assembly of a whole mesh into a given CSR pattern,
- * used as the reference arm of the benchmark: element matrices are formed in
- * parallel and summed per entry in element order (bit-identical to the eager
- * path).  Elements are given in call order; kinds: 0 truss, 1 beam, 2 plate.
- * Returns elapsed seconds in *seconds. */
-int orc_parallel_plates_assemble(const double* xyz, const int32_t* nodes4_idx, const double* young,
-                                 const double* poisson, const double* thickness, const double* shear,
-                                 size_t n_elems, double rel_tol, double abs_tol, int n_threads,
-                                 double* element_out /* n_elems*576 or NULL */, double* seconds);
+/* A whole mesh by node index (0-based), elements in call order per kind:
+ * trusses, then beams, then plates.  t_area2 may be NULL (NaN = no taper). */
+typedef struct {
+  uint32_t nodes_number;
+  const double* xyz; /* nodes_number x 3 */
+  size_t n_truss;
+  const int32_t* t_nodes;
+  const double *t_young, *t_area, *t_area2;
+  size_t n_beam;
+  const int32_t* b_nodes;
+  const double *b_young, *b_poisson, *b_area, *b_i11, *b_i22, *b_i12, *b_it, *b_shear, *b_axis;
+  size_t n_plate;
+  const int32_t* p_nodes;
+  const double *p_young, *p_poisson, *p_thickness, *p_shear;
+} orc_mesh_t;
+
+/* Multi-threaded port of the eager assembly (no validation): n_threads
+ * threads own contiguous node ranges and sum their rows' entries in element
+ * call order, so the result is bit-identical to orc_add_* in that order.
+ * Writes the CSR when row_ptr is given and nnz <= values_cap; *nnz_out gets
+ * nnz, *seconds the wall time of assembly + CSR conversion. */
+int orc_assemble_parallel(const orc_mesh_t* mesh, double rel_tol, double abs_tol, int n_threads, int64_t* row_ptr,
+                          int32_t* col_idx, double* values, int64_t values_cap, int64_t* nnz_out, double* seconds);
 
 #ifdef __cplusplus
 }

@@ -65,8 +65,8 @@ def lib():
         for f in ("orc_sin", "orc_cos", "orc_atan", "orc_acos"):
             getattr(L, f).restype = c_double
             getattr(L, f).argtypes = [c_double]
-        L.orc_parallel_plates_assemble.argtypes = [dp, ip32, dp, dp, dp, dp, c_size_t, c_double, c_double, c_int,
-                                                   dp, dp]
+        L.orc_assemble_parallel.argtypes = [ctypes.POINTER(OrcMesh), c_double, c_double, c_int, i64p, ip32, dp,
+                                            c_int64, i64p, dp]
         _lib = L
     return _lib
 
@@ -249,20 +249,77 @@ def truss_rotation(x1, x2, rel_tol=1e-12, abs_tol=1e-12):
     return r.reshape(3, 3)
 
 
-def parallel_plates_element_matrices(xyz, nodes4_idx, young, poisson, thickness, shear, n_threads, keep=False,
-                                     rel_tol=1e-12, abs_tol=1e-12):
-    """Element matrices of many plates on n_threads host threads; returns (seconds, matrices or None)."""
+class OrcMesh(ctypes.Structure):
+    _fields_ = [("nodes_number", c_uint32), ("xyz", POINTER(c_double)),
+                ("n_truss", c_size_t), ("t_nodes", POINTER(c_int32)), ("t_young", POINTER(c_double)),
+                ("t_area", POINTER(c_double)), ("t_area2", POINTER(c_double)),
+                ("n_beam", c_size_t), ("b_nodes", POINTER(c_int32))]
+    _fields_ += [(f"b_{k}", POINTER(c_double)) for k in ("young", "poisson", "area", "i11", "i22", "i12", "it",
+                                                             "shear", "axis")]
+    _fields_ += [("n_plate", c_size_t), ("p_nodes", POINTER(c_int32))]
+    _fields_ += [(f"p_{k}", POINTER(c_double)) for k in ("young", "poisson", "thickness", "shear")]
+
+
+def mesh_struct(mesh):
+    """OrcMesh view of a finite_element_method_gb300.meshes.Mesh (node numbers 1..N in index order)."""
+    keep = []
+
+    def d(a, shape=None):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        keep.append(a)
+        return _p(a, c_double)
+
+    def i(a):
+        a = np.ascontiguousarray(np.asarray(a, dtype=np.int64) - 1, dtype=np.int32)
+        keep.append(a)
+        return _p(a, c_int32)
+
+    assert np.array_equal(mesh.node_numbers, np.arange(1, mesh.nodes_number + 1))
+    s = OrcMesh()
+    s.nodes_number = mesh.nodes_number
+    s.xyz = d(mesh.xyz)
+    t, b, p = mesh.trusses, mesh.beams, mesh.plates
+    if t is not None:
+        s.n_truss, s.t_nodes, s.t_young, s.t_area = len(t["numbers"]), i(t["nodes"]), d(t["young"]), d(t["area"])
+        s.t_area2 = d(t["area_2"]) if t.get("area_2") is not None else None
+    if b is not None:
+        s.n_beam, s.b_nodes = len(b["numbers"]), i(b["nodes"])
+        for k, src in (("young", "young"), ("poisson", "poisson"), ("area", "area"), ("i11", "i11"), ("i22", "i22"),
+                       ("i12", "i12"), ("it", "it"), ("shear", "shear_factor"), ("axis", "axis")):
+            setattr(s, f"b_{k}", d(b[src]))
+    if p is not None:
+        s.n_plate, s.p_nodes = len(p["numbers"]), i(p["nodes"])
+        for k, src in (("young", "young"), ("poisson", "poisson"), ("thickness", "thickness"),
+                       ("shear", "shear_factor")):
+            setattr(s, f"p_{k}", d(p[src]))
+    s._keep = keep
+    return s
+
+
+def assemble_parallel(mesh, n_threads, rel_tol=1e-12, abs_tol=1e-12, want_csr=True):
+    """Multi-threaded port of the eager assembly; returns (seconds, nnz, (row_ptr, col_idx, values) or None)."""
     L = lib()
-    m = len(nodes4_idx)
-    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
-    nd = np.ascontiguousarray(nodes4_idx, dtype=np.int32)
-    arrs = [np.ascontiguousarray(np.broadcast_to(v, (m,)), dtype=np.float64) for v in (young, poisson, thickness,
-                                                                                         shear)]
-    out = np.zeros((m, 576)) if keep else None
+    s = mesh_struct(mesh)
+    nnz = c_int64(0)
     sec = c_double(0)
-    L.orc_parallel_plates_assemble(_p(xyz, c_double), _p(nd, c_int32), *[_p(a, c_double) for a in arrs], m, rel_tol,
-                                   abs_tol, n_threads, _p(out, c_double) if keep else None, ctypes.byref(sec))
-    return sec.value, out
+    if not want_csr:
+        st = L.orc_assemble_parallel(ctypes.byref(s), rel_tol, abs_tol, n_threads, None, None, None, 0,
+                                     ctypes.byref(nnz), ctypes.byref(sec))
+        if st:
+            raise OracleError(st, "parallel assembly failed")
+        return sec.value, nnz.value, None
+    # size first with a cheap upper bound: every element entry distinct
+    cap = sum(len(d["numbers"]) * w for d, w in ((mesh.trusses, 36), (mesh.beams, 144), (mesh.plates, 576))
+              if d is not None)
+    rp = np.zeros(mesh.nodes_number * 6 + 1, np.int64)
+    ci = np.zeros(max(cap, 1), np.int32)
+    va = np.zeros(max(cap, 1), np.float64)
+    st = L.orc_assemble_parallel(ctypes.byref(s), rel_tol, abs_tol, n_threads, _p(rp, c_int64), _p(ci, c_int32),
+                                 _p(va, c_double), cap, ctypes.byref(nnz), ctypes.byref(sec))
+    if st:
+        raise OracleError(st, "parallel assembly failed")
+    n = nnz.value
+    return sec.value, n, (rp, ci[:n], va[:n])
 
 
 def sin(x):

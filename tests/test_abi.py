@@ -1,0 +1,41 @@
+"""CPU checks of the C ABI: the library builds for sm_103a, loads, and exports
+every entry point include/*.h declares (no compute calls: no GPU here)."""
+import ctypes
+import glob
+import os
+import re
+
+from finite_element_method_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(fem_gpu_\w+)\s*\(", src))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    names = declared_symbols()
+    assert len(names) >= 27
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header():
+    """every declared entry point has a ctypes signature (and no stale ones remain)."""
+    assert set(_lib.SIGNATURES) == declared_symbols()
+
+
+
+def test_no_gpu_call_surface_without_device():
+    """creating a handle allocates nothing on the device and succeeds without a GPU."""
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    assert lib.fem_gpu_create(1e-12, 1e-12, 4, ctypes.byref(h)) == 0
+    assert lib.fem_gpu_destroy(h) == 0
