@@ -122,13 +122,13 @@ class OracleFEM:
                                           ctypes.byref(n)))
         return n.value
 
-    def add_trusses(self, numbers, nodes, young, area, area2=None):
+    def add_trusses(self, numbers, nodes, young, area, area_2=None):
         m = len(numbers)
         numbers = np.ascontiguousarray(numbers, dtype=np.uint32)
         nodes = np.ascontiguousarray(nodes, dtype=np.uint32).reshape(m, 2)
         young = np.ascontiguousarray(np.broadcast_to(young, (m,)), dtype=np.float64)
         area = np.ascontiguousarray(np.broadcast_to(area, (m,)), dtype=np.float64)
-        a2 = np.full(m, np.nan) if area2 is None else np.ascontiguousarray(np.broadcast_to(area2, (m,)),
+        a2 = np.full(m, np.nan) if area_2 is None else np.ascontiguousarray(np.broadcast_to(area_2, (m,)),
                                                                           dtype=np.float64)
         n = c_size_t(0)
         self._check(self._L.orc_add_trusses(self._h, _p(numbers, c_uint32), _p(nodes, c_uint32), _p(young, c_double),
