@@ -66,7 +66,8 @@ enum {
   FEM_GPU_ERR_STATE = 31,          /* e.g. CSR requested before fem_gpu_assemble */
   FEM_GPU_ERR_CUDA = 40,           /* CUDA runtime failure or no device */
   FEM_GPU_ERR_OUT_OF_MEMORY = 41,
-  FEM_GPU_ERR_PATTERN_CHANGED = 42 /* numeric pass saw a non-zero outside the stored pattern */
+  FEM_GPU_ERR_PATTERN_CHANGED = 42, /* numeric pass saw a non-zero outside the stored pattern */
+  FEM_GPU_ERR_NOALLOC_LIMIT = 43    /* fem_gpu_assemble_dense_noalloc: structure above its fixed maximum */
 };
 
 /* FEM::create (fem.rs:34).  Allocates nothing on the device until the first add. */
@@ -146,6 +147,35 @@ int fem_gpu_numeric_launch_count(fem_gpu_t* h, int* n_launches);
 /* Per-kernel timing of the last numeric pass, measured with CUDA events on the
  * handle's stream (milliseconds): element kernels (all types) and the reduction. */
 int fem_gpu_last_numeric_timing(fem_gpu_t* h, float* element_ms, float* reduce_ms);
+
+/* Dense assembly of one small structure without any device allocation.
+ * No counterpart in the reference: it serves callers that cannot call
+ * cudaMalloc -- hosts that own all device memory through their own pool or
+ * arena, or that must keep a fixed memory footprint after set-up.  Every
+ * pointer except `stream` is DEVICE memory owned by the caller:
+ *   xyz          n_nodes x 3 coordinates, node index order
+ *   truss_nodes  n_truss x 2 node indices (0-based); truss_props n_truss x 3 (E, A, A2 or NaN)
+ *   beam_nodes   n_beam x 2; beam_props n_beam x 11 (E, nu, A, I11, I22, I12, It, shear factor,
+ *                local axis 1 x, y, z)
+ *   plate_nodes  n_plate x 4; plate_props n_plate x 4 (E, nu, thickness, shear factor)
+ *   K            (6 n_nodes) x (6 n_nodes) row-major, fully overwritten
+ * Elements are taken in the call order trusses, beams, plates, and every
+ * entry of K is the sum of its element contributions in that order -- the
+ * values fem_gpu_assemble puts in the CSR for the same model, with zeros
+ * where the CSR has no entry.  No validation beyond index range and
+ * degenerate geometry (FEM_GPU_ERR_ARGUMENT).  Working memory is one fixed
+ * device array of 32768 node-pair blocks (3 per truss or beam, 10 per
+ * plate; about 10 MB held by every GPU that loads the library): larger
+ * structures return FEM_GPU_ERR_NOALLOC_LIMIT.  The array's address is
+ * looked up on the first call on each device (make it before any stream
+ * capture); all calls share it, so calls that overlap on the GPU race and
+ * must be serialised by the caller.  Synchronises `stream` (a cudaStream_t,
+ * NULL = legacy default stream) before returning. */
+int fem_gpu_assemble_dense_noalloc(uint32_t n_nodes, const double* xyz, size_t n_truss, const int32_t* truss_nodes,
+                                   const double* truss_props, size_t n_beam, const int32_t* beam_nodes,
+                                   const double* beam_props, size_t n_plate, const int32_t* plate_nodes,
+                                   const double* plate_props, double rel_tol, double abs_tol, double* K,
+                                   void* stream);
 
 #ifdef __cplusplus
 }
