@@ -32,18 +32,23 @@ sys.path.insert(0, ROOT)
 
 from finite_element_method_gb300 import FEM, meshes  # noqa: E402
 
-# FP64 FMA throughput of a GB300 measured with a dependent-chain DFMA loop on all
-# 152 SMs at 2070 MHz (1.6 DFMA/clk/SM): 504.6e9 DFMA/s = 1.009e12 FP64 flop/s.
-FP64_PEAK_FLOPS = 1.009e12
+# FP64 peak of a GB300: 2 DFMA per clock per SM (ncu: sm__sass_thread_inst_executed_op_dfma_pred_on
+# peak_sustained = 304/cycle on 152 SMs) at the 2070 MHz maximum SM clock, FMA = 2 flops: 1.2586 TFLOP/s.
+# (A dependent-chain DFMA loop reached 1.009 TFLOP/s; the hardware figure is the stricter denominator.)
+FP64_PEAK_FLOPS = 2 * 152 * 2070e6 * 2
 
-# Algorithmic work per element of the numeric pass (counted from the kernels'
-# formulation: one FMA = 2 flops; bytes = compulsory HBM traffic of each kernel).
+# Algorithmic FP64 work per element of the numeric pass, counted from the kernels' formulation by
+# compiling element_math.cuh with an operation-counting double type (FMA = 2 flops, add/mul/div = 1):
+#   plate, R = I: core 70 add + 169 mul + 176 fma + 2 div, 10 node-pair blocks 56 mul + 154 fma
+#   beam: 57 add + 213 mul + 201 fma + 19 div + 7 sqrt (trig as polynomial fma chains)
+#   truss: 20 add + 46 mul + 9 fma + 4 div + 4 sqrt
 WORK = {
-    # plate, R = I (flat mesh in z = 0): core 552 flops + 10 node-pair blocks x 68 flops
-    "plate": dict(elem_flops=1232, pairs=10),
-    "beam": dict(elem_flops=1100, pairs=3),
-    "truss": dict(elem_flops=60, pairs=3),
+    "plate": dict(elem_flops=70 + 169 + 2 * 176 + 2 + 56 + 2 * 154, pairs=10),
+    "beam": dict(elem_flops=57 + 213 + 2 * 201 + 19 + 7, pairs=3),
+    "truss": dict(elem_flops=20 + 46 + 2 * 9 + 4 + 4, pairs=3),
 }
+# bytes per element read by the element kernel (connectivity, coordinates of its nodes, properties)
+IN_BYTES = {"plate": 4 * 4 + 4 * 24 + 4 * 8, "beam": 2 * 4 + 2 * 24 + 11 * 8, "truss": 2 * 4 + 2 * 24 + 3 * 8}
 
 
 def measured_peaks():
@@ -230,15 +235,15 @@ def main():
     # roofline of the dominant kernel
     hbm_gbs, peak_src = measured_peaks()
     w = WORK[args.workload]
-    pairs = w["pairs"] * n_el
-    # element kernels: write 36 doubles per node-pair block + read inputs (conn, coords, props)
-    in_bytes = {"plate": 16 + 4 * 24 + 32, "beam": 8 + 2 * 24 + 13 * 8, "truss": 8 + 2 * 24 + 24}[args.workload]
-    elem_bytes = pairs * 36 * 8 + n_el * in_bytes
-    # reduction: read every slot once + block metadata, write CSR values
-    red_bytes = pairs * 36 * 8 + nnz * 8
+    n_blocks, n_contrib, scratch = fem.pattern_stats()
+    # element kernels: inputs + per-contribution offset and mask (16 B) + packed blocks written to scratch
+    elem_bytes = n_el * IN_BYTES[args.workload] + n_contrib * 16 + scratch * 8
+    # reduction: packed scratch read once, CSR values written once, per-block metadata (masks, offset,
+    # count, node pair, 12 column offsets = 84 B) and the row pointers
+    red_bytes = scratch * 8 + nnz * 8 + n_blocks * 84 + (n_rows + 1) * 8
     t_e, t_r = float(np.mean(elem_ms)), float(np.mean(red_ms))
     kern = {"element": dict(ms=t_e, bytes=elem_bytes, flops=w["elem_flops"] * n_el),
-            "reduce": dict(ms=t_r, bytes=red_bytes, flops=0)}
+            "reduce": dict(ms=t_r, bytes=red_bytes, flops=scratch)}  # <= one FP64 add per packed entry
     dom = max(kern, key=lambda k: kern[k]["ms"])
     kd = kern[dom]
     gbs = kd["bytes"] / (kd["ms"] * 1e-3) / 1e9
@@ -249,11 +254,16 @@ def main():
                 "frac": frac_fp64}
     else:
         roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_gbs, "unit": "GB/s", "frac": frac_hbm}
-    roof.update({"kernel": dom, "traffic": None, "peak_source": f"{peak_src} (hbm); FP64 FMA loop (fp64)",
+    roof.update({"kernel": dom, "traffic": None,
+                 "peak_source": f"hbm: {peak_src} copy bandwidth; fp64: 2 DFMA/clk/SM x 152 SMs x 2070 MHz",
+                 "algorithmic": {k: {"bytes": int(v["bytes"]), "flops": int(v["flops"])} for k, v in kern.items()},
                  "per_kernel_ms": {k: v["ms"] for k, v in kern.items()},
                  "per_kernel_frac": {k: {"hbm": v["bytes"] / (v["ms"] * 1e-3) / 1e9 / hbm_gbs,
                                          "fp64": v["flops"] / (v["ms"] * 1e-3) / FP64_PEAK_FLOPS}
-                                     for k, v in kern.items()}})
+                                     for k, v in kern.items()},
+                 "pass_frac": {"hbm": (elem_bytes + red_bytes) / (t_step * 1e-3) / 1e9 / hbm_gbs,
+                               "fp64": (kern["element"]["flops"] + kern["reduce"]["flops"]) / (t_step * 1e-3)
+                               / FP64_PEAK_FLOPS}})
 
     # e2e: the drop-in call sequence from host arrays to a host CSR
     e2e_ms = []

@@ -473,10 +473,10 @@ struct PlateCore {
   double P14[6], P23[6], P1423[9];  // upper-triangle index for P14/P23
 };
 
-__device__ __forceinline__ int ut4(int i, int j) {  // 4x4 upper index, i <= j
+__host__ __device__ constexpr int ut4(int i, int j) {  // 4x4 upper index, i <= j
   return i == 0 ? j : i == 1 ? 3 + j : i == 2 ? 5 + j : 9;
 }
-__device__ __forceinline__ int ut3(int a, int b) {  // 3x3 upper index, a <= b
+__host__ __device__ constexpr int ut3(int a, int b) {  // 3x3 upper index, a <= b
   return a == 0 ? b : a == 1 ? 2 + b : 5;
 }
 
@@ -637,6 +637,63 @@ __device__ __forceinline__ void plate_local_block(const PlateCore& C, int i, int
       if (i == j) blk[6 * (2 + b) + 2 + a] = v;
     }
   if (i == j) blk[35] = 0.0 + 1.0;  // KROT6 (plate.rs:25, :716-721)
+}
+
+// The same block with the node pair fixed at compile time: every index, group
+// and sign of the assumed-strain shear terms folds to a constant, so the only
+// FP64 instructions left are the products and sums themselves (same operations,
+// same order, bit-identical to plate_local_block).
+template <int I, int J>
+__device__ __forceinline__ void plate_block_ct(const PlateCore& C, double blk[36]) {
+  static_assert(I <= J, "pairs are enumerated with I <= J");
+  constexpr int g0i = I < 2 ? 0 : 1, g0j = J < 2 ? 0 : 1;
+  constexpr bool n0i = I == 1 || I == 2, n0j = J == 1 || J == 2;
+  constexpr int g1i = (I == 0 || I == 3) ? 0 : 1, g1j = (J == 0 || J == 3) ? 0 : 1;
+  constexpr bool n1i = I >= 2, n1j = J >= 2;
+#pragma unroll
+  for (int k = 0; k < 36; ++k) blk[k] = 0.0;
+  const double Sxx = C.Sxx[ut4(I, J)], Syy = C.Syy[ut4(I, J)];
+  const double tuu = fma(C.gam, Syy, Sxx);
+  const double tvv = fma(C.gam, Sxx, Syy);
+  const double tuv_ij = fma(C.gam, C.Sxy[4 * J + I], C.nu * C.Sxy[4 * I + J]);
+  const double tuv_ji = fma(C.gam, C.Sxy[4 * I + J], C.nu * C.Sxy[4 * J + I]);
+  blk[0] = C.cmq * tuu;
+  blk[7] = C.cmq * tvv;
+  const double uv = C.cmq * tuv_ij;
+  blk[1] = uv;
+  blk[6] = (I == J) ? uv : C.cmq * tuv_ji;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      if (I == J && b < a) continue;
+      const int l3 = a < b ? a : b, h3 = a < b ? b : a;
+      double t1;
+      if (g1i == 0 && g1j == 0) t1 = C.P14[ut3(l3, h3)];
+      else if (g1i == 1 && g1j == 1) t1 = C.P23[ut3(l3, h3)];
+      else if (g1i == 0) t1 = C.P1423[3 * a + b];
+      else t1 = C.P1423[3 * b + a];
+      const bool neg1 = ((a == 0) && n1i) != ((b == 0) && n1j);
+      if (neg1) t1 = -t1;
+      double f, e;
+      if (g0i == 0 && g0j == 0) { f = C.F12[l3]; e = C.E12[h3]; }
+      else if (g0i == 1 && g0j == 1) { f = C.F43[l3]; e = C.E43[h3]; }
+      else if (g0i == 0) { f = C.G12[a]; e = C.E43[b]; }
+      else { f = C.G12[b]; e = C.E43[a]; }
+      const bool neg0 = ((a == 0) && n0i) != ((b == 0) && n0j);
+      if (neg0) f = -f;
+      const double sh = fma(f, e, t1);
+      double v = sh;
+      if (a >= 1 && b >= 1) {
+        if (a == 2 && b == 2) v = fma(C.cbq, tuu, sh);
+        else if (a == 1 && b == 1) v = fma(C.cbq, tvv, sh);
+        else if (a == 2 && b == 1) v = fma(-C.cbq, tuv_ij, sh);
+        else v = fma(-C.cbq, tuv_ji, sh);
+      }
+      blk[6 * (2 + a) + 2 + b] = v;
+      if (I == J) blk[6 * (2 + b) + 2 + a] = v;
+    }
+  if (I == J) blk[35] = 0.0 + 1.0;  // KROT6 (plate.rs:25, :716-721)
 }
 
 // rotate a local node-pair block to global axes: T^T K T restricted to (i, j)

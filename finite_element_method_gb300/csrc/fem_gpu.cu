@@ -233,12 +233,23 @@ __global__ void k_gen_pairs(int kind, const int32_t* __restrict__ n1, const int3
   }
 }
 
-// a 6x6 block in element orientation -> destination (mask bits or V slot),
-// transposed when the element's first node has the larger global index
+// v != 0.0 on the integer pipe (true for every value but +-0.0, NaN included):
+// on GB300 an FP64 compare occupies the same narrow pipe as the arithmetic.
+__device__ __forceinline__ bool nonzero(double v) { return (__double_as_longlong(v) << 1) != 0; }
+
+// a 6x6 block in element orientation -> destination, transposed (to the
+// block's (lower node, higher node) orientation) when the element's first node
+// of the pair has the larger global index.
+//   mask mode:    record the 36-bit mask of the block's non-zero entries;
+//   numeric mode: write the entries of the block's pattern, packed in row-major
+//                 order, at this contribution's offset in the compacted scratch V;
+//                 a non-zero outside the stored pattern raises *flag.
 struct BlockSink {
-  uint64_t* mask;        // mask mode: per (element, pair)
-  double* V;             // numeric mode
-  const uint32_t* slot;  // numeric mode: per (element, pair)
+  uint64_t* mask;                       // mask mode: per (element, pair)
+  double* V;                            // numeric mode
+  const unsigned long long* off;        // numeric mode: per (element, pair), in doubles
+  const uint64_t* bmask;                // numeric mode: per (element, pair), block orientation
+  int* flag;
   __device__ __forceinline__ void put(size_t ep, bool transpose, const double blk[36]) const {
     if (mask) {
       uint64_t m = 0;
@@ -247,23 +258,25 @@ struct BlockSink {
 #pragma unroll
         for (int b = 0; b < 6; ++b) {
           int e = transpose ? 6 * b + a : 6 * a + b;
-          if (blk[6 * a + b] != 0.0) m |= 1ull << e;
+          if (nonzero(blk[6 * a + b])) m |= 1ull << e;
         }
       mask[ep] = m;
     } else {
-      double* dst = V + (size_t)slot[ep] * 36;
-      if (!transpose) {
-        double2* d2 = reinterpret_cast<double2*>(dst);
+      const uint64_t m = bmask[ep];
+      double* dst = V + off[ep];
+      int r = 0;
+      bool outside = false;
 #pragma unroll
-        for (int k = 0; k < 18; ++k) d2[k] = make_double2(blk[2 * k], blk[2 * k + 1]);
-      } else {
-        double2* d2 = reinterpret_cast<double2*>(dst);
-#pragma unroll
-        for (int k = 0; k < 18; ++k) {
-          int e0 = 2 * k, e1 = 2 * k + 1;
-          d2[k] = make_double2(blk[6 * (e0 % 6) + e0 / 6], blk[6 * (e1 % 6) + e1 / 6]);
+      for (int en = 0; en < 36; ++en) {
+        const double v = transpose ? blk[6 * (en % 6) + en / 6] : blk[en];
+        if ((m >> en) & 1ull) {
+          dst[r] = v;
+          ++r;
+        } else {
+          outside |= nonzero(v);
         }
       }
+      if (outside) atomicOr(flag, 1);
     }
   }
 };
@@ -348,6 +361,20 @@ __global__ void __launch_bounds__(128) k_beam(NodesView nd, BeamView b, double r
   sink.put(e * kPairs2 + 2, false, blk);
 }
 
+template <int I, int J>
+__device__ __forceinline__ void plate_pair(const PlateCore& C, const double R[9], bool ident, const int nidx[4],
+                                           size_t ep, const BlockSink& sink) {
+  double blk[36];
+  plate_block_ct<I, J>(C, blk);
+  if (!ident) {
+    double o[36];
+    plate_rotate_block(R, I == J, blk, o);
+#pragma unroll
+    for (int k = 0; k < 36; ++k) blk[k] = o[k];
+  }
+  sink.put(ep, I != J && nidx[I] > nidx[J], blk);
+}
+
 __global__ void __launch_bounds__(128) k_plate(NodesView nd, PlateView pl, double abs_tol, size_t count,
                                                BlockSink sink) {
   size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -369,21 +396,19 @@ __global__ void __launch_bounds__(128) k_plate(NodesView nd, PlateView pl, doubl
   }
   PlateCore C;
   plate_core(xl, yl, pl.E[e], pl.nu[e], pl.t[e], pl.ks[e], C);
-  bool ident = is_identity(R);
-#pragma unroll 1
-  for (int p = 0; p < kPairs4; ++p) {
-    int i, j;
-    pair_nodes4(p, i, j);
-    double blk[36];
-    plate_local_block(C, i, j, blk);
-    if (!ident) {
-      double o[36];
-      plate_rotate_block(R, i == j, blk, o);
-#pragma unroll
-      for (int k = 0; k < 36; ++k) blk[k] = o[k];
-    }
-    sink.put(e * kPairs4 + p, i != j && nidx[i] > nidx[j], blk);
-  }
+  const bool ident = is_identity(R);
+  const size_t ep = e * kPairs4;
+  // node pairs in the order of pair_nodes4
+  plate_pair<0, 0>(C, R, ident, nidx, ep + 0, sink);
+  plate_pair<0, 1>(C, R, ident, nidx, ep + 1, sink);
+  plate_pair<0, 2>(C, R, ident, nidx, ep + 2, sink);
+  plate_pair<0, 3>(C, R, ident, nidx, ep + 3, sink);
+  plate_pair<1, 1>(C, R, ident, nidx, ep + 4, sink);
+  plate_pair<1, 2>(C, R, ident, nidx, ep + 5, sink);
+  plate_pair<1, 3>(C, R, ident, nidx, ep + 6, sink);
+  plate_pair<2, 2>(C, R, ident, nidx, ep + 7, sink);
+  plate_pair<2, 3>(C, R, ident, nidx, ep + 8, sink);
+  plate_pair<3, 3>(C, R, ident, nidx, ep + 9, sink);
 }
 
 // sorted position k: record the element pair's slot and its mask
@@ -535,44 +560,153 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
 }
 
 // ---------------------------------------------------------------------------
+// compacted scratch layout
+// ---------------------------------------------------------------------------
+// Block b stores count_b contributions of c_b = popcount(mask_b) doubles each,
+// contiguous and in element order, at blk_voff[b] (an exclusive scan of
+// count_b * c_b).
+__global__ void k_block_sizes(size_t nb, const uint32_t* __restrict__ blk_count, const uint64_t* __restrict__ blk_mask,
+                              unsigned long long* sizes) {
+  size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  sizes[b] = (unsigned long long)blk_count[b] * (unsigned long long)__popcll(blk_mask[b]);
+}
+
+// per element pair: its offset in V and its block's mask (block orientation)
+__global__ void k_pair_offsets(const uint32_t* __restrict__ svals, const uint32_t* __restrict__ incl, size_t n,
+                               const uint32_t* __restrict__ blk_start, const unsigned long long* __restrict__ blk_voff,
+                               const uint64_t* __restrict__ blk_mask, unsigned long long* off_t,
+                               unsigned long long* off_b, unsigned long long* off_p, uint64_t* bm_t, uint64_t* bm_b,
+                               uint64_t* bm_p) {
+  size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  uint32_t v = svals[k];
+  uint32_t kind = v >> 30, idx = v & 0x3fffffffu;
+  uint32_t b = incl[k] - 1;
+  uint64_t m = blk_mask[b];
+  unsigned long long off = blk_voff[b] + (unsigned long long)(k - blk_start[b]) * (unsigned long long)__popcll(m);
+  if (kind == kTruss) { off_t[idx] = off; bm_t[idx] = m; }
+  else if (kind == kBeam) { off_b[idx] = off; bm_b[idx] = m; }
+  else { off_p[idx] = off; bm_p[idx] = m; }
+}
+
+// ---------------------------------------------------------------------------
 // kernel: deterministic block reduction into CSR
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(288) k_reduce(size_t nb, const uint32_t* __restrict__ blk_start,
-                                                const uint32_t* __restrict__ blk_count,
-                                                const uint64_t* __restrict__ blk_mask,
-                                                const int32_t* __restrict__ blk_I, const int32_t* __restrict__ blk_J,
-                                                const int32_t* __restrict__ blk_colpos,
-                                                const int64_t* __restrict__ row_ptr, const double* __restrict__ V,
-                                                double* values, int* flag) {
-  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (t >= nb * 36) return;
-  size_t b = t / 36;
-  int en = (int)(t - b * 36);
-  int a = en / 6, c = en - 6 * (en / 6);
-  uint32_t s = blk_start[b], n = blk_count[b];
-  const double* src = V + (size_t)s * 36 + en;
-  double sum = src[0];
-  bool nz = sum != 0.0;
-  for (uint32_t k = 1; k < n; ++k) {
-    double v = src[(size_t)k * 36];
-    nz |= v != 0.0;
-    sum = sum + v;
-  }
-  uint64_t m = blk_mask[b];
-  bool inpat = (m >> en) & 1ull;
-  if (nz != inpat) atomicOr(flag, 1);
-  if (!inpat) return;
-  int32_t I = blk_I[b], J = blk_J[b];
-  uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
-  int64_t pos = row_ptr[6 * (int64_t)I + a] + blk_colpos[b * 12 + a] + __popc(rowbits & ((1u << c) - 1u));
-  values[pos] = sum;
-  if (I != J) {
-    uint32_t colbits = 0;
+// position of the n-th (0-based) set bit of a 36-bit mask
+__device__ __forceinline__ int nth_set_bit(uint64_t m, int n) {
+  uint32_t lo = (uint32_t)m;
+  int plo = __popc(lo);
+  if (n < plo) return (int)__fns(lo, 0, n + 1);
+  return 32 + (int)__fns((uint32_t)(m >> 32), 0, n - plo + 1);
+}
+
+constexpr int kRedThreads = 256;
+constexpr int kRedBlocks = 64;  // global blocks per CTA
+
+// One CTA reduces kRedBlocks consecutive global blocks: every pattern entry is
+// the sum of its block's contributions in element order (left to right, as the
+// reference's call-order accumulation), staged in shared memory, then written
+// to its CSR position in row-major order of the block and, for off-diagonal
+// blocks, in row-major order of the transposed block -- so consecutive threads
+// write consecutive CSR entries in both passes.  No atomics on values.
+__global__ void __launch_bounds__(kRedThreads) k_reduce(size_t nb, const uint32_t* __restrict__ blk_count,
+                                                        const uint64_t* __restrict__ blk_mask,
+                                                        const uint64_t* __restrict__ blk_maskT,
+                                                        const unsigned long long* __restrict__ blk_voff,
+                                                        const int32_t* __restrict__ blk_I,
+                                                        const int32_t* __restrict__ blk_J,
+                                                        const int32_t* __restrict__ blk_colpos,
+                                                        const int64_t* __restrict__ row_ptr,
+                                                        const double* __restrict__ V, double* __restrict__ values,
+                                                        int* flag) {
+  __shared__ uint64_t s_m[kRedBlocks], s_mT[kRedBlocks];
+  __shared__ unsigned long long s_voff[kRedBlocks];
+  __shared__ uint32_t s_cnt[kRedBlocks];
+  __shared__ int32_t s_I[kRedBlocks], s_J[kRedBlocks];
+  __shared__ int s_pre[kRedBlocks + 1];
+  __shared__ double s_sum[kRedBlocks * 36];
+  __shared__ uint8_t s_lb[kRedBlocks * 36];
+  const size_t b0 = (size_t)blockIdx.x * kRedBlocks;
+  const int nloc = (int)min((size_t)kRedBlocks, nb - b0);
+  const int tid = threadIdx.x;
+  if (tid < kRedBlocks) {
+    int c = 0;
+    if (tid < nloc) {
+      size_t b = b0 + tid;
+      uint64_t m = blk_mask[b];
+      s_m[tid] = m;
+      s_mT[tid] = blk_maskT[b];
+      s_voff[tid] = blk_voff[b];
+      s_cnt[tid] = blk_count[b];
+      s_I[tid] = blk_I[b];
+      s_J[tid] = blk_J[b];
+      c = __popcll(m);
+    }
+    // inclusive scan of the entry counts over the 64 blocks (two warps)
+    const int lane = tid & 31;
+    int x = c;
 #pragma unroll
-    for (int r = 0; r < 6; ++r) colbits |= (uint32_t)((m >> (6 * r + c)) & 1ull) << r;
-    int64_t pos2 = row_ptr[6 * (int64_t)J + c] + blk_colpos[b * 12 + 6 + c] + __popc(colbits & ((1u << a) - 1u));
-    values[pos2] = sum;
+    for (int d = 1; d < 32; d <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += y;
+    }
+    s_pre[tid + 1] = x;  // per-warp inclusive
   }
+  __syncthreads();
+  if (tid == 0) {
+    s_pre[0] = 0;
+    int w0 = s_pre[32];
+    for (int k = 33; k <= kRedBlocks; ++k) s_pre[k] += w0;
+  }
+  __syncthreads();
+  if (tid < nloc)
+    for (int t = s_pre[tid]; t < s_pre[tid + 1]; ++t) s_lb[t] = (uint8_t)tid;
+  __syncthreads();
+  const int E = s_pre[nloc];
+  bool bad = false;
+  // sums
+  for (int t = tid; t < E; t += kRedThreads) {
+    const int lb = s_lb[t];
+    const int c = s_pre[lb + 1] - s_pre[lb];
+    const int j = t - s_pre[lb];
+    const double* src = V + s_voff[lb] + j;
+    double sum = src[0];
+    bool nz = nonzero(sum);
+    const uint32_t n = s_cnt[lb];
+    for (uint32_t k = 1; k < n; ++k) {
+      double v = src[(size_t)k * c];
+      nz |= nonzero(v);
+      sum = sum + v;
+    }
+    bad |= !nz;
+    s_sum[t] = sum;
+  }
+  __syncthreads();
+  // row-major writes of the (I, J) block, then of its transpose (J, I)
+  for (int t = tid; t < E; t += kRedThreads) {
+    const int lb = s_lb[t];
+    const int j = t - s_pre[lb];
+    const size_t b = b0 + lb;
+    const uint64_t m = s_m[lb];
+    const int en = nth_set_bit(m, j);
+    const int a = en / 6, c = en - 6 * (en / 6);
+    const uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
+    const int64_t pos = row_ptr[6 * (int64_t)s_I[lb] + a] + blk_colpos[b * 12 + a] + __popc(rowbits & ((1u << c) - 1u));
+    values[pos] = s_sum[t];
+    if (s_I[lb] != s_J[lb]) {
+      const uint64_t mT = s_mT[lb];
+      const int enT = nth_set_bit(mT, j);  // j-th entry of the transposed block, row-major
+      const int cT = enT / 6, aT = enT - 6 * (enT / 6);
+      const int en0 = 6 * aT + cT;  // the same entry in the (I, J) block
+      const int j0 = __popcll(m & ((1ull << en0) - 1ull));
+      const uint32_t rowbitsT = (uint32_t)((mT >> (6 * cT)) & 63ull);
+      const int64_t pos2 =
+          row_ptr[6 * (int64_t)s_J[lb] + cT] + blk_colpos[b * 12 + 6 + cT] + __popc(rowbitsT & ((1u << aT) - 1u));
+      values[pos2] = s_sum[s_pre[lb] + j0];
+    }
+  }
+  if (bad) atomicOr(flag, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -722,6 +856,9 @@ struct fem_gpu {
   size_t n_blocks = 0;
   DevBuf<uint32_t> slot_t, slot_b, slot_p;
   DevBuf<uint64_t> mask_t, mask_b, mask_p;
+  DevBuf<unsigned long long> off_t, off_b, off_p, blk_voff;
+  DevBuf<uint64_t> bm_t, bm_b, bm_p;
+  size_t v_words = 0;
   DevBuf<double> V;
   DevBuf<uint32_t> blk_start, blk_count;
   DevBuf<uint64_t> blk_mask, blk_maskT;
@@ -853,6 +990,13 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   h->slot_t.release();
   h->slot_b.release();
   h->slot_p.release();
+  h->off_t.release();
+  h->off_b.release();
+  h->off_p.release();
+  h->blk_voff.release();
+  h->bm_t.release();
+  h->bm_b.release();
+  h->bm_p.release();
   h->mask_t.release();
   h->mask_b.release();
   h->mask_p.release();
@@ -1232,14 +1376,16 @@ int launch_elements(fem_gpu* h, BlockSink sink_t, BlockSink sink_b, BlockSink si
 int numeric_launch(fem_gpu* h) {
   CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->stream));
   CK(cudaEventRecord(h->ev[0], h->stream));
-  BlockSink st{nullptr, h->V.p, h->slot_t.p}, sb{nullptr, h->V.p, h->slot_b.p}, sp{nullptr, h->V.p, h->slot_p.p};
+  BlockSink st{nullptr, h->V.p, h->off_t.p, h->bm_t.p, h->flag.p};
+  BlockSink sb{nullptr, h->V.p, h->off_b.p, h->bm_b.p, h->flag.p};
+  BlockSink sp{nullptr, h->V.p, h->off_p.p, h->bm_p.p, h->flag.p};
   int r = launch_elements(h, st, sb, sp);
   if (r) return r;
   CK(cudaEventRecord(h->ev[1], h->stream));
   if (h->n_blocks)
-    k_reduce<<<grid_for(h->n_blocks * 36, 288), 288, 0, h->stream>>>(
-        h->n_blocks, h->blk_start.p, h->blk_count.p, h->blk_mask.p, h->blk_I.p, h->blk_J.p, h->blk_colpos.p,
-        h->row_ptr.p, h->V.p, h->values.p, h->flag.p);
+    k_reduce<<<grid_for(h->n_blocks, kRedBlocks), kRedThreads, 0, h->stream>>>(
+        h->n_blocks, h->blk_count.p, h->blk_mask.p, h->blk_maskT.p, h->blk_voff.p, h->blk_I.p, h->blk_J.p,
+        h->blk_colpos.p, h->row_ptr.p, h->V.p, h->values.p, h->flag.p);
   CK(cudaGetLastError());
   CK(cudaEventRecord(h->ev[2], h->stream));
   h->numeric_done = true;
@@ -1293,7 +1439,9 @@ int symbolic(fem_gpu* h) {
   CK(h->mask_b.reserve(h->nbm * kPairs2 + 1, s));
   CK(h->mask_p.reserve(h->np * kPairs4 + 1, s));
   {
-    BlockSink st{h->mask_t.p, nullptr, nullptr}, sb{h->mask_b.p, nullptr, nullptr}, sp{h->mask_p.p, nullptr, nullptr};
+    BlockSink st{h->mask_t.p, nullptr, nullptr, nullptr, nullptr};
+    BlockSink sb{h->mask_b.p, nullptr, nullptr, nullptr, nullptr};
+    BlockSink sp{h->mask_p.p, nullptr, nullptr, nullptr, nullptr};
     int r = launch_elements(h, st, sb, sp);
     if (r) return r;
   }
@@ -1341,6 +1489,32 @@ int symbolic(fem_gpu* h) {
     return cub::DeviceScan::ExclusiveSum(tmp, bytes, adj_n.p, adj_off.p, (int64_t)nb, s);
   });
   if (st) return st;
+  // compacted scratch: block offsets and, per element pair, its offset and mask
+  {
+    DevBuf<unsigned long long> sizes;
+    CK(sizes.reserve(nb + 1, s));
+    CK(h->blk_voff.reserve(nb + 1, s));
+    CK(cudaMemsetAsync(sizes.p + nb, 0, sizeof(unsigned long long), s));
+    k_block_sizes<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_mask.p, sizes.p);
+    st = cub_call(h, [&](void* tmp, size_t& bytes) {
+      return cub::DeviceScan::ExclusiveSum(tmp, bytes, sizes.p, h->blk_voff.p, (int64_t)(nb + 1), s);
+    });
+    if (st) return st;
+    unsigned long long total = 0;
+    CK(cudaMemcpyAsync(&total, h->blk_voff.p + nb, sizeof total, cudaMemcpyDeviceToHost, s));
+    CK(h->off_t.reserve(h->nt * kPairs2 + 1, s));
+    CK(h->off_b.reserve(h->nbm * kPairs2 + 1, s));
+    CK(h->off_p.reserve(h->np * kPairs4 + 1, s));
+    CK(h->bm_t.reserve(h->nt * kPairs2 + 1, s));
+    CK(h->bm_b.reserve(h->nbm * kPairs2 + 1, s));
+    CK(h->bm_p.reserve(h->np * kPairs4 + 1, s));
+    k_pair_offsets<<<grid_for(np, 256), 256, 0, s>>>(svals.p, incl.p, np, h->blk_start.p, h->blk_voff.p,
+                                                     h->blk_mask.p, h->off_t.p, h->off_b.p, h->off_p.p, h->bm_t.p,
+                                                     h->bm_b.p, h->bm_p.p);
+    CK(cudaStreamSynchronize(s));
+    sizes.release();
+    h->v_words = (size_t)total;
+  }
   uint32_t last_off = 0, last_n = 0;
   CK(cudaMemcpyAsync(&last_off, adj_off.p + nb - 1, sizeof last_off, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(&last_n, adj_n.p + nb - 1, sizeof last_n, cudaMemcpyDeviceToHost, s));
@@ -1397,7 +1571,7 @@ int symbolic(fem_gpu* h) {
                                                h->blk_maskT.p, h->blk_colpos.p, h->row_ptr.p, gbase.p, h->col_idx.p,
                                                h->nnz_group.p, h->g_row.p, h->g_col.p, h->g_kind.p);
   CK(cudaGetLastError());
-  CK(h->V.reserve(np * 36, s));
+  CK(h->V.reserve(h->v_words + 1, s));
   CK(cudaStreamSynchronize(s));
   // temporaries
   keys.release();
@@ -1613,6 +1787,16 @@ extern "C" int fem_gpu_get_stream(fem_gpu_t* h, void** stream) {
 extern "C" int fem_gpu_numeric_launch_count(fem_gpu_t* h, int* n_launches) {
   if (!h || !n_launches) return FEM_GPU_ERR_ARGUMENT;
   *n_launches = (h->nt ? 1 : 0) + (h->nbm ? 1 : 0) + (h->np ? 1 : 0) + (h->n_blocks ? 1 : 0);
+  return FEM_GPU_OK;
+}
+
+extern "C" int fem_gpu_get_pattern_stats(fem_gpu_t* h, int64_t* n_blocks, int64_t* n_contributions,
+                                         int64_t* scratch_doubles) {
+  if (!h) return FEM_GPU_ERR_ARGUMENT;
+  if (!h->pattern_valid) return h->fail(FEM_GPU_ERR_STATE, "call fem_gpu_assemble first");
+  if (n_blocks) *n_blocks = (int64_t)h->n_blocks;
+  if (n_contributions) *n_contributions = (int64_t)h->n_pairs;
+  if (scratch_doubles) *scratch_doubles = (int64_t)h->v_words;
   return FEM_GPU_OK;
 }
 

@@ -245,6 +245,12 @@ class FEM:
         self._check(self._L.fem_gpu_numeric_launch_count(self._h, ctypes.byref(n)))
         return n.value
 
+    def pattern_stats(self):
+        """(global node-pair blocks, element node-pair contributions, packed scratch doubles)."""
+        a, b, c = c_int64(0), c_int64(0), c_int64(0)
+        self._check(self._L.fem_gpu_get_pattern_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
     def last_numeric_timing(self):
         """(element kernels ms, reduction ms) of the last numeric pass, CUDA events on the handle's stream."""
         a, b = c_float(0), c_float(0)
