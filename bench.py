@@ -265,34 +265,67 @@ def main():
                                "fp64": (kern["element"]["flops"] + kern["reduce"]["flops"]) / (t_step * 1e-3)
                                / FP64_PEAK_FLOPS}})
 
-    # e2e: the drop-in call sequence from host arrays to a host CSR
-    e2e_ms = []
-    h2d = mesh.xyz.nbytes + mesh.node_numbers.nbytes
-    for d in (mesh.trusses, mesh.beams, mesh.plates):
+    # e2e: the drop-in call sequence from pinned host arrays to a pinned host CSR
+    def pinned(a):
+        """a copy of `a` in page-locked host memory (torch allocates it; numpy views it)."""
+        tdt = {1: torch.uint8, 4: torch.int32, 8: torch.int64}[a.dtype.itemsize]
+        t = torch.empty(a.shape, dtype=tdt, pin_memory=True)
+        out = t.numpy().view(a.dtype)
+        out[...] = a
+        return out, t
+
+    keep = []
+    pn, pt = pinned(mesh.node_numbers)
+    px, pxt = pinned(mesh.xyz)
+    keep += [pt, pxt]
+    pmesh = meshes.Mesh(mesh.name, pn, px)
+    for kind in ("trusses", "beams", "plates"):
+        d = getattr(mesh, kind)
         if d is not None:
-            h2d += sum(np.asarray(v).nbytes for k, v in d.items() if v is not None and k != "numbers")
+            pd = {}
+            for k, v in d.items():
+                if v is None:
+                    pd[k] = None
+                else:
+                    arr, t = pinned(np.ascontiguousarray(v))
+                    keep.append(t)
+                    pd[k] = arr
+            setattr(pmesh, kind, pd)
+    h2d = pmesh.xyz.nbytes + pmesh.node_numbers.nbytes
+    for d in (pmesh.trusses, pmesh.beams, pmesh.plates):
+        if d is not None:
+            h2d += sum(v.nbytes for k, v in d.items() if v is not None)
     d2h = (n_rows + 1) * 8 + nnz * (4 + 8)
-    rp = np.empty(n_rows + 1, np.int64)
-    ci = np.empty(nnz, np.int32)
-    va = np.empty(nnz, np.float64)
+    rp, t_rp = pinned(np.empty(n_rows + 1, np.int64))
+    ci, t_ci = pinned(np.empty(nnz, np.int32))
+    va, t_va = pinned(np.empty(nnz, np.float64))
+    from finite_element_method_gb300._lib import ptr
+    import ctypes
+
+    e2e_ms, phases = [], []
     for _ in range(args.e2e_steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         f2 = FEM(meshes.REL_TOL, meshes.ABS_TOL, mesh.nodes_number)
-        meshes.load(f2, mesh)
+        f2.add_nodes(pmesh.node_numbers, pmesh.xyz)
+        t1 = time.perf_counter()
+        meshes.load_elements(f2, pmesh)
+        t2 = time.perf_counter()
         f2.assemble()
-        from finite_element_method_gb300._lib import ptr
-        import ctypes
-
+        t3 = time.perf_counter()
         st = f2._L.fem_gpu_get_csr(f2.handle, ptr(rp, ctypes.c_int64), ptr(ci, ctypes.c_int32),
                                    ptr(va, ctypes.c_double))
         assert st == 0
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        t4 = time.perf_counter()
+        e2e_ms.append((t4 - t0) * 1e3)
+        phases.append([(t1 - t0) * 1e3, (t2 - t1) * 1e3, (t3 - t2) * 1e3, (t4 - t3) * 1e3])
         f2.close()
     e2e_t = float(np.median(e2e_ms))
+    ph = np.median(np.array(phases), axis=0)
     e2e = {"value": n_el * world / (e2e_t * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t,
-           "what": "create + add_nodes + add_* + assemble (symbolic + numeric) + CSR to host"}
+           "phases_ms": {"add_nodes": ph[0], "add_elements": ph[1], "assemble": ph[2], "csr_to_host": ph[3]},
+           "what": "create + add_nodes + add_* + assemble (symbolic + numeric) + CSR to host, pinned buffers"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

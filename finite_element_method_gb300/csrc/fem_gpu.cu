@@ -237,18 +237,36 @@ __global__ void k_gen_pairs(int kind, const int32_t* __restrict__ n1, const int3
 // on GB300 an FP64 compare occupies the same narrow pipe as the arithmetic.
 __device__ __forceinline__ bool nonzero(double v) { return (__double_as_longlong(v) << 1) != 0; }
 
+// Packing of a block's entries in the scratch.  A global block whose every
+// contribution is non-zero only inside the plate's structural set (membrane
+// 2x2 u-v, plate 3x3 w-thx-thy and, on diagonal blocks, the drilling thz-thz:
+// the shape of every flat-plate block, where R = I) stores 14 (diagonal) or 13
+// (off-diagonal) entries per contribution in a fixed order; any other block
+// stores all 36 row-major.  Both sets are closed under transposition.
+enum : uint32_t { kLayFull = 0, kLayDiag14 = 1, kLayOff13 = 2 };
+__constant__ int8_t c_lay_en[3][36] = {
+    {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17,
+     18, 19, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31, 32, 33, 34, 35},
+    {0, 1, 6, 7, 14, 15, 16, 20, 21, 22, 26, 27, 28, 35},
+    {0, 1, 6, 7, 14, 15, 16, 20, 21, 22, 26, 27, 28}};
+constexpr uint64_t kSetOff13 = (1ull << 0) | (1ull << 1) | (1ull << 6) | (1ull << 7) | (1ull << 14) | (1ull << 15) |
+                               (1ull << 16) | (1ull << 20) | (1ull << 21) | (1ull << 22) | (1ull << 26) |
+                               (1ull << 27) | (1ull << 28);
+constexpr uint64_t kSetDiag14 = kSetOff13 | (1ull << 35);
+__host__ __device__ constexpr int lay_size(uint32_t lay) { return lay == kLayFull ? 36 : lay == kLayDiag14 ? 14 : 13; }
+
 // a 6x6 block in element orientation -> destination, transposed (to the
 // block's (lower node, higher node) orientation) when the element's first node
 // of the pair has the larger global index.
 //   mask mode:    record the 36-bit mask of the block's non-zero entries;
-//   numeric mode: write the entries of the block's pattern, packed in row-major
-//                 order, at this contribution's offset in the compacted scratch V;
-//                 a non-zero outside the stored pattern raises *flag.
+//   numeric mode: write the block's packed entries at this contribution's
+//                 offset in the scratch V (offset in the low 62 bits of
+//                 pack[ep], packing in the top 2); a non-zero outside a
+//                 structural packing raises *flag (the pattern changed).
 struct BlockSink {
   uint64_t* mask;                       // mask mode: per (element, pair)
   double* V;                            // numeric mode
-  const unsigned long long* off;        // numeric mode: per (element, pair), in doubles
-  const uint64_t* bmask;                // numeric mode: per (element, pair), block orientation
+  const unsigned long long* pack;       // numeric mode: per (element, pair)
   int* flag;
   __device__ __forceinline__ void put(size_t ep, bool transpose, const double blk[36]) const {
     if (mask) {
@@ -261,23 +279,33 @@ struct BlockSink {
           if (nonzero(blk[6 * a + b])) m |= 1ull << e;
         }
       mask[ep] = m;
-    } else {
-      const uint64_t m = bmask[ep];
-      double* dst = V + off[ep];
-      int r = 0;
-      bool outside = false;
-#pragma unroll
-      for (int en = 0; en < 36; ++en) {
-        const double v = transpose ? blk[6 * (en % 6) + en / 6] : blk[en];
-        if ((m >> en) & 1ull) {
-          dst[r] = v;
-          ++r;
-        } else {
-          outside |= nonzero(v);
-        }
-      }
-      if (outside) atomicOr(flag, 1);
+      return;
     }
+    const unsigned long long pk = pack[ep];
+    const uint32_t lay = (uint32_t)(pk >> 62);
+    double* dst = V + (pk & ((1ull << 62) - 1ull));
+    if (lay == kLayFull) {
+#pragma unroll
+      for (int en = 0; en < 36; ++en) dst[en] = transpose ? blk[6 * (en % 6) + en / 6] : blk[en];
+      return;
+    }
+    // structural packings: the set is symmetric, so a transposed block packs its
+    // transposed entries at the same positions
+    const int8_t order[14] = {0, 1, 6, 7, 14, 15, 16, 20, 21, 22, 26, 27, 28, 35};
+    bool outside = false;
+#pragma unroll
+    for (int en = 0; en < 36; ++en) {
+      bool in = (kSetOff13 >> en) & 1ull;
+      if (!in && en != 35) outside |= nonzero(blk[en]);
+    }
+#pragma unroll
+    for (int j = 0; j < 13; ++j) {
+      const int en = order[j];
+      dst[j] = transpose ? blk[6 * (en % 6) + en / 6] : blk[en];
+    }
+    if (lay == kLayDiag14) dst[13] = blk[35];
+    else outside |= nonzero(blk[35]);
+    if (outside) atomicOr(flag, 1);
   }
 };
 
@@ -566,28 +594,37 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
 // contiguous and in element order, at blk_voff[b] (an exclusive scan of
 // count_b * c_b).
 __global__ void k_block_sizes(size_t nb, const uint32_t* __restrict__ blk_count, const uint64_t* __restrict__ blk_mask,
+                              const int32_t* __restrict__ blk_I, const int32_t* __restrict__ blk_J, uint8_t* blk_lay,
                               unsigned long long* sizes) {
   size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (b >= nb) return;
-  sizes[b] = (unsigned long long)blk_count[b] * (unsigned long long)__popcll(blk_mask[b]);
+  const uint64_t m = blk_mask[b];
+  uint32_t lay = kLayFull;
+  if (blk_I[b] == blk_J[b]) {
+    if ((m & ~kSetDiag14) == 0) lay = kLayDiag14;
+  } else if ((m & ~kSetOff13) == 0) {
+    lay = kLayOff13;
+  }
+  blk_lay[b] = (uint8_t)lay;
+  sizes[b] = (unsigned long long)blk_count[b] * (unsigned long long)lay_size(lay);
 }
 
-// per element pair: its offset in V and its block's mask (block orientation)
+// per element pair: its packed offset in V (low 62 bits) and the block's packing (top 2 bits)
 __global__ void k_pair_offsets(const uint32_t* __restrict__ svals, const uint32_t* __restrict__ incl, size_t n,
                                const uint32_t* __restrict__ blk_start, const unsigned long long* __restrict__ blk_voff,
-                               const uint64_t* __restrict__ blk_mask, unsigned long long* off_t,
-                               unsigned long long* off_b, unsigned long long* off_p, uint64_t* bm_t, uint64_t* bm_b,
-                               uint64_t* bm_p) {
+                               const uint8_t* __restrict__ blk_lay, unsigned long long* pk_t,
+                               unsigned long long* pk_b, unsigned long long* pk_p) {
   size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (k >= n) return;
   uint32_t v = svals[k];
   uint32_t kind = v >> 30, idx = v & 0x3fffffffu;
   uint32_t b = incl[k] - 1;
-  uint64_t m = blk_mask[b];
-  unsigned long long off = blk_voff[b] + (unsigned long long)(k - blk_start[b]) * (unsigned long long)__popcll(m);
-  if (kind == kTruss) { off_t[idx] = off; bm_t[idx] = m; }
-  else if (kind == kBeam) { off_b[idx] = off; bm_b[idx] = m; }
-  else { off_p[idx] = off; bm_p[idx] = m; }
+  const uint32_t lay = blk_lay[b];
+  unsigned long long off = blk_voff[b] + (unsigned long long)(k - blk_start[b]) * (unsigned long long)lay_size(lay);
+  off |= (unsigned long long)lay << 62;
+  if (kind == kTruss) pk_t[idx] = off;
+  else if (kind == kBeam) pk_b[idx] = off;
+  else pk_p[idx] = off;
 }
 
 // ---------------------------------------------------------------------------
@@ -604,15 +641,19 @@ __device__ __forceinline__ int nth_set_bit(uint64_t m, int n) {
 constexpr int kRedThreads = 256;
 constexpr int kRedBlocks = 64;  // global blocks per CTA
 
-// One CTA reduces kRedBlocks consecutive global blocks: every pattern entry is
+// One CTA reduces kRedBlocks consecutive global blocks: every packed entry is
 // the sum of its block's contributions in element order (left to right, as the
-// reference's call-order accumulation), staged in shared memory, then written
-// to its CSR position in row-major order of the block and, for off-diagonal
-// blocks, in row-major order of the transposed block -- so consecutive threads
-// write consecutive CSR entries in both passes.  No atomics on values.
+// reference's call-order accumulation), staged in shared memory, then the
+// pattern entries are written to their CSR positions in row-major order of the
+// block and, for off-diagonal blocks, in row-major order of the transposed block
+// -- consecutive threads write consecutive CSR entries in both passes.  No
+// atomics on values.  A packed entry outside the stored pattern that sums
+// contributions with a non-zero, or a pattern entry whose contributions are all
+// zero, raises *flag (the exact-zero pattern changed).
 __global__ void __launch_bounds__(kRedThreads) k_reduce(size_t nb, const uint32_t* __restrict__ blk_count,
                                                         const uint64_t* __restrict__ blk_mask,
                                                         const uint64_t* __restrict__ blk_maskT,
+                                                        const uint8_t* __restrict__ blk_lay,
                                                         const unsigned long long* __restrict__ blk_voff,
                                                         const int32_t* __restrict__ blk_I,
                                                         const int32_t* __restrict__ blk_J,
@@ -624,26 +665,34 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(size_t nb, const uint32_
   __shared__ unsigned long long s_voff[kRedBlocks];
   __shared__ uint32_t s_cnt[kRedBlocks];
   __shared__ int32_t s_I[kRedBlocks], s_J[kRedBlocks];
+  __shared__ uint8_t s_lay[kRedBlocks];
   __shared__ int s_pre[kRedBlocks + 1];
   __shared__ double s_sum[kRedBlocks * 36];
   __shared__ uint8_t s_lb[kRedBlocks * 36];
+  __shared__ int8_t s_pos[3][36];  // position of block entry en in each packing (-1: not packed)
   const size_t b0 = (size_t)blockIdx.x * kRedBlocks;
   const int nloc = (int)min((size_t)kRedBlocks, nb - b0);
   const int tid = threadIdx.x;
+  if (tid < 108) s_pos[tid / 36][tid % 36] = -1;
+  __syncthreads();
+  if (tid < 36) s_pos[0][tid] = (int8_t)tid;
+  if (tid < 14) s_pos[1][c_lay_en[1][tid]] = (int8_t)tid;
+  if (tid < 13) s_pos[2][c_lay_en[2][tid]] = (int8_t)tid;
   if (tid < kRedBlocks) {
     int c = 0;
     if (tid < nloc) {
       size_t b = b0 + tid;
-      uint64_t m = blk_mask[b];
-      s_m[tid] = m;
+      s_m[tid] = blk_mask[b];
       s_mT[tid] = blk_maskT[b];
       s_voff[tid] = blk_voff[b];
       s_cnt[tid] = blk_count[b];
       s_I[tid] = blk_I[b];
       s_J[tid] = blk_J[b];
-      c = __popcll(m);
+      const uint32_t lay = blk_lay[b];
+      s_lay[tid] = (uint8_t)lay;
+      c = lay_size(lay);
     }
-    // inclusive scan of the entry counts over the 64 blocks (two warps)
+    // inclusive scan of the packed sizes over the 64 blocks (two warps)
     const int lane = tid & 31;
     int x = c;
 #pragma unroll
@@ -665,7 +714,7 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(size_t nb, const uint32_
   __syncthreads();
   const int E = s_pre[nloc];
   bool bad = false;
-  // sums
+  // sums of the packed entries
   for (int t = tid; t < E; t += kRedThreads) {
     const int lb = s_lb[t];
     const int c = s_pre[lb + 1] - s_pre[lb];
@@ -679,31 +728,33 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(size_t nb, const uint32_
       nz |= nonzero(v);
       sum = sum + v;
     }
-    bad |= !nz;
+    const int en = c_lay_en[s_lay[lb]][j];
+    bad |= nz != (((s_m[lb] >> en) & 1ull) != 0);
     s_sum[t] = sum;
   }
   __syncthreads();
-  // row-major writes of the (I, J) block, then of its transpose (J, I)
+  // pattern entries: row-major writes of the (I, J) block, then of its transpose (J, I)
   for (int t = tid; t < E; t += kRedThreads) {
     const int lb = s_lb[t];
     const int j = t - s_pre[lb];
-    const size_t b = b0 + lb;
     const uint64_t m = s_m[lb];
+    if (j >= __popcll(m)) continue;
+    const size_t b = b0 + lb;
+    const int lay = s_lay[lb];
     const int en = nth_set_bit(m, j);
     const int a = en / 6, c = en - 6 * (en / 6);
     const uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
     const int64_t pos = row_ptr[6 * (int64_t)s_I[lb] + a] + blk_colpos[b * 12 + a] + __popc(rowbits & ((1u << c) - 1u));
-    values[pos] = s_sum[t];
+    values[pos] = s_sum[s_pre[lb] + s_pos[lay][en]];
     if (s_I[lb] != s_J[lb]) {
       const uint64_t mT = s_mT[lb];
       const int enT = nth_set_bit(mT, j);  // j-th entry of the transposed block, row-major
       const int cT = enT / 6, aT = enT - 6 * (enT / 6);
       const int en0 = 6 * aT + cT;  // the same entry in the (I, J) block
-      const int j0 = __popcll(m & ((1ull << en0) - 1ull));
       const uint32_t rowbitsT = (uint32_t)((mT >> (6 * cT)) & 63ull);
       const int64_t pos2 =
           row_ptr[6 * (int64_t)s_J[lb] + cT] + blk_colpos[b * 12 + 6 + cT] + __popc(rowbitsT & ((1u << aT) - 1u));
-      values[pos2] = s_sum[s_pre[lb] + j0];
+      values[pos2] = s_sum[s_pre[lb] + s_pos[lay][en0]];
     }
   }
   if (bad) atomicOr(flag, 1);
@@ -806,6 +857,98 @@ struct Run {
   size_t begin, count, pair_base;
 };
 
+uint64_t mix64(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return x;
+}
+
+// Open-addressing table of (64-bit key, value) with linear probing and
+// backward-shift deletion; several entries may share a key (the caller's
+// predicate tells them apart), so it serves as map, set and multimap.  The
+// registries behind add_node / add_* (duplicate numbers, node pairs, plate
+// node sets, exact coordinates) hold one entry per node or element.
+class FlatTable {
+ public:
+  FlatTable() { init(64); }
+  template <class Eq>
+  int64_t find(uint64_t key, Eq eq) const {
+    size_t i = mix64(key) & mask_;
+    while (val_[i] >= 0) {
+      if (key_[i] == key && eq(val_[i])) return val_[i];
+      i = (i + 1) & mask_;
+    }
+    return -1;
+  }
+  int64_t find(uint64_t key) const {
+    return find(key, [](int64_t) { return true; });
+  }
+  void insert(uint64_t key, int64_t v) {
+    if (2 * (len_ + 1) > key_.size()) grow();
+    put(key, v);
+  }
+  void erase(uint64_t key, int64_t v) {
+    size_t i = mix64(key) & mask_;
+    while (val_[i] >= 0 && !(key_[i] == key && val_[i] == v)) i = (i + 1) & mask_;
+    if (val_[i] < 0) return;
+    // backward-shift deletion
+    size_t j = i;
+    for (;;) {
+      j = (j + 1) & mask_;
+      if (val_[j] < 0) break;
+      size_t home = mix64(key_[j]) & mask_;
+      if (((j - home) & mask_) >= ((j - i) & mask_)) {
+        key_[i] = key_[j];
+        val_[i] = val_[j];
+        i = j;
+      }
+    }
+    val_[i] = -1;
+    --len_;
+  }
+  void reserve(size_t n) {
+    if (2 * n > key_.size()) rehash(n);
+  }
+
+ private:
+  void init(size_t cap) {
+    size_t c = 64;
+    while (c < cap) c <<= 1;
+    key_.assign(c, 0);
+    val_.assign(c, -1);
+    mask_ = c - 1;
+    len_ = 0;
+  }
+  void put(uint64_t key, int64_t v) {
+    size_t i = mix64(key) & mask_;
+    while (val_[i] >= 0) i = (i + 1) & mask_;
+    key_[i] = key;
+    val_[i] = v;
+    ++len_;
+  }
+  void rehash(size_t n) {
+    std::vector<uint64_t> k;
+    std::vector<int64_t> v;
+    k.swap(key_);
+    v.swap(val_);
+    init(4 * n);
+    for (size_t i = 0; i < k.size(); ++i)
+      if (v[i] >= 0) put(k[i], v[i]);
+  }
+  void grow() { rehash(len_ + 1); }
+  std::vector<uint64_t> key_;
+  std::vector<int64_t> val_;
+  size_t mask_ = 0, len_ = 0;
+};
+
+uint64_t coord_hash(const CoordKey& k) { return mix64(k.a ^ mix64(k.b ^ mix64(k.c))); }
+uint64_t set4_hash(const Set4& k) {
+  return mix64(((uint64_t)k.s[0] << 32 | k.s[1]) ^ mix64((uint64_t)k.s[2] << 32 | k.s[3]));
+}
+
 unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
 }  // namespace
@@ -821,8 +964,9 @@ struct fem_gpu {
   // nodes
   size_t n_nodes = 0;
   std::vector<uint32_t> idx_number;
-  std::unordered_map<uint32_t, int32_t> node_idx;
-  std::unordered_map<CoordKey, int32_t, CoordHash> node_coords;
+  std::vector<CoordKey> node_ck;  // normalised coordinate bits by index
+  FlatTable node_idx;             // number -> index
+  FlatTable node_coords;          // coordinate hash -> index
   DevBuf<double> dx, dy, dz;
   // elements
   std::vector<Run> runs;
@@ -830,22 +974,22 @@ struct fem_gpu {
   // truss
   size_t nt = 0;
   std::vector<uint32_t> t_num;
-  std::unordered_map<uint32_t, size_t> t_by_num;
-  std::unordered_set<uint64_t> t_pairs;
+  FlatTable t_by_num;  // number -> element index
+  FlatTable t_pairs;   // node pair -> element index
   DevBuf<int32_t> t_n1, t_n2;
   DevBuf<double> t_E, t_A, t_A2;
   // beam
   size_t nbm = 0;
   std::vector<uint32_t> b_num;
-  std::unordered_map<uint32_t, size_t> b_by_num;
-  std::unordered_set<uint64_t> b_pairs;
+  FlatTable b_by_num;
+  FlatTable b_pairs;
   DevBuf<int32_t> b_n1, b_n2;
   DevBuf<double> b_E, b_nu, b_A, b_i11, b_i22, b_i12, b_it, b_ks, b_ax, b_ay, b_az;
   // plate
   size_t np = 0;
   std::vector<uint32_t> p_num, p_nodes;
-  std::unordered_map<uint32_t, size_t> p_by_num;
-  std::unordered_map<Set4, int, Set4Hash> p_sets;
+  FlatTable p_by_num;
+  FlatTable p_sets;  // sorted node-number set hash -> element index
   DevBuf<int32_t> p_n1, p_n2, p_n3, p_n4;
   DevBuf<double> p_E, p_nu, p_t, p_ks;
   // validation scratch
@@ -856,8 +1000,8 @@ struct fem_gpu {
   size_t n_blocks = 0;
   DevBuf<uint32_t> slot_t, slot_b, slot_p;
   DevBuf<uint64_t> mask_t, mask_b, mask_p;
-  DevBuf<unsigned long long> off_t, off_b, off_p, blk_voff;
-  DevBuf<uint64_t> bm_t, bm_b, bm_p;
+  DevBuf<unsigned long long> off_t, off_b, off_p, blk_voff;  // packed offsets (offset | packing << 62)
+  DevBuf<uint8_t> blk_lay;
   size_t v_words = 0;
   DevBuf<double> V;
   DevBuf<uint32_t> blk_start, blk_count;
@@ -994,9 +1138,7 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   h->off_b.release();
   h->off_p.release();
   h->blk_voff.release();
-  h->bm_t.release();
-  h->bm_b.release();
-  h->bm_p.release();
+  h->blk_lay.release();
   h->mask_t.release();
   h->mask_b.release();
   h->mask_p.release();
@@ -1028,6 +1170,9 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
   if (st) return st;
   size_t start = h->n_nodes, k = 0;
   int code = FEM_GPU_OK;
+  h->node_idx.reserve(h->n_nodes + n);
+  h->node_coords.reserve(h->n_nodes + n);
+  h->node_ck.reserve(h->n_nodes + n);
   std::vector<double> xs, ys, zs;
   xs.reserve(n);
   ys.reserve(n);
@@ -1040,20 +1185,23 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
       code = h->fail(FEM_GPU_ERR_NODE_LIMIT, "Nodes number could not be greater than %u!", h->nodes_number);
       break;
     }
-    if (h->node_idx.count(num)) {
+    if (h->node_idx.find(num) >= 0) {
       code = h->fail(FEM_GPU_ERR_NODE_NUMBER, "Node with number %u already exists!", num);
       break;
     }
+    CoordKey ck = coord_key(x, y, z);
     if (x == x && y == y && z == z) {
-      CoordKey ck = coord_key(x, y, z);
-      if (h->node_coords.count(ck)) {
+      uint64_t hk = coord_hash(ck);
+      const std::vector<CoordKey>& known = h->node_ck;
+      if (h->node_coords.find(hk, [&](int64_t i) { return known[(size_t)i] == ck; }) >= 0) {
         code = h->fail(FEM_GPU_ERR_NODE_COORDS, "Node with coordinates x: %s, y: %s, z: %s already exists!",
                        rust_f64(x).c_str(), rust_f64(y).c_str(), rust_f64(z).c_str());
         break;
       }
-      h->node_coords.emplace(ck, (int32_t)index);
+      h->node_coords.insert(hk, (int64_t)index);
     }
-    h->node_idx.emplace(num, (int32_t)index);
+    h->node_idx.insert(num, (int64_t)index);
+    h->node_ck.push_back(ck);
     h->idx_number.push_back(num);
     xs.push_back(x);
     ys.push_back(y);
@@ -1075,9 +1223,9 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
 
 namespace {
 int lookup_node(fem_gpu* h, uint32_t num, int32_t* idx) {
-  auto it = h->node_idx.find(num);
-  if (it == h->node_idx.end()) return h->fail(FEM_GPU_ERR_NODE_NOT_EXIST, "Node with number %u does not exist!", num);
-  *idx = it->second;
+  int64_t i = h->node_idx.find(num);
+  if (i < 0) return h->fail(FEM_GPU_ERR_NODE_NOT_EXIST, "Node with number %u does not exist!", num);
+  *idx = (int32_t)i;
   return FEM_GPU_OK;
 }
 }  // namespace
@@ -1101,16 +1249,16 @@ extern "C" int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const 
     uint32_t num = numbers[k], u = nodes[2 * k], v = nodes[2 * k + 1];
     int32_t a, b;
     if ((host_code = lookup_node(h, u, &a)) || (host_code = lookup_node(h, v, &b))) break;
-    if (h->t_by_num.count(num)) {
+    if (h->t_by_num.find(num) >= 0) {
       host_code = h->fail(FEM_GPU_ERR_ELEM_NUMBER, "Truss element with number %u already exists!", num);
       break;
     }
-    if (h->t_pairs.count(pair_key(u, v))) {
+    if (h->t_pairs.find(pair_key(u, v)) >= 0) {
       host_code = h->fail(FEM_GPU_ERR_ELEM_SAME_NODES, "Truss element with node number %u and %u already exists!", u, v);
       break;
     }
-    h->t_by_num.emplace(num, h->nt + k);
-    h->t_pairs.insert(pair_key(u, v));
+    h->t_by_num.insert(num, (int64_t)(h->nt + k));
+    h->t_pairs.insert(pair_key(u, v), (int64_t)(h->nt + k));
     i1.push_back(a);
     i2.push_back(b);
     a2v.push_back(area2 ? area2[k] : NAN);
@@ -1133,8 +1281,8 @@ extern "C" int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const 
   if (st) return st;
   size_t accepted = std::min(m, bad);
   for (size_t j = accepted; j < m; ++j) {  // roll back registry entries past the failure
-    h->t_by_num.erase(numbers[j]);
-    h->t_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]));
+    h->t_by_num.erase(numbers[j], (int64_t)(base + j));
+    h->t_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]), (int64_t)(base + j));
   }
   for (size_t j = 0; j < accepted; ++j) h->t_num.push_back(numbers[j]);
   h->nt += accepted;
@@ -1180,16 +1328,16 @@ extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const ui
     uint32_t num = numbers[k], u = nodes[2 * k], v = nodes[2 * k + 1];
     int32_t a, b;
     if ((host_code = lookup_node(h, u, &a)) || (host_code = lookup_node(h, v, &b))) break;
-    if (h->b_by_num.count(num)) {
+    if (h->b_by_num.find(num) >= 0) {
       host_code = h->fail(FEM_GPU_ERR_ELEM_NUMBER, "Beam element with number %u already exists!", num);
       break;
     }
-    if (h->b_pairs.count(pair_key(u, v))) {
+    if (h->b_pairs.find(pair_key(u, v)) >= 0) {
       host_code = h->fail(FEM_GPU_ERR_ELEM_SAME_NODES, "Beam element with node number %u and %u already exists!", u, v);
       break;
     }
-    h->b_by_num.emplace(num, h->nbm + k);
-    h->b_pairs.insert(pair_key(u, v));
+    h->b_by_num.insert(num, (int64_t)(h->nbm + k));
+    h->b_pairs.insert(pair_key(u, v), (int64_t)(h->nbm + k));
     i1.push_back(a);
     i2.push_back(b);
     ax.push_back(local_axis[3 * k]);
@@ -1221,8 +1369,8 @@ extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const ui
   if (st) return st;
   size_t accepted = std::min(m, bad);
   for (size_t j = accepted; j < m; ++j) {
-    h->b_by_num.erase(numbers[j]);
-    h->b_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]));
+    h->b_by_num.erase(numbers[j], (int64_t)(base + j));
+    h->b_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]), (int64_t)(base + j));
   }
   for (size_t j = 0; j < accepted; ++j) h->b_num.push_back(numbers[j]);
   h->nbm += accepted;
@@ -1278,7 +1426,7 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
     for (int q = 0; q < 4 && okn; ++q)
       if ((host_code = lookup_node(h, nn[q], &ix[q]))) okn = false;
     if (!okn) break;
-    if (h->p_by_num.count(num)) {
+    if (h->p_by_num.find(num) >= 0) {
       host_code = h->fail(FEM_GPU_ERR_ELEM_NUMBER, "Plate element with number %u already exists!", num);
       break;
     }
@@ -1287,7 +1435,12 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
                     nn[2] != nn[3];
     bool same = false;
     if (distinct) {
-      same = h->p_sets.count(sorted4(nn)) > 0;
+      const Set4 key = sorted4(nn);
+      const size_t np0 = h->np;
+      same = h->p_sets.find(set4_hash(key), [&](int64_t e) {
+        const uint32_t* mm = (size_t)e < np0 ? &h->p_nodes[4 * (size_t)e] : nodes + 4 * ((size_t)e - np0);
+        return sorted4(mm) == key;
+      }) >= 0;
     } else {
       for (size_t e = 0; e < h->p_num.size() + k && !same; ++e) {
         const uint32_t* mm = e < h->p_num.size() ? &h->p_nodes[4 * e] : nodes + 4 * (e - h->p_num.size());
@@ -1301,8 +1454,8 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
                           nn[0], nn[1], nn[2], nn[3]);
       break;
     }
-    h->p_by_num.emplace(num, h->np + k);
-    h->p_sets[sorted4(nn)] += 1;
+    h->p_by_num.insert(num, (int64_t)(h->np + k));
+    h->p_sets.insert(set4_hash(sorted4(nn)), (int64_t)(h->np + k));
     for (int q = 0; q < 4; ++q) id[q].push_back(ix[q]);
   }
   if (host_code) host_err = h->err;
@@ -1326,9 +1479,8 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
   if (st) return st;
   size_t accepted = std::min(m, bad);
   for (size_t j = accepted; j < m; ++j) {
-    h->p_by_num.erase(numbers[j]);
-    auto it2 = h->p_sets.find(sorted4(nodes + 4 * j));
-    if (it2 != h->p_sets.end() && --it2->second == 0) h->p_sets.erase(it2);
+    h->p_by_num.erase(numbers[j], (int64_t)(base + j));
+    h->p_sets.erase(set4_hash(sorted4(nodes + 4 * j)), (int64_t)(base + j));
   }
   for (size_t j = 0; j < accepted; ++j) {
     h->p_num.push_back(numbers[j]);
@@ -1376,16 +1528,16 @@ int launch_elements(fem_gpu* h, BlockSink sink_t, BlockSink sink_b, BlockSink si
 int numeric_launch(fem_gpu* h) {
   CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->stream));
   CK(cudaEventRecord(h->ev[0], h->stream));
-  BlockSink st{nullptr, h->V.p, h->off_t.p, h->bm_t.p, h->flag.p};
-  BlockSink sb{nullptr, h->V.p, h->off_b.p, h->bm_b.p, h->flag.p};
-  BlockSink sp{nullptr, h->V.p, h->off_p.p, h->bm_p.p, h->flag.p};
+  BlockSink st{nullptr, h->V.p, h->off_t.p, h->flag.p};
+  BlockSink sb{nullptr, h->V.p, h->off_b.p, h->flag.p};
+  BlockSink sp{nullptr, h->V.p, h->off_p.p, h->flag.p};
   int r = launch_elements(h, st, sb, sp);
   if (r) return r;
   CK(cudaEventRecord(h->ev[1], h->stream));
   if (h->n_blocks)
     k_reduce<<<grid_for(h->n_blocks, kRedBlocks), kRedThreads, 0, h->stream>>>(
-        h->n_blocks, h->blk_count.p, h->blk_mask.p, h->blk_maskT.p, h->blk_voff.p, h->blk_I.p, h->blk_J.p,
-        h->blk_colpos.p, h->row_ptr.p, h->V.p, h->values.p, h->flag.p);
+        h->n_blocks, h->blk_count.p, h->blk_mask.p, h->blk_maskT.p, h->blk_lay.p, h->blk_voff.p, h->blk_I.p,
+        h->blk_J.p, h->blk_colpos.p, h->row_ptr.p, h->V.p, h->values.p, h->flag.p);
   CK(cudaGetLastError());
   CK(cudaEventRecord(h->ev[2], h->stream));
   h->numeric_done = true;
@@ -1439,9 +1591,9 @@ int symbolic(fem_gpu* h) {
   CK(h->mask_b.reserve(h->nbm * kPairs2 + 1, s));
   CK(h->mask_p.reserve(h->np * kPairs4 + 1, s));
   {
-    BlockSink st{h->mask_t.p, nullptr, nullptr, nullptr, nullptr};
-    BlockSink sb{h->mask_b.p, nullptr, nullptr, nullptr, nullptr};
-    BlockSink sp{h->mask_p.p, nullptr, nullptr, nullptr, nullptr};
+    BlockSink st{h->mask_t.p, nullptr, nullptr, nullptr};
+    BlockSink sb{h->mask_b.p, nullptr, nullptr, nullptr};
+    BlockSink sp{h->mask_p.p, nullptr, nullptr, nullptr};
     int r = launch_elements(h, st, sb, sp);
     if (r) return r;
   }
@@ -1494,8 +1646,10 @@ int symbolic(fem_gpu* h) {
     DevBuf<unsigned long long> sizes;
     CK(sizes.reserve(nb + 1, s));
     CK(h->blk_voff.reserve(nb + 1, s));
+    CK(h->blk_lay.reserve(nb + 1, s));
     CK(cudaMemsetAsync(sizes.p + nb, 0, sizeof(unsigned long long), s));
-    k_block_sizes<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_mask.p, sizes.p);
+    k_block_sizes<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_mask.p, h->blk_I.p, h->blk_J.p,
+                                                    h->blk_lay.p, sizes.p);
     st = cub_call(h, [&](void* tmp, size_t& bytes) {
       return cub::DeviceScan::ExclusiveSum(tmp, bytes, sizes.p, h->blk_voff.p, (int64_t)(nb + 1), s);
     });
@@ -1505,12 +1659,8 @@ int symbolic(fem_gpu* h) {
     CK(h->off_t.reserve(h->nt * kPairs2 + 1, s));
     CK(h->off_b.reserve(h->nbm * kPairs2 + 1, s));
     CK(h->off_p.reserve(h->np * kPairs4 + 1, s));
-    CK(h->bm_t.reserve(h->nt * kPairs2 + 1, s));
-    CK(h->bm_b.reserve(h->nbm * kPairs2 + 1, s));
-    CK(h->bm_p.reserve(h->np * kPairs4 + 1, s));
     k_pair_offsets<<<grid_for(np, 256), 256, 0, s>>>(svals.p, incl.p, np, h->blk_start.p, h->blk_voff.p,
-                                                     h->blk_mask.p, h->off_t.p, h->off_b.p, h->off_p.p, h->bm_t.p,
-                                                     h->bm_b.p, h->bm_p.p);
+                                                     h->blk_lay.p, h->off_t.p, h->off_b.p, h->off_p.p);
     CK(cudaStreamSynchronize(s));
     sizes.release();
     h->v_words = (size_t)total;
@@ -1735,21 +1885,21 @@ extern "C" int fem_gpu_get_groups(fem_gpu_t* h, int32_t* row_node, int32_t* col_
 namespace {
 int rotation_of(fem_gpu* h, int kind, uint32_t number, double* r9) {
   if (!h || !r9) return FEM_GPU_ERR_ARGUMENT;
-  const std::unordered_map<uint32_t, size_t>& m = kind == kTruss ? h->t_by_num : kind == kBeam ? h->b_by_num : h->p_by_num;
-  auto it = m.find(number);
+  const FlatTable& m = kind == kTruss ? h->t_by_num : kind == kBeam ? h->b_by_num : h->p_by_num;
+  const int64_t found = m.find(number);
   const char* nm = kind == kTruss ? "Truss" : kind == kBeam ? "Beam" : "Plate";
-  if (it == m.end()) return h->fail(FEM_GPU_ERR_ARGUMENT, "%s element with number %u does not exist!", nm, number);
+  if (found < 0) return h->fail(FEM_GPU_ERR_ARGUMENT, "%s element with number %u does not exist!", nm, number);
   DevBuf<double> out;
   CK(out.reserve(9, h->stream));
   if (kind == kTruss)
     k_rotation<<<1, 1, 0, h->stream>>>(kind, h->nodes(), h->t_n1.p, h->t_n2.p, nullptr, nullptr, h->beams(), h->rel_tol,
-                                       h->abs_tol, it->second, out.p);
+                                       h->abs_tol, (size_t)found, out.p);
   else if (kind == kBeam)
     k_rotation<<<1, 1, 0, h->stream>>>(kind, h->nodes(), nullptr, nullptr, nullptr, nullptr, h->beams(), h->rel_tol,
-                                       h->abs_tol, it->second, out.p);
+                                       h->abs_tol, (size_t)found, out.p);
   else
     k_rotation<<<1, 1, 0, h->stream>>>(kind, h->nodes(), h->p_n1.p, h->p_n2.p, h->p_n3.p, h->p_n4.p, h->beams(),
-                                       h->rel_tol, h->abs_tol, it->second, out.p);
+                                       h->rel_tol, h->abs_tol, (size_t)found, out.p);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(r9, out.p, 9 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));

@@ -228,6 +228,11 @@ def batch_structures(n_structures=512, lo=1e3, hi=2e5, seed=4, kinds=("truss", "
 def load(model, mesh: Mesh) -> None:
     """Add the mesh's nodes and elements to `model` (reference add_* API), in call order."""
     model.add_nodes(mesh.node_numbers, mesh.xyz)
+    load_elements(model, mesh)
+
+
+def load_elements(model, mesh: Mesh) -> None:
+    """Add the mesh's elements (nodes already added), in call order."""
     for kind in mesh.order:
         d = getattr(mesh, kind)
         if d is None or len(d["numbers"]) == 0:
