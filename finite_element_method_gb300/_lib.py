@@ -46,7 +46,7 @@ SIGNATURES = {
     "fem_gpu_get_stream": (c_int, [hp, POINTER(c_void_p)]),
     "fem_gpu_numeric_launch_count": (c_int, [hp, POINTER(c_int)]),
     "fem_gpu_last_numeric_timing": (c_int, [hp, fp, fp]),
-    "fem_gpu_get_pattern_stats": (c_int, [hp, i64p, i64p, i64p]),
+    "fem_gpu_get_pattern_stats": (c_int, [hp, i64p, i64p, i64p, i64p]),
     "fem_gpu_assemble_dense_noalloc": (c_int, [c_uint32, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p,
                                                c_void_p, c_size_t, c_void_p, c_void_p, c_double, c_double, c_void_p,
                                                c_void_p]),

@@ -595,7 +595,7 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
 // count_b * c_b).
 __global__ void k_block_sizes(size_t nb, const uint32_t* __restrict__ blk_count, const uint64_t* __restrict__ blk_mask,
                               const int32_t* __restrict__ blk_I, const int32_t* __restrict__ blk_J, uint8_t* blk_lay,
-                              unsigned long long* sizes) {
+                              uint64_t* blk_pmask, unsigned long long* sizes) {
   size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (b >= nb) return;
   const uint64_t m = blk_mask[b];
@@ -606,6 +606,11 @@ __global__ void k_block_sizes(size_t nb, const uint32_t* __restrict__ blk_count,
     lay = kLayOff13;
   }
   blk_lay[b] = (uint8_t)lay;
+  // the pattern over packed positions: bit j set when packed entry j is a pattern entry
+  uint64_t pm = 0;
+  for (int j = 0; j < lay_size(lay); ++j)
+    if ((m >> c_lay_en[lay][j]) & 1ull) pm |= 1ull << j;
+  blk_pmask[b] = pm;
   sizes[b] = (unsigned long long)blk_count[b] * (unsigned long long)lay_size(lay);
 }
 
@@ -639,125 +644,204 @@ __device__ __forceinline__ int nth_set_bit(uint64_t m, int n) {
 }
 
 constexpr int kRedThreads = 256;
-constexpr int kRedBlocks = 64;  // global blocks per CTA
+constexpr int kRedLanes = 16;                        // lanes per global block
+constexpr int kRedBlocks = kRedThreads / kRedLanes;  // global blocks per CTA
+constexpr int kFlagPattern = 1;                      // bit of *flag: the exact-zero pattern changed
 
-// One CTA reduces kRedBlocks consecutive global blocks: every packed entry is
-// the sum of its block's contributions in element order (left to right, as the
-// reference's call-order accumulation), staged in shared memory, then the
-// pattern entries are written to their CSR positions in row-major order of the
-// block and, for off-diagonal blocks, in row-major order of the transposed block
-// -- consecutive threads write consecutive CSR entries in both passes.  No
-// atomics on values.  A packed entry outside the stored pattern that sums
-// contributions with a non-zero, or a pattern entry whose contributions are all
-// zero, raises *flag (the exact-zero pattern changed).
-__global__ void __launch_bounds__(kRedThreads) k_reduce(size_t nb, const uint32_t* __restrict__ blk_count,
-                                                        const uint64_t* __restrict__ blk_mask,
-                                                        const uint64_t* __restrict__ blk_maskT,
-                                                        const uint8_t* __restrict__ blk_lay,
-                                                        const unsigned long long* __restrict__ blk_voff,
-                                                        const int32_t* __restrict__ blk_I,
-                                                        const int32_t* __restrict__ blk_J,
-                                                        const int32_t* __restrict__ blk_colpos,
-                                                        const int64_t* __restrict__ row_ptr,
-                                                        const double* __restrict__ V, double* __restrict__ values,
-                                                        int* flag) {
-  __shared__ uint64_t s_m[kRedBlocks], s_mT[kRedBlocks];
-  __shared__ unsigned long long s_voff[kRedBlocks];
-  __shared__ uint32_t s_cnt[kRedBlocks];
-  __shared__ int32_t s_I[kRedBlocks], s_J[kRedBlocks];
-  __shared__ uint8_t s_lay[kRedBlocks];
-  __shared__ int s_pre[kRedBlocks + 1];
-  __shared__ double s_sum[kRedBlocks * 36];
-  __shared__ uint8_t s_lb[kRedBlocks * 36];
-  __shared__ int8_t s_pos[3][36];  // position of block entry en in each packing (-1: not packed)
-  const size_t b0 = (size_t)blockIdx.x * kRedBlocks;
-  const int nloc = (int)min((size_t)kRedBlocks, nb - b0);
-  const int tid = threadIdx.x;
-  if (tid < 108) s_pos[tid / 36][tid % 36] = -1;
-  __syncthreads();
-  if (tid < 36) s_pos[0][tid] = (int8_t)tid;
-  if (tid < 14) s_pos[1][c_lay_en[1][tid]] = (int8_t)tid;
-  if (tid < 13) s_pos[2][c_lay_en[2][tid]] = (int8_t)tid;
-  if (tid < kRedBlocks) {
-    int c = 0;
-    if (tid < nloc) {
-      size_t b = b0 + tid;
-      s_m[tid] = blk_mask[b];
-      s_mT[tid] = blk_maskT[b];
-      s_voff[tid] = blk_voff[b];
-      s_cnt[tid] = blk_count[b];
-      s_I[tid] = blk_I[b];
-      s_J[tid] = blk_J[b];
-      const uint32_t lay = blk_lay[b];
-      s_lay[tid] = (uint8_t)lay;
-      c = lay_size(lay);
-    }
-    // inclusive scan of the packed sizes over the 64 blocks (two warps)
-    const int lane = tid & 31;
-    int x = c;
+// Block-sum slots.  A packed entry of a block with one contribution needs no
+// sum: its CSR value is gathered straight from the scratch.  Entries of blocks
+// with 2, 3, 4 and 5+ contributions get a slot in S, grouped by that count so a
+// warp adds the same number of terms on every lane (on GB300 the FP64 adds of
+// the reduction are themselves a throughput limit).  Blocks with one
+// contribution keep a check-only descriptor for each packed entry outside the
+// pattern (to see the exact-zero pattern change).  Categories: 0 = one
+// contribution, 1..4 = 2, 3, 4, 5+ contributions.
+constexpr int kSlotCats = 5;
+__host__ __device__ __forceinline__ int slot_cat(uint32_t count) { return count <= 1 ? 0 : count >= 5 ? 4 : (int)count - 1; }
+
+__global__ void k_slot_sizes(size_t nb, const uint32_t* __restrict__ blk_count, const uint64_t* __restrict__ blk_pmask,
+                             const uint8_t* __restrict__ blk_lay, unsigned long long* sz /* kSlotCats x (nb + 1) */) {
+  size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const int c = lay_size(blk_lay[b]);
+  const int cat = slot_cat(blk_count[b]);
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, x, d);
-      if (lane >= d) x += y;
+  for (int g = 0; g < kSlotCats; ++g) sz[(size_t)g * (nb + 1) + b] = 0;
+  sz[(size_t)cat * (nb + 1) + b] = cat == 0 ? (unsigned long long)(c - __popcll(blk_pmask[b])) : (unsigned long long)c;
+}
+
+struct SlotLayout {
+  const unsigned long long* base;  // kSlotCats x (nb + 1): per category, exclusive scan over blocks
+  size_t stride;                   // nb + 1
+  unsigned long long off[kSlotCats];  // first descriptor of each category (category 0 last)
+  unsigned long long vs_off;          // S starts at this scratch position
+};
+
+// position of a block entry in its packing (-1: not packed)
+__device__ __forceinline__ int packed_pos(uint32_t lay, int en) {
+  if (lay == kLayFull) return en;
+  const int n = lay_size(lay);
+  int p = -1;
+  for (int q = 0; q < n; ++q)
+    if (c_lay_en[lay][q] == en) p = q;
+  return p;
+}
+
+// Symbolic, once per pattern: the source of every CSR entry -- the scratch
+// position of its packed entry when its block has one contribution, otherwise
+// its S slot (both in one buffer: S starts at vs_off), for the (I, J) block
+// entry and for the transposed entry of the (J, I) block below the diagonal.
+__global__ void k_csr_sources(size_t nb, const uint64_t* __restrict__ blk_mask, const uint64_t* __restrict__ blk_maskT,
+                              const uint8_t* __restrict__ blk_lay, const uint32_t* __restrict__ blk_count,
+                              const unsigned long long* __restrict__ blk_voff, SlotLayout L,
+                              const int32_t* __restrict__ blk_I, const int32_t* __restrict__ blk_J,
+                              const int32_t* __restrict__ blk_colpos, const int64_t* __restrict__ row_ptr,
+                              uint32_t* src_map) {
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= nb * 36) return;
+  const size_t b = t / 36;
+  const int j = (int)(t - 36 * b);
+  const uint64_t m = blk_mask[b];
+  if (j >= __popcll(m)) return;
+  const uint32_t lay = blk_lay[b];
+  const int cat = slot_cat(blk_count[b]);
+  const unsigned long long sb =
+      cat == 0 ? blk_voff[b] : L.vs_off + L.off[cat] + L.base[(size_t)cat * L.stride + b];
+  const int32_t I = blk_I[b], J = blk_J[b];
+  const int en = nth_set_bit(m, j);
+  const int a = en / 6, c = en - 6 * (en / 6);
+  const uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
+  const int64_t pos = row_ptr[6 * (int64_t)I + a] + blk_colpos[b * 12 + a] + __popc(rowbits & ((1u << c) - 1u));
+  src_map[pos] = (uint32_t)(sb + (unsigned long long)packed_pos(lay, en));
+  if (I != J) {
+    const uint64_t mT = blk_maskT[b];
+    const int enT = nth_set_bit(mT, j);  // j-th entry of the transposed block, row-major
+    const int cT = enT / 6, aT = enT - 6 * (enT / 6);
+    const uint32_t rowbitsT = (uint32_t)((mT >> (6 * cT)) & 63ull);
+    const int64_t pos2 =
+        row_ptr[6 * (int64_t)J + cT] + blk_colpos[b * 12 + 6 + cT] + __popc(rowbitsT & ((1u << aT) - 1u));
+    src_map[pos2] = (uint32_t)(sb + (unsigned long long)packed_pos(lay, 6 * aT + cT));
+  }
+}
+
+// Symbolic, once per pattern: the descriptors -- the scratch position of the
+// first contribution, the number of contributions (bits 0-23), the packed
+// block size, i.e. the stride between contributions (bits 24-30), and whether
+// the entry is a pattern entry (bit 31).
+__global__ void k_slot_desc(size_t nb, const uint32_t* __restrict__ blk_count, const uint64_t* __restrict__ blk_pmask,
+                            const uint8_t* __restrict__ blk_lay, const unsigned long long* __restrict__ blk_voff,
+                            SlotLayout L, uint2* desc, int* too_many) {
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= nb * 36) return;
+  const size_t b = t / 36;
+  const int j = (int)(t - 36 * b);
+  const int c = lay_size(blk_lay[b]);
+  if (j >= c) return;
+  const uint32_t cnt = blk_count[b];
+  if (cnt >= (1u << 24)) atomicOr(too_many, 1);
+  const uint64_t pm = blk_pmask[b];
+  const uint32_t inpat = (uint32_t)((pm >> j) & 1ull);
+  const int cat = slot_cat(cnt);
+  unsigned long long at;
+  if (cat == 0) {
+    if (inpat) return;  // gathered straight from the scratch
+    at = L.off[0] + L.base[b] + (unsigned long long)__popcll(~pm & ((1ull << j) - 1ull));
+  } else {
+    at = L.off[cat] + L.base[(size_t)cat * L.stride + b] + (unsigned long long)j;
+  }
+  desc[at] = make_uint2((uint32_t)(blk_voff[b] + (unsigned long long)j), (cnt & 0xffffffu) | ((uint32_t)c << 24) |
+                                                                              (inpat << 31));
+}
+
+// Numeric pass, part 1: one thread per descriptor.  Slots in S (descriptors
+// below n_sums) sum their contributions in element order (left to right, as
+// the reference's call-order accumulation): descriptors are grouped by
+// contribution count, so every lane of a warp adds the same number of terms.
+// Check-only descriptors (one contribution, outside the pattern) only test
+// their entry.  No atomics on values.  A non-pattern entry with a non-zero, or
+// a pattern slot whose contributions are all zero, raises kFlagPattern (the
+// exact-zero pattern changed).
+__global__ void __launch_bounds__(256) k_block_sums(size_t n_desc, size_t n_sums, const uint2* __restrict__ desc,
+                                                    const double* __restrict__ V, double* __restrict__ S, int* flag) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n_desc) return;
+  const uint2 d = desc[i];
+  const uint32_t n = d.y & 0xffffffu, stride = (d.y >> 24) & 0x7fu;
+  const bool inpat = (d.y >> 31) != 0;
+  const double* src = V + d.x;
+  bool nz;
+  double sum;
+  switch (n) {
+    case 1:
+      if (nonzero(src[0])) atomicOr(flag, kFlagPattern);
+      return;
+    case 2: {
+      const double a = src[0], b = src[stride];
+      nz = nonzero(a) | nonzero(b);
+      sum = a + b;
+      break;
     }
-    s_pre[tid + 1] = x;  // per-warp inclusive
-  }
-  __syncthreads();
-  if (tid == 0) {
-    s_pre[0] = 0;
-    int w0 = s_pre[32];
-    for (int k = 33; k <= kRedBlocks; ++k) s_pre[k] += w0;
-  }
-  __syncthreads();
-  if (tid < nloc)
-    for (int t = s_pre[tid]; t < s_pre[tid + 1]; ++t) s_lb[t] = (uint8_t)tid;
-  __syncthreads();
-  const int E = s_pre[nloc];
-  bool bad = false;
-  // sums of the packed entries
-  for (int t = tid; t < E; t += kRedThreads) {
-    const int lb = s_lb[t];
-    const int c = s_pre[lb + 1] - s_pre[lb];
-    const int j = t - s_pre[lb];
-    const double* src = V + s_voff[lb] + j;
-    double sum = src[0];
-    bool nz = nonzero(sum);
-    const uint32_t n = s_cnt[lb];
-    for (uint32_t k = 1; k < n; ++k) {
-      double v = src[(size_t)k * c];
-      nz |= nonzero(v);
-      sum = sum + v;
+    case 3: {
+      const double a = src[0], b = src[stride], c = src[2 * stride];
+      nz = nonzero(a) | nonzero(b) | nonzero(c);
+      sum = (a + b) + c;
+      break;
     }
-    const int en = c_lay_en[s_lay[lb]][j];
-    bad |= nz != (((s_m[lb] >> en) & 1ull) != 0);
-    s_sum[t] = sum;
-  }
-  __syncthreads();
-  // pattern entries: row-major writes of the (I, J) block, then of its transpose (J, I)
-  for (int t = tid; t < E; t += kRedThreads) {
-    const int lb = s_lb[t];
-    const int j = t - s_pre[lb];
-    const uint64_t m = s_m[lb];
-    if (j >= __popcll(m)) continue;
-    const size_t b = b0 + lb;
-    const int lay = s_lay[lb];
-    const int en = nth_set_bit(m, j);
-    const int a = en / 6, c = en - 6 * (en / 6);
-    const uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
-    const int64_t pos = row_ptr[6 * (int64_t)s_I[lb] + a] + blk_colpos[b * 12 + a] + __popc(rowbits & ((1u << c) - 1u));
-    values[pos] = s_sum[s_pre[lb] + s_pos[lay][en]];
-    if (s_I[lb] != s_J[lb]) {
-      const uint64_t mT = s_mT[lb];
-      const int enT = nth_set_bit(mT, j);  // j-th entry of the transposed block, row-major
-      const int cT = enT / 6, aT = enT - 6 * (enT / 6);
-      const int en0 = 6 * aT + cT;  // the same entry in the (I, J) block
-      const uint32_t rowbitsT = (uint32_t)((mT >> (6 * cT)) & 63ull);
-      const int64_t pos2 =
-          row_ptr[6 * (int64_t)s_J[lb] + cT] + blk_colpos[b * 12 + 6 + cT] + __popc(rowbitsT & ((1u << aT) - 1u));
-      values[pos2] = s_sum[s_pre[lb] + s_pos[lay][en0]];
+    case 4: {
+      const double a = src[0], b = src[stride], c = src[2 * stride], e = src[3 * stride];
+      nz = nonzero(a) | nonzero(b) | nonzero(c) | nonzero(e);
+      sum = ((a + b) + c) + e;
+      break;
+    }
+    default: {
+      sum = src[0];
+      nz = nonzero(sum);
+      for (uint32_t k = 1; k < n; ++k) {
+        const double x = src[(size_t)k * stride];
+        nz |= nonzero(x);
+        sum = sum + x;
+      }
     }
   }
-  if (bad) atomicOr(flag, 1);
+  if (i < n_sums) S[i] = sum;
+  if (nz != inpat) atomicOr(flag, kFlagPattern);
+}
+
+// Numeric pass, part 2: CSR values in storage order, each read from its source
+// (the scratch for one-contribution entries, S otherwise; S starts at vs_off of
+// the same buffer); eight consecutive entries per thread so their loads
+// overlap.  A one-contribution pattern entry that reads zero raises kFlagPattern.
+constexpr int kGatherPerThread = 8;
+__global__ void __launch_bounds__(256) k_gather_values(size_t nnz, const uint32_t* __restrict__ src_map,
+                                                       const double* __restrict__ VS, unsigned long long vs_off,
+                                                       double* __restrict__ values, int* flag) {
+  const size_t k0 = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) * kGatherPerThread;
+  if (k0 >= nnz) return;
+  bool zero_direct = false;
+  if (k0 + kGatherPerThread <= nnz) {
+    // src_map and values are 256-byte aligned and k0 % 8 == 0
+    const uint4 s0 = reinterpret_cast<const uint4*>(src_map + k0)[0];
+    const uint4 s1 = reinterpret_cast<const uint4*>(src_map + k0)[1];
+    const uint32_t sx[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+    double a[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] = VS[sx[q]];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) zero_direct |= sx[q] < vs_off && !nonzero(a[q]);
+    double2* out = reinterpret_cast<double2*>(values + k0);
+    out[0] = make_double2(a[0], a[1]);
+    out[1] = make_double2(a[2], a[3]);
+    out[2] = make_double2(a[4], a[5]);
+    out[3] = make_double2(a[6], a[7]);
+  } else {
+    for (size_t k = k0; k < nnz; ++k) {
+      const uint32_t sx = src_map[k];
+      const double v = VS[sx];
+      zero_direct |= sx < vs_off && !nonzero(v);
+      values[k] = v;
+    }
+  }
+  if (zero_direct) atomicOr(flag, kFlagPattern);
 }
 
 // ---------------------------------------------------------------------------
@@ -1002,6 +1086,14 @@ struct fem_gpu {
   DevBuf<uint64_t> mask_t, mask_b, mask_p;
   DevBuf<unsigned long long> off_t, off_b, off_p, blk_voff;  // packed offsets (offset | packing << 62)
   DevBuf<uint8_t> blk_lay;
+  DevBuf<uint64_t> blk_pmask;  // pattern bits over packed positions
+  DevBuf<unsigned long long> sbase;  // kSlotCats x (n_blocks + 1) slot scans
+  unsigned long long slot_off[kSlotCats] = {0, 0, 0, 0, 0};
+  unsigned long long vs_off = 0;     // S starts here in V
+  size_t n_desc = 0;
+  DevBuf<uint32_t> src_map;          // per CSR entry: its slot in S
+  DevBuf<uint2> slot_desc;           // per slot: scratch start, count | stride << 24 | in-pattern << 31
+  size_t s_words = 0;
   size_t v_words = 0;
   DevBuf<double> V;
   DevBuf<uint32_t> blk_start, blk_count;
@@ -1139,6 +1231,10 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   h->off_p.release();
   h->blk_voff.release();
   h->blk_lay.release();
+  h->blk_pmask.release();
+  h->sbase.release();
+  h->src_map.release();
+  h->slot_desc.release();
   h->mask_t.release();
   h->mask_b.release();
   h->mask_p.release();
@@ -1534,10 +1630,13 @@ int numeric_launch(fem_gpu* h) {
   int r = launch_elements(h, st, sb, sp);
   if (r) return r;
   CK(cudaEventRecord(h->ev[1], h->stream));
-  if (h->n_blocks)
-    k_reduce<<<grid_for(h->n_blocks, kRedBlocks), kRedThreads, 0, h->stream>>>(
-        h->n_blocks, h->blk_count.p, h->blk_mask.p, h->blk_maskT.p, h->blk_lay.p, h->blk_voff.p, h->blk_I.p,
-        h->blk_J.p, h->blk_colpos.p, h->row_ptr.p, h->V.p, h->values.p, h->flag.p);
+  if (h->n_blocks) {
+    if (h->n_desc)
+      k_block_sums<<<grid_for(h->n_desc, 256), 256, 0, h->stream>>>(h->n_desc, h->s_words, h->slot_desc.p, h->V.p,
+                                                                     h->V.p + h->vs_off, h->flag.p);
+    k_gather_values<<<grid_for(((size_t)h->nnz + kGatherPerThread - 1) / kGatherPerThread, 256), 256, 0,
+                      h->stream>>>((size_t)h->nnz, h->src_map.p, h->V.p, h->vs_off, h->values.p, h->flag.p);
+  }
   CK(cudaGetLastError());
   CK(cudaEventRecord(h->ev[2], h->stream));
   h->numeric_done = true;
@@ -1648,8 +1747,9 @@ int symbolic(fem_gpu* h) {
     CK(h->blk_voff.reserve(nb + 1, s));
     CK(h->blk_lay.reserve(nb + 1, s));
     CK(cudaMemsetAsync(sizes.p + nb, 0, sizeof(unsigned long long), s));
+    CK(h->blk_pmask.reserve(nb + 1, s));
     k_block_sizes<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_mask.p, h->blk_I.p, h->blk_J.p,
-                                                    h->blk_lay.p, sizes.p);
+                                                    h->blk_lay.p, h->blk_pmask.p, sizes.p);
     st = cub_call(h, [&](void* tmp, size_t& bytes) {
       return cub::DeviceScan::ExclusiveSum(tmp, bytes, sizes.p, h->blk_voff.p, (int64_t)(nb + 1), s);
     });
@@ -1721,7 +1821,58 @@ int symbolic(fem_gpu* h) {
                                                h->blk_maskT.p, h->blk_colpos.p, h->row_ptr.p, gbase.p, h->col_idx.p,
                                                h->nnz_group.p, h->g_row.p, h->g_col.p, h->g_kind.p);
   CK(cudaGetLastError());
-  CK(h->V.reserve(h->v_words + 1, s));
+  // block-sum slots by contribution count, their descriptors and the source of every CSR entry
+  {
+    const size_t st_ = nb + 1;
+    DevBuf<unsigned long long> sz;
+    CK(sz.reserve(kSlotCats * st_, s));
+    CK(h->sbase.reserve(kSlotCats * st_, s));
+    for (int g = 0; g < kSlotCats; ++g) CK(cudaMemsetAsync(sz.p + g * st_ + nb, 0, sizeof(unsigned long long), s));
+    k_slot_sizes<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_pmask.p, h->blk_lay.p, sz.p);
+    for (int g = 0; g < kSlotCats; ++g) {
+      st = cub_call(h, [&](void* tmp, size_t& bytes) {
+        return cub::DeviceScan::ExclusiveSum(tmp, bytes, sz.p + g * st_, h->sbase.p + g * st_, (int64_t)st_, s);
+      });
+      if (st) return st;
+    }
+    unsigned long long tot[kSlotCats];
+    for (int g = 0; g < kSlotCats; ++g)
+      CK(cudaMemcpyAsync(&tot[g], h->sbase.p + g * st_ + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    // descriptor order: 2, 3, 4, 5+ contributions (the S slots), then the check-only ones
+    unsigned long long at = 0;
+    for (int g = 1; g < kSlotCats; ++g) {
+      h->slot_off[g] = at;
+      at += tot[g];
+    }
+    h->s_words = (size_t)at;
+    h->slot_off[0] = at;
+    h->n_desc = (size_t)(at + tot[0]);
+    h->vs_off = ((unsigned long long)h->v_words + 3ull) & ~3ull;  // S 32-byte aligned after the scratch
+    if (h->vs_off + h->s_words + 4 >= (1ull << 32))
+      return h->fail(FEM_GPU_ERR_ARGUMENT, "model too large: %llu doubles of scratch and sums (limit 2^32)",
+                     (unsigned long long)(h->vs_off + h->s_words));
+    CK(h->V.reserve(h->vs_off + h->s_words + 4, s));
+    SlotLayout L;
+    L.base = h->sbase.p;
+    L.stride = st_;
+    for (int g = 0; g < kSlotCats; ++g) L.off[g] = h->slot_off[g];
+    L.vs_off = h->vs_off;
+    CK(h->src_map.reserve(nnz + 1, s));
+    k_csr_sources<<<grid_for(nb * 36, 256), 256, 0, s>>>(nb, h->blk_mask.p, h->blk_maskT.p, h->blk_lay.p,
+                                                         h->blk_count.p, h->blk_voff.p, L, h->blk_I.p, h->blk_J.p,
+                                                         h->blk_colpos.p, h->row_ptr.p, h->src_map.p);
+    CK(h->slot_desc.reserve(h->n_desc + 1, s));
+    CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), s));
+    k_slot_desc<<<grid_for(nb * 36, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_pmask.p, h->blk_lay.p,
+                                                       h->blk_voff.p, L, h->slot_desc.p, h->flag.p);
+    CK(cudaGetLastError());
+    int too_many = 0;
+    CK(cudaMemcpyAsync(&too_many, h->flag.p, sizeof too_many, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (too_many) return h->fail(FEM_GPU_ERR_ARGUMENT, "a node pair is shared by 2^24 or more elements");
+    sz.release();
+  }
   CK(cudaStreamSynchronize(s));
   // temporaries
   keys.release();
@@ -1936,17 +2087,18 @@ extern "C" int fem_gpu_get_stream(fem_gpu_t* h, void** stream) {
 
 extern "C" int fem_gpu_numeric_launch_count(fem_gpu_t* h, int* n_launches) {
   if (!h || !n_launches) return FEM_GPU_ERR_ARGUMENT;
-  *n_launches = (h->nt ? 1 : 0) + (h->nbm ? 1 : 0) + (h->np ? 1 : 0) + (h->n_blocks ? 1 : 0);
+  *n_launches = (h->nt ? 1 : 0) + (h->nbm ? 1 : 0) + (h->np ? 1 : 0) + (h->n_blocks ? 2 : 0);
   return FEM_GPU_OK;
 }
 
 extern "C" int fem_gpu_get_pattern_stats(fem_gpu_t* h, int64_t* n_blocks, int64_t* n_contributions,
-                                         int64_t* scratch_doubles) {
+                                         int64_t* scratch_doubles, int64_t* sum_slots) {
   if (!h) return FEM_GPU_ERR_ARGUMENT;
   if (!h->pattern_valid) return h->fail(FEM_GPU_ERR_STATE, "call fem_gpu_assemble first");
   if (n_blocks) *n_blocks = (int64_t)h->n_blocks;
   if (n_contributions) *n_contributions = (int64_t)h->n_pairs;
   if (scratch_doubles) *scratch_doubles = (int64_t)h->v_words;
+  if (sum_slots) *sum_slots = (int64_t)h->s_words;
   return FEM_GPU_OK;
 }
 

@@ -246,10 +246,11 @@ class FEM:
         return n.value
 
     def pattern_stats(self):
-        """(global node-pair blocks, element node-pair contributions, packed scratch doubles)."""
-        a, b, c = c_int64(0), c_int64(0), c_int64(0)
-        self._check(self._L.fem_gpu_get_pattern_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-        return a.value, b.value, c.value
+        """(global node-pair blocks, element node-pair contributions, packed scratch doubles, block-sum slots)."""
+        a, b, c, d = c_int64(0), c_int64(0), c_int64(0), c_int64(0)
+        self._check(self._L.fem_gpu_get_pattern_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                                      ctypes.byref(d)))
+        return a.value, b.value, c.value, d.value
 
     def last_numeric_timing(self):
         """(element kernels ms, reduction ms) of the last numeric pass, CUDA events on the handle's stream."""

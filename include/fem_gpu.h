@@ -145,9 +145,10 @@ int fem_gpu_get_stream(fem_gpu_t* h, void** stream);
 int fem_gpu_numeric_launch_count(fem_gpu_t* h, int* n_launches);
 
 /* Sizes of the stored pattern: global node-pair blocks, element node-pair
- * contributions, and doubles of packed element-block scratch one numeric pass
- * writes and reads (the reduction's input). */
-int fem_gpu_get_pattern_stats(fem_gpu_t* h, int64_t* n_blocks, int64_t* n_contributions, int64_t* scratch_doubles);
+ * contributions, doubles of packed element-block scratch one numeric pass
+ * writes and reads, and packed block-sum slots the CSR values are gathered from. */
+int fem_gpu_get_pattern_stats(fem_gpu_t* h, int64_t* n_blocks, int64_t* n_contributions, int64_t* scratch_doubles,
+                              int64_t* sum_slots);
 
 /* Per-kernel timing of the last numeric pass, measured with CUDA events on the
  * handle's stream (milliseconds): element kernels (all types) and the reduction. */

@@ -231,3 +231,27 @@ def test_plate_mesh_full_config():
     order = np.lexsort((rows, ci))
     np.testing.assert_array_equal(ci[order], rows)
     np.testing.assert_array_equal(va[order].view(np.uint64), va.view(np.uint64))
+
+
+def test_hub_node_many_contributions():
+    """a hub node shared by 400 trusses and 300 beams: its diagonal block sums 700 contributions
+    (a reduction tile too large to stage in shared memory takes the global-memory path)."""
+    rng = np.random.default_rng(5)
+    n_spokes = 700
+    ang = rng.uniform(0, 2 * np.pi, n_spokes)
+    el = rng.uniform(-1.2, 1.2, n_spokes)
+    r = rng.uniform(1.0, 3.0, n_spokes)
+    xyz = np.concatenate([[[0.0, 0.0, 0.0]], np.stack([r * np.cos(ang) * np.cos(el), r * np.sin(ang) * np.cos(el),
+                                                        r * np.sin(el)], 1)])
+    n = len(xyz)
+    spokes = np.stack([np.ones(n_spokes, np.uint32), np.arange(2, n + 1, dtype=np.uint32)], 1)
+    g, o = FEM(1e-12, 1e-12, n), OracleFEM(1e-12, 1e-12, n)
+    areas = rng.uniform(1e-4, 5e-4, 400)
+    m = n_spokes - 400
+    for model in (g, o):
+        model.add_nodes(np.arange(1, n + 1), xyz)
+        model.add_trusses(np.arange(1, 401), spokes[:400], 200e9, areas)
+        model.add_beams(np.arange(1, m + 1), spokes[400:], 210e9, 0.3, 1e-2, 5e-5, 3e-5, 0.0, 1e-5, 5 / 6,
+                        [0.3, 0.2, 1.0])
+    g.assemble()
+    compare(g, o)
