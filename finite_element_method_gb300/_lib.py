@@ -47,6 +47,17 @@ SIGNATURES = {
     "fem_gpu_numeric_launch_count": (c_int, [hp, POINTER(c_int)]),
     "fem_gpu_last_numeric_timing": (c_int, [hp, fp, fp]),
     "fem_gpu_get_pattern_stats": (c_int, [hp, i64p, i64p, i64p, i64p]),
+    "fem_gpu_batch_create": (c_int, [POINTER(c_void_p), c_size_t, POINTER(c_void_p)]),
+    "fem_gpu_batch_destroy": (c_int, [hp]),
+    "fem_gpu_batch_last_error": (c_char_p, [hp]),
+    "fem_gpu_batch_assemble": (c_int, [hp]),
+    "fem_gpu_batch_assemble_async": (c_int, [hp]),
+    "fem_gpu_batch_get_values": (c_int, [hp, c_size_t, dp]),
+    "fem_gpu_batch_get_values_device": (c_int, [hp, c_size_t, POINTER(c_void_p)]),
+    "fem_gpu_batch_get_stream": (c_int, [hp, POINTER(c_void_p)]),
+    "fem_gpu_batch_last_ms": (c_int, [hp, fp]),
+    "fem_gpu_batch_autotune": (c_int, [hp, c_int, c_char_p, c_char_p, c_size_t]),
+    "fem_gpu_batch_configure": (c_int, [hp, c_int, c_int, c_int, c_int, c_int, c_int, c_int]),
     "fem_gpu_assemble_dense_noalloc": (c_int, [c_uint32, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p,
                                                c_void_p, c_size_t, c_void_p, c_void_p, c_double, c_double, c_void_p,
                                                c_void_p]),

@@ -309,39 +309,43 @@ struct BlockSink {
   }
 };
 
-__global__ void __launch_bounds__(128) k_truss(NodesView nd, const int32_t* __restrict__ n1,
-                                               const int32_t* __restrict__ n2, const double* __restrict__ E,
-                                               const double* __restrict__ A, const double* __restrict__ A2,
-                                               double abs_tol, size_t count, BlockSink sink) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= count) return;
-  int I = n1[e], J = n2[e];
+struct TrussView {
+  const int32_t *n1, *n2;
+  const double *E, *A, *A2;
+};
+
+__device__ __forceinline__ void truss_element(size_t e, NodesView nd, const TrussView& t, double abs_tol,
+                                              const BlockSink& sink) {
+  int I = t.n1[e], J = t.n2[e];
   double x1[3], x2[3], g[9];
   nd.get(I, x1);
   nd.get(J, x2);
-  if (!truss_block(x1, x2, E[e], A[e], A2[e], abs_tol, g)) {
+  if (!truss_block(x1, x2, t.E[e], t.A[e], t.A2[e], abs_tol, g)) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) g[k] = 0.0;
   }
   double blk[36];
 #pragma unroll
   for (int s = 0; s < 3; ++s) {
-    double sg = s == 1 ? -1.0 : 1.0;
 #pragma unroll
     for (int k = 0; k < 36; ++k) blk[k] = 0.0;
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
       for (int b = 0; b < 3; ++b) blk[6 * a + b] = s == 1 ? -g[3 * a + b] : g[3 * a + b];
-    (void)sg;
     sink.put(e * kPairs2 + s, s == 1 && I > J, blk);
   }
 }
 
-__global__ void __launch_bounds__(128) k_beam(NodesView nd, BeamView b, double rel_tol, double abs_tol, size_t count,
-                                              BlockSink sink) {
+__global__ void __launch_bounds__(256) k_truss(NodesView nd, TrussView t, double abs_tol, size_t count,
+                                               BlockSink sink) {
   size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (e >= count) return;
+  truss_element(e, nd, t, abs_tol, sink);
+}
+
+__device__ __forceinline__ void beam_element(size_t e, NodesView nd, const BeamView& b, double rel_tol,
+                                             double abs_tol, const BlockSink& sink) {
   int I = b.n1[e], J = b.n2[e];
   double x1[3], x2[3];
   nd.get(I, x1);
@@ -389,6 +393,13 @@ __global__ void __launch_bounds__(128) k_beam(NodesView nd, BeamView b, double r
   sink.put(e * kPairs2 + 2, false, blk);
 }
 
+__global__ void __launch_bounds__(256) k_beam(NodesView nd, BeamView b, double rel_tol, double abs_tol, size_t count,
+                                              BlockSink sink) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= count) return;
+  beam_element(e, nd, b, rel_tol, abs_tol, sink);
+}
+
 template <int I, int J>
 __device__ __forceinline__ void plate_pair(const PlateCore& C, const double R[9], bool ident, const int nidx[4],
                                            size_t ep, const BlockSink& sink) {
@@ -403,10 +414,8 @@ __device__ __forceinline__ void plate_pair(const PlateCore& C, const double R[9]
   sink.put(ep, I != J && nidx[I] > nidx[J], blk);
 }
 
-__global__ void __launch_bounds__(128) k_plate(NodesView nd, PlateView pl, double abs_tol, size_t count,
-                                               BlockSink sink) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= count) return;
+__device__ __forceinline__ void plate_element(size_t e, NodesView nd, const PlateView& pl, double abs_tol,
+                                              const BlockSink& sink) {
   int nidx[4] = {pl.n1[e], pl.n2[e], pl.n3[e], pl.n4[e]};
   double X[4][3];
 #pragma unroll
@@ -437,6 +446,13 @@ __global__ void __launch_bounds__(128) k_plate(NodesView nd, PlateView pl, doubl
   plate_pair<2, 2>(C, R, ident, nidx, ep + 7, sink);
   plate_pair<2, 3>(C, R, ident, nidx, ep + 8, sink);
   plate_pair<3, 3>(C, R, ident, nidx, ep + 9, sink);
+}
+
+__global__ void __launch_bounds__(256) k_plate(NodesView nd, PlateView pl, double abs_tol, size_t count,
+                                               BlockSink sink) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= count) return;
+  plate_element(e, nd, pl, abs_tol, sink);
 }
 
 // sorted position k: record the element pair's slot and its mask
@@ -761,7 +777,7 @@ __global__ void k_slot_desc(size_t nb, const uint32_t* __restrict__ blk_count, c
 // their entry.  No atomics on values.  A non-pattern entry with a non-zero, or
 // a pattern slot whose contributions are all zero, raises kFlagPattern (the
 // exact-zero pattern changed).
-__global__ void __launch_bounds__(256) k_block_sums(size_t n_desc, size_t n_sums, const uint2* __restrict__ desc,
+__global__ void __launch_bounds__(512) k_block_sums(size_t n_desc, size_t n_sums, const uint2* __restrict__ desc,
                                                     const double* __restrict__ V, double* __restrict__ S, int* flag) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i >= n_desc) return;
@@ -812,7 +828,7 @@ __global__ void __launch_bounds__(256) k_block_sums(size_t n_desc, size_t n_sums
 // the same buffer); eight consecutive entries per thread so their loads
 // overlap.  A one-contribution pattern entry that reads zero raises kFlagPattern.
 constexpr int kGatherPerThread = 8;
-__global__ void __launch_bounds__(256) k_gather_values(size_t nnz, const uint32_t* __restrict__ src_map,
+__global__ void __launch_bounds__(512) k_gather_values(size_t nnz, const uint32_t* __restrict__ src_map,
                                                        const double* __restrict__ VS, unsigned long long vs_off,
                                                        double* __restrict__ values, int* flag) {
   const size_t k0 = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) * kGatherPerThread;
@@ -1130,6 +1146,7 @@ struct fem_gpu {
     return BeamView{b_n1.p, b_n2.p, b_E.p, b_nu.p, b_A.p, b_i11.p, b_i22.p, b_i12.p, b_it.p, b_ks.p, b_ax.p, b_ay.p, b_az.p};
   }
   PlateView plates() const { return PlateView{p_n1.p, p_n2.p, p_n3.p, p_n4.p, p_E.p, p_nu.p, p_t.p, p_ks.p}; }
+  TrussView trusses() const { return TrussView{t_n1.p, t_n2.p, t_E.p, t_A.p, t_A2.p}; }
   void append_run(int kind, size_t begin, size_t count) {
     if (!count) return;
     size_t ppe = kind == kPlate ? kPairs4 : kPairs2;
@@ -1612,8 +1629,7 @@ namespace {
 int launch_elements(fem_gpu* h, BlockSink sink_t, BlockSink sink_b, BlockSink sink_p) {
   NodesView nd = h->nodes();
   if (h->nt)
-    k_truss<<<grid_for(h->nt, 128), 128, 0, h->stream>>>(nd, h->t_n1.p, h->t_n2.p, h->t_E.p, h->t_A.p, h->t_A2.p,
-                                                         h->abs_tol, h->nt, sink_t);
+    k_truss<<<grid_for(h->nt, 128), 128, 0, h->stream>>>(nd, h->trusses(), h->abs_tol, h->nt, sink_t);
   if (h->nbm)
     k_beam<<<grid_for(h->nbm, 128), 128, 0, h->stream>>>(nd, h->beams(), h->rel_tol, h->abs_tol, h->nbm, sink_b);
   if (h->np) k_plate<<<grid_for(h->np, 128), 128, 0, h->stream>>>(nd, h->plates(), h->abs_tol, h->np, sink_p);
@@ -2112,3 +2128,6 @@ extern "C" int fem_gpu_last_numeric_timing(fem_gpu_t* h, float* element_ms, floa
   if (reduce_ms) *reduce_ms = h->t_reduce_ms;
   return FEM_GPU_OK;
 }
+
+// batched assembly of many structures (reuses the kernels and the handle above)
+#include "fem_batch.cuh"

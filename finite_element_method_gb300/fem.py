@@ -257,3 +257,73 @@ class FEM:
         a, b = c_float(0), c_float(0)
         self._check(self._L.fem_gpu_last_numeric_timing(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+
+class Batch:
+    """Many independent, assembled `FEM` models assembled together in one numeric pass (one CUDA graph launch).
+
+    The models must stay alive and keep their topology; model i's CSR pattern is its own
+    (`models[i].stiffness_csr()`), the batch supplies its values (`values(i)`)."""
+
+    def __init__(self, models):
+        self._L = _lib.load()
+        self.models = list(models)
+        arr = (c_void_p * len(self.models))(*[m.handle for m in self.models])
+        h = c_void_p()
+        st = self._L.fem_gpu_batch_create(arr, len(self.models), ctypes.byref(h))
+        self._h = h
+        if st:
+            msg = self._L.fem_gpu_batch_last_error(h).decode() if h else f"status {st}"
+            self.close()
+            raise FEMError(st, msg)
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._L.fem_gpu_batch_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st:
+            raise FEMError(st, self._L.fem_gpu_batch_last_error(self._h).decode())
+
+    def assemble(self):
+        self._check(self._L.fem_gpu_batch_assemble(self._h))
+
+    def assemble_async(self):
+        self._check(self._L.fem_gpu_batch_assemble_async(self._h))
+
+    def values(self, i):
+        _, nnz = self.models[i].csr_sizes()
+        out = np.zeros(max(nnz, 1), np.float64)
+        self._check(self._L.fem_gpu_batch_get_values(self._h, i, ptr(out, c_double)))
+        return out[:nnz]
+
+    def stream(self) -> int:
+        s = c_void_p()
+        self._check(self._L.fem_gpu_batch_get_stream(self._h, ctypes.byref(s)))
+        return s.value or 0
+
+    def last_ms(self) -> float:
+        x = c_float(0)
+        self._check(self._L.fem_gpu_batch_last_ms(self._h, ctypes.byref(x)))
+        return x.value
+
+    def autotune(self, reps=5, cache_path=None):
+        """Time the candidate launch configurations, keep the fastest; returns the JSON table (dict)."""
+        import json
+
+        buf = ctypes.create_string_buffer(1 << 16)
+        self._check(self._L.fem_gpu_batch_autotune(self._h, reps, cache_path.encode() if cache_path else None, buf,
+                                                   len(buf)))
+        return json.loads(buf.value.decode())
+
+    def configure(self, persistent, block, ctas_per_sm, tile_truss, tile_beam, tile_plate, sum_block):
+        self._check(self._L.fem_gpu_batch_configure(self._h, int(persistent), block, ctas_per_sm, tile_truss,
+                                                    tile_beam, tile_plate, sum_block))

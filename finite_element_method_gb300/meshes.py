@@ -213,12 +213,14 @@ def batch_structures(n_structures=512, lo=1e3, hi=2e5, seed=4, kinds=("truss", "
             b = max(2, int(round(target / a)))
             m = plate_mesh(a, b, size=0.1 * max(a, b), seed=sub_seed)
         elif kind == "beam":
-            # nx = ny, nz chosen so that ~3 n^2 nz beams ~ target
-            n = max(2, int(round((target / 3.0 / 4.0) ** (1 / 3) * 1.6)))
-            nz = max(2, int(round(target / (3.0 * n * n))))
-            m = beam_frame(n, n, nz, seed=sub_seed)
+            # an n x n x nz frame with nz ~ n / 4: 2 n (n - 1) nz + n^2 (nz - 1) beams closest to the target
+            cand = [(abs(2 * n * (n - 1) * max(2, n // 4) + n * n * (max(2, n // 4) - 1) - target), n)
+                    for n in range(2, 400)]
+            n = min(cand)[1]
+            m = beam_frame(n, n, max(2, n // 4), seed=sub_seed)
         else:
-            n = max(2, int(round((target / 4.0) ** (1 / 3))))
+            # an n^3 lattice: 3 n^2 (n - 1) bars + (n - 1)^3 diagonals closest to the target
+            n = min((abs(3 * n * n * (n - 1) + (n - 1) ** 3 - target), n) for n in range(2, 200))[1]
             m = truss_lattice(n, seed=sub_seed)
         m.name = f"{kind}_{s}"
         out.append(m)

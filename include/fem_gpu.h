@@ -154,6 +154,36 @@ int fem_gpu_get_pattern_stats(fem_gpu_t* h, int64_t* n_blocks, int64_t* n_contri
  * handle's stream (milliseconds): element kernels (all types) and the reduction. */
 int fem_gpu_last_numeric_timing(fem_gpu_t* h, float* element_ms, float* reduce_ms);
 
+/* ---- batched assembly -------------------------------------------------------
+ * No counterpart in the reference (it assembles one model per FEM value): a
+ * batch assembles many independent, already assembled models in one numeric
+ * pass -- one CUDA graph launch -- instead of one pass per model.  The models
+ * must outlive the batch and keep their topology; their CSR patterns stay
+ * theirs (fem_gpu_get_csr on model i gives row_ptr / col_idx), the batch
+ * supplies the values.  Results are bit-identical to each model's own pass. */
+typedef struct fem_gpu_batch fem_gpu_batch_t;
+int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, fem_gpu_batch_t** out);
+int fem_gpu_batch_destroy(fem_gpu_batch_t* b);
+const char* fem_gpu_batch_last_error(const fem_gpu_batch_t* b);
+/* one numeric pass of every model: synchronous (checks the exact-zero patterns) or enqueued */
+int fem_gpu_batch_assemble(fem_gpu_batch_t* b);
+int fem_gpu_batch_assemble_async(fem_gpu_batch_t* b);
+/* CSR values of model i (its own pattern order), to host or as a device pointer */
+int fem_gpu_batch_get_values(fem_gpu_batch_t* b, size_t i, double* values);
+int fem_gpu_batch_get_values_device(fem_gpu_batch_t* b, size_t i, const double** values);
+int fem_gpu_batch_get_stream(fem_gpu_batch_t* b, void** stream);
+/* device time of the last synchronous fem_gpu_batch_assemble (CUDA events), ms */
+int fem_gpu_batch_last_ms(fem_gpu_batch_t* b, float* ms);
+/* Measure the candidate launch configurations (plain element launches of 64,
+ * 128 or 256 threads; one persistent launch with 1 or 2 CTAs per SM and four
+ * tile-size sets; reduction blocks of 128, 256, 512 threads) with `reps` graph
+ * replays each, keep the fastest, write the table as JSON to cache_path (if
+ * not NULL) and into summary (if not NULL, at most cap bytes). */
+int fem_gpu_batch_autotune(fem_gpu_batch_t* b, int reps, const char* cache_path, char* summary, size_t cap);
+/* apply a configuration read back from that table */
+int fem_gpu_batch_configure(fem_gpu_batch_t* b, int persistent, int block, int ctas_per_sm, int tile_truss,
+                            int tile_beam, int tile_plate, int sum_block);
+
 /* Dense assembly of one small structure without any device allocation.
  * No counterpart in the reference: it serves callers that cannot call
  * cudaMalloc -- hosts that own all device memory through their own pool or

@@ -255,3 +255,34 @@ def test_hub_node_many_contributions():
                         [0.3, 0.2, 1.0])
     g.assemble()
     compare(g, o)
+
+
+def test_batch_matches_each_model():
+    """several structures of every kind assembled in one batch pass: each structure's values equal its own
+    assembly bit for bit, for the default and for the autotuned launch configuration."""
+    from finite_element_method_gb300 import Batch
+
+    structures = meshes.batch_structures(9, lo=200, hi=3000, seed=8)
+    models, refs = [], []
+    for m in structures:
+        g = FEM(meshes.REL_TOL, meshes.ABS_TOL, m.nodes_number)
+        meshes.load(g, m)
+        g.assemble()
+        models.append(g)
+        refs.append(g.stiffness_values().copy())
+    b = Batch(models)
+    b.assemble()
+    for i, r in enumerate(refs):
+        np.testing.assert_array_equal(b.values(i).view(np.uint64), r.view(np.uint64))
+    table = b.autotune(reps=2)
+    assert table["best_ms"] > 0 and len(table["candidates"]) >= 10
+    b.assemble()
+    for i, r in enumerate(refs):
+        np.testing.assert_array_equal(b.values(i).view(np.uint64), r.view(np.uint64))
+    # against the oracle for two of them
+    for i in (0, len(structures) - 1):
+        o = OracleFEM(meshes.REL_TOL, meshes.ABS_TOL, structures[i].nodes_number)
+        meshes.load(o, structures[i])
+        _, _, va = o.csr()
+        np.testing.assert_array_equal(b.values(i).view(np.uint64), va.view(np.uint64))
+    b.close()
