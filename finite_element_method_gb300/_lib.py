@@ -47,6 +47,8 @@ SIGNATURES = {
     "fem_gpu_numeric_launch_count": (c_int, [hp, POINTER(c_int)]),
     "fem_gpu_last_numeric_timing": (c_int, [hp, fp, fp]),
     "fem_gpu_get_pattern_stats": (c_int, [hp, i64p, i64p, i64p, i64p]),
+    "fem_gpu_vjp": (c_int, [hp, dp, dp, c_int, dp, dp, dp, dp]),
+    "fem_gpu_vjp_last_ms": (c_int, [hp, fp]),
     "fem_gpu_batch_create": (c_int, [POINTER(c_void_p), c_size_t, POINTER(c_void_p)]),
     "fem_gpu_batch_destroy": (c_int, [hp]),
     "fem_gpu_batch_last_error": (c_char_p, [hp]),

@@ -139,27 +139,41 @@ __device__ __forceinline__ double datan(double t) {
 
 __device__ __forceinline__ double dacos(double x) { return 2.0 * datan(sqrt((1.0 - x) / (1.0 + x))); }
 
+}  // namespace femgpu
+#include "dual.cuh"
+namespace femgpu {
+
 // ---------------------------------------------------------------------------
 // vectors (plain left-to-right, no fusion)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double dot3(const double a[3], const double b[3]) {
+template <class T>
+__device__ __forceinline__ T dot3(const T a[3], const T b[3]) {
   return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
 }
-__device__ __forceinline__ double norm3(const double a[3]) { return sqrt(dot3(a, a)); }
-__device__ __forceinline__ void sub3(const double a[3], const double b[3], double o[3]) {
+template <class T>
+__device__ __forceinline__ T norm3(const T a[3]) { return sqrt(dot3(a, a)); }
+template <class T>
+__device__ __forceinline__ void sub3(const T a[3], const T b[3], T o[3]) {
   o[0] = a[0] - b[0];
   o[1] = a[1] - b[1];
   o[2] = a[2] - b[2];
 }
-__device__ __forceinline__ void cross3(const double a[3], const double b[3], double o[3]) {
+template <class T>
+__device__ __forceinline__ void cross3(const T a[3], const T b[3], T o[3]) {
   o[0] = a[1] * b[2] - a[2] * b[1];
   o[1] = a[2] * b[0] - a[0] * b[2];
   o[2] = a[0] * b[1] - a[1] * b[0];
 }
 // compare_with_tolerance, math_functions.rs:3-12
-__device__ __forceinline__ double cwt(double v, double abs_tol) { return fabs(v) < abs_tol ? 0.0 : v; }
+template <class T>
+__device__ __forceinline__ T cwt(T v, double abs_tol) { return fabs(v) < abs_tol ? 0.0 : v; }
+// differentiated: the clamp zeroes the value only -- its plateau (|v| < abs_tol) is far narrower than
+// any finite-difference step, so the derivative that central differences see passes through
+template <>
+__device__ __forceinline__ Dual cwt<Dual>(Dual v, double abs_tol) { return fabs(v.v) < abs_tol ? Dual(0.0, v.d) : v; }
 
-__device__ __forceinline__ void set_identity(double R[9]) {
+template <class T>
+__device__ __forceinline__ void set_identity(T R[9]) {
   R[0] = 1.0; R[1] = 0.0; R[2] = 0.0;
   R[3] = 0.0; R[4] = 1.0; R[5] = 0.0;
   R[6] = 0.0; R[7] = 0.0; R[8] = 1.0;
@@ -171,22 +185,28 @@ __device__ __forceinline__ void set_identity(double R[9]) {
 // quadrilateral_4n_element_functions.rs:158): Rodrigues rotation about a x b,
 // R = c I + [v]x + v v^T / (1 + c); exact parallel -> I; exact anti-parallel ->
 // half turn about a x e_z (or a x e_x); entries below abs_tol -> 0.
-__device__ __forceinline__ void align_rotation(const double a[3], const double b[3], double abs_tol, double R[9]) {
-  double ia = 1.0 / norm3(a), ib = 1.0 / norm3(b);
-  double ua[3] = {a[0] * ia, a[1] * ia, a[2] * ia};
-  double ub[3] = {b[0] * ib, b[1] * ib, b[2] * ib};
-  double v[3];
+template <class T>
+__device__ __forceinline__ void align_rotation(const T a[3], const T b[3], double abs_tol, T R[9]) {
+  T ia = 1.0 / norm3(a), ib = 1.0 / norm3(b);
+  T ua[3] = {a[0] * ia, a[1] * ia, a[2] * ia};
+  T ub[3] = {b[0] * ib, b[1] * ib, b[2] * ib};
+  T v[3];
   cross3(ua, ub, v);
-  double c = dot3(ua, ub);
+  T c = dot3(ua, ub);
   if (v[0] == 0.0 && v[1] == 0.0 && v[2] == 0.0) {
-    if (c > 0.0) {
+    // Exactly parallel: the identity.  Differentiated code takes the general
+    // formula below instead, which gives the same identity value and the
+    // rotation's derivative ([dv]x).
+    if (c > 0.0 && !IsDual<T>::value) {
       set_identity(R);
       return;
     }
-    double ez[3] = {0.0, 0.0, 1.0}, ex[3] = {1.0, 0.0, 0.0}, n[3];
+  }
+  if (v[0] == 0.0 && v[1] == 0.0 && v[2] == 0.0 && !(c > 0.0)) {
+    T ez[3] = {0.0, 0.0, 1.0}, ex[3] = {1.0, 0.0, 0.0}, n[3];
     cross3(ua, ez, n);
     if (n[0] == 0.0 && n[1] == 0.0 && n[2] == 0.0) cross3(ua, ex, n);
-    double in = 1.0 / norm3(n);
+    T in = 1.0 / norm3(n);
     n[0] *= in;
     n[1] *= in;
     n[2] *= in;
@@ -194,13 +214,13 @@ __device__ __forceinline__ void align_rotation(const double a[3], const double b
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        double tn = 2.0 * n[i];
+        T tn = 2.0 * n[i];
         R[3 * i + j] = cwt(i == j ? fma(tn, n[j], -1.0) : tn * n[j], abs_tol);
       }
     return;
   }
-  double h = 1.0 / (1.0 + c);
-  double hv0 = h * v[0], hv1 = h * v[1], hv2 = h * v[2];
+  T h = 1.0 / (1.0 + c);
+  T hv0 = h * v[0], hv1 = h * v[1], hv2 = h * v[2];
   R[0] = cwt(fma(hv0, v[0], c), abs_tol);
   R[1] = cwt(fma(hv0, v[1], -v[2]), abs_tol);
   R[2] = cwt(fma(hv0, v[2], v[1]), abs_tol);
@@ -212,14 +232,16 @@ __device__ __forceinline__ void align_rotation(const double a[3], const double b
   R[8] = cwt(fma(hv2, v[2], c), abs_tol);
 }
 
-__device__ __forceinline__ bool is_identity(const double R[9]) {
+template <class T>
+__device__ __forceinline__ bool is_identity(const T R[9]) {
   return R[0] == 1.0 && R[1] == 0.0 && R[2] == 0.0 && R[3] == 0.0 && R[4] == 1.0 && R[5] == 0.0 && R[6] == 0.0 &&
          R[7] == 0.0 && R[8] == 1.0;
 }
 
 // symmetric R^T diag(d) R (upper computed, lower mirrored)
-__device__ __forceinline__ void rt_diag_r(const double R[9], const double d[3], double out[9]) {
-  double t[9];
+template <class T>
+__device__ __forceinline__ void rt_diag_r(const T R[9], const T d[3], T out[9]) {
+  T t[9];
 #pragma unroll
   for (int k = 0; k < 3; ++k)
 #pragma unroll
@@ -228,15 +250,16 @@ __device__ __forceinline__ void rt_diag_r(const double R[9], const double d[3], 
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = i; j < 3; ++j) {
-      double s = fma(t[6 + i], R[6 + j], fma(t[3 + i], R[3 + j], t[i] * R[j]));
+      T s = fma(t[6 + i], R[6 + j], fma(t[3 + i], R[3 + j], t[i] * R[j]));
       out[3 * i + j] = s;
       out[3 * j + i] = s;
     }
 }
 
 // R^T M R for one 3x3 block (dense fma chains); sym: i <= j computed, mirrored
-__device__ __forceinline__ void rt_m_r(const double R[9], const double M[9], double out[9], bool sym) {
-  double Y[9];
+template <class T>
+__device__ __forceinline__ void rt_m_r(const T R[9], const T M[9], T out[9], bool sym) {
+  T Y[9];
 #pragma unroll
   for (int k = 0; k < 3; ++k)
 #pragma unroll
@@ -246,7 +269,7 @@ __device__ __forceinline__ void rt_m_r(const double R[9], const double M[9], dou
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
       if (sym && b < a) continue;
-      double s = fma(R[6 + a], Y[6 + b], fma(R[3 + a], Y[3 + b], R[a] * Y[b]));
+      T s = fma(R[6 + a], Y[6 + b], fma(R[3 + a], Y[3 + b], R[a] * Y[b]));
       out[3 * a + b] = s;
       if (sym) out[3 * b + a] = s;
     }
@@ -256,41 +279,43 @@ __device__ __forceinline__ void rt_m_r(const double R[9], const double M[9], dou
 // truss (structs/truss.rs:66-214)
 // ---------------------------------------------------------------------------
 // returns false for coincident nodes
-__device__ __forceinline__ bool truss_rotation(const double x1[3], const double x2[3], double abs_tol, double R[9]) {
-  double d[3];
+template <class T>
+__device__ __forceinline__ bool truss_rotation(const T x1[3], const T x2[3], double abs_tol, T R[9]) {
+  T d[3];
   sub3(x2, x1, d);
-  double L = norm3(d);
+  T L = norm3(d);
   if (!(L > 0.0)) return false;
-  double target[3] = {L, 0.0, 0.0};
+  T target[3] = {L, 0.0, 0.0};
   align_rotation(d, target, abs_tol, R);
   return true;
 }
 
 // g (3x3, node-pair (1,1) block of the 6x6 truss matrix in global axes);
 // blocks: (1,1) = g, (1,2) = (2,1) = -g, (2,2) = g
-__device__ __forceinline__ bool truss_block(const double x1[3], const double x2[3], double young, double area,
-                                            double area2 /* NaN: none */, double abs_tol, double g[9]) {
-  double R[9];
+template <class T>
+__device__ __forceinline__ bool truss_block(const T x1[3], const T x2[3], T young, T area,
+                                            T area2 /* NaN: none */, double abs_tol, T g[9]) {
+  T R[9];
   if (!truss_rotation(x1, x2, abs_tol, R)) return false;
-  double d[3];
+  T d[3];
   sub3(x2, x1, d);
-  double L = norm3(d);
-  double jac = L * 0.5;
-  double inv = 1.0 / jac;
-  double b = 0.5 * inv;
-  double a_r = area;
+  T L = norm3(d);
+  T jac = L * 0.5;
+  T inv = 1.0 / jac;
+  T b = 0.5 * inv;
+  T a_r = area;
   if (area2 == area2) {
-    double hh = (area2 - area) * 0.5;
+    T hh = (area2 - area) * 0.5;
     a_r = area + hh;
   }
-  double scalar = ((a_r * young) * jac) * 2.0;
-  double q = (b * b) * scalar;
-  double m[3] = {R[0] * q, R[1] * q, R[2] * q};
+  T scalar = ((a_r * young) * jac) * 2.0;
+  T q = (b * b) * scalar;
+  T m[3] = {R[0] * q, R[1] * q, R[2] * q};
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = i; j < 3; ++j) {
-      double s = m[i] * R[j];
+      T s = m[i] * R[j];
       g[3 * i + j] = s;
       g[3 * j + i] = s;
     }
@@ -300,13 +325,14 @@ __device__ __forceinline__ bool truss_block(const double x1[3], const double x2[
 // ---------------------------------------------------------------------------
 // beam (structs/beam.rs)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void principal_moments(double i11, double i22, double i12, double rel_tol, double& i11p,
-                                                  double& i22p, double& angle_out) {
-  double angle;
+template <class T>
+__device__ __forceinline__ void principal_moments(T i11, T i22, T i12, double rel_tol, T& i11p,
+                                                  T& i22p, T& angle_out) {
+  T angle;
   if (i11 != i22) {
     angle = datan((2.0 * i12) / (i22 - i11)) / 2.0;
   } else {
-    double i11m, i22m;
+    T i11m, i22m;
     if (i22 < i11) {
       i11m = i11;
       i22m = ((fabs(i22) - fabs(i22) * rel_tol) * i22) / fabs(i22);
@@ -316,12 +342,12 @@ __device__ __forceinline__ void principal_moments(double i11, double i22, double
     }
     angle = datan((2.0 * i12) / (i22m - i11m)) / 2.0;
   }
-  double c = dcos(angle), s = dsin(angle), s2 = dsin(2.0 * angle);
-  double a = (i11 * (c * c) + i22 * (s * s)) - i12 * s2;
-  double bb = (i11 * (s * s) + i22 * (c * c)) + i12 * s2;
+  T c = dcos(angle), s = dsin(angle), s2 = dsin(2.0 * angle);
+  T a = (i11 * (c * c) + i22 * (s * s)) - i12 * s2;
+  T bb = (i11 * (s * s) + i22 * (c * c)) + i12 * s2;
   int it = 1;
   while (a < bb && it <= 8) {
-    angle = (datan((2.0 * i12) / (i22 - i11)) + FEM_PI_F32 * (double)it) / 2.0;
+    angle = (datan((2.0 * i12) / (i22 - i11)) + FEM_PI_F32 * (T)it) / 2.0;
     c = dcos(angle);
     s = dsin(angle);
     s2 = dsin(2.0 * angle);
@@ -335,38 +361,62 @@ __device__ __forceinline__ void principal_moments(double i11, double i22, double
 }
 
 // projection_perpendicular_to_vector: a - ((a.b)/(b.b)) b
-__device__ __forceinline__ void project_perp(const double a[3], const double b[3], double p[3]) {
-  double s = dot3(a, b) / dot3(b, b);
+template <class T>
+__device__ __forceinline__ void project_perp(const T a[3], const T b[3], T p[3]) {
+  T s = dot3(a, b) / dot3(b, b);
   p[0] = a[0] - s * b[0];
   p[1] = a[1] - s * b[1];
   p[2] = a[2] - s * b[2];
 }
 
-// find_rotation_matrix_elements, beam.rs:162-258 (false: coincident nodes)
-__device__ __forceinline__ bool beam_rotation(const double x1[3], const double x2[3], double i11, double i22,
-                                              double i12, const double axis[3], double rel_tol, double abs_tol,
-                                              double R[9], double& i11p, double& i22p) {
-  double angle;
-  principal_moments(i11, i22, i12, rel_tol, i11p, i22p, angle);
-  double d[3];
-  sub3(x2, x1, d);
-  double L = norm3(d);
-  if (!(L > 0.0)) return false;
-  double target[3] = {L, 0.0, 0.0};
-  double Ri[9];
-  align_rotation(d, target, abs_tol, Ri);
-  double p[3];
-  project_perp(axis, d, p);
-  double tp[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) tp[i] = (Ri[3 * i] * p[0] + Ri[3 * i + 1] * p[1]) + Ri[3 * i + 2] * p[2];
-  double cosang = tp[2] / norm3(tp);
+// The section twist of find_rotation_matrix_elements (beam.rs:162-258): acos of
+// the cosine between the rotated projected axis tp and local z, the cosine
+// clamped to [-1, 1].
+template <class T>
+__device__ __forceinline__ T twist_angle(const T tp[3]) {
+  T cosang = tp[2] / norm3(tp);
   if (cosang > 1.0) cosang = 1.0;
   if (cosang < -1.0) cosang = -1.0;
-  double total = angle + dacos(cosang);
-  double cx = cwt(d[0] / L, abs_tol), cy = cwt(d[1] / L, abs_tol), cz = cwt(d[2] / L, abs_tol);
-  double cxz = cwt(sqrt(cx * cx + cz * cz), abs_tol);
-  double c = cwt(dcos(total), abs_tol), s = cwt(dsin(total), abs_tol);
+  return dacos(cosang);
+}
+// Differentiated: the value exactly as above; the derivative written without
+// the cancellation in 1 - cos^2, which costs eps / theta^2 of relative
+// accuracy at a small twist theta.  With q = tp0^2 + tp1^2 (so sin theta =
+// sqrt(q) / |tp|):  theta' = -(tp2' q - tp2 (tp0 tp0' + tp1 tp1')) / (|tp|^2 sqrt(q)),
+// and 0 where q = 0 (the kink of acos at +-1, whose symmetric derivative is 0).
+template <>
+__device__ __forceinline__ Dual twist_angle<Dual>(const Dual tp[3]) {
+  const double v[3] = {tp[0].v, tp[1].v, tp[2].v};
+  const double theta = twist_angle(v);
+  const double q = tp[0].v * tp[0].v + tp[1].v * tp[1].v;
+  if (!(q > 0.0)) return Dual(theta, 0.0);
+  const double num = tp[2].d * q - tp[2].v * (tp[0].v * tp[0].d + tp[1].v * tp[1].d);
+  return Dual(theta, -num / ((q + tp[2].v * tp[2].v) * sqrt(q)));
+}
+
+// find_rotation_matrix_elements, beam.rs:162-258 (false: coincident nodes)
+template <class T>
+__device__ __forceinline__ bool beam_rotation(const T x1[3], const T x2[3], T i11, T i22,
+                                              T i12, const T axis[3], double rel_tol, double abs_tol,
+                                              T R[9], T& i11p, T& i22p) {
+  T angle;
+  principal_moments(i11, i22, i12, rel_tol, i11p, i22p, angle);
+  T d[3];
+  sub3(x2, x1, d);
+  T L = norm3(d);
+  if (!(L > 0.0)) return false;
+  T target[3] = {L, 0.0, 0.0};
+  T Ri[9];
+  align_rotation(d, target, abs_tol, Ri);
+  T p[3];
+  project_perp(axis, d, p);
+  T tp[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) tp[i] = (Ri[3 * i] * p[0] + Ri[3 * i + 1] * p[1]) + Ri[3 * i + 2] * p[2];
+  T total = angle + twist_angle(tp);
+  T cx = cwt(d[0] / L, abs_tol), cy = cwt(d[1] / L, abs_tol), cz = cwt(d[2] / L, abs_tol);
+  T cxz = cwt(sqrt(cx * cx + cz * cz), abs_tol);
+  T c = cwt(dcos(total), abs_tol), s = cwt(dsin(total), abs_tol);
   if (cxz != 0.0) {
     R[0] = cx;
     R[1] = cy;
@@ -394,39 +444,43 @@ __device__ __forceinline__ bool beam_rotation(const double x1[3], const double x
 // 3x3 blocks of the beam matrix in global axes (block order u1, th1, u2, th2):
 // uu, ut (u1-th1 = u1-th2), th (th1-th1 = th2-th2), tu (th1-u2), thth2 (th1-th2);
 // u1-u2 = -uu, u2-u2 = uu, u2-th2 = -ut.
-struct BeamBlocks {
-  double uu[9], ut[9], th[9], tu[9], thth2[9];
+template <class T>
+struct BeamBlocksT {
+  T uu[9], ut[9], th[9], tu[9], thth2[9];
 };
+using BeamBlocks = BeamBlocksT<double>;
 
-__device__ __forceinline__ bool beam_blocks(const double x1[3], const double x2[3], double young, double poisson,
-                                            double area, double i11, double i22, double i12, double it,
-                                            double shear_factor, const double axis[3], double rel_tol, double abs_tol,
-                                            BeamBlocks& B) {
-  double R[9], i11p, i22p;
+
+template <class T>
+__device__ __forceinline__ bool beam_blocks(const T x1[3], const T x2[3], T young, T poisson,
+                                            T area, T i11, T i22, T i12, T it,
+                                            T shear_factor, const T axis[3], double rel_tol, double abs_tol,
+                                            BeamBlocksT<T>& B) {
+  T R[9], i11p, i22p;
   if (!beam_rotation(x1, x2, i11, i22, i12, axis, rel_tol, abs_tol, R, i11p, i22p)) return false;
-  double d[3];
+  T d[3];
   sub3(x2, x1, d);
-  double L = norm3(d);
-  double jac = L * 0.5, inv = 1.0 / jac;
-  double b = 0.5 * inv;
-  double hb = 0.5 * b;
-  double b2 = b * b;
-  double G = young / (2.0 * (1.0 + poisson));
-  double su = ((area * young) * jac) * 2.0;
-  double sv = ((((G * area) * shear_factor)) * jac) * 2.0;
-  double sw = ((((G * area) * shear_factor)) * jac) * 2.0;
-  double stu = ((G * it) * jac) * 2.0;
-  double stv = ((young * i22p) * jac) * 2.0;
-  double stw = ((young * i11p) * jac) * 2.0;
-  double A1 = b2 * su, V1 = b2 * sv, W1 = b2 * sw, T1 = b2 * stu, Y1 = b2 * stv, Z1 = b2 * stw;
-  double HV = hb * sv, HW = hb * sw, QV = 0.25 * sv, QW = 0.25 * sw;
-  double du[3] = {A1, V1, W1};
-  double dth[3] = {T1, QW + Y1, QV + Z1};
-  double dth2[3] = {-T1, QW + (-Y1), QV + (-Z1)};
+  T L = norm3(d);
+  T jac = L * 0.5, inv = 1.0 / jac;
+  T b = 0.5 * inv;
+  T hb = 0.5 * b;
+  T b2 = b * b;
+  T G = young / (2.0 * (1.0 + poisson));
+  T su = ((area * young) * jac) * 2.0;
+  T sv = ((((G * area) * shear_factor)) * jac) * 2.0;
+  T sw = ((((G * area) * shear_factor)) * jac) * 2.0;
+  T stu = ((G * it) * jac) * 2.0;
+  T stv = ((young * i22p) * jac) * 2.0;
+  T stw = ((young * i11p) * jac) * 2.0;
+  T A1 = b2 * su, V1 = b2 * sv, W1 = b2 * sw, T1 = b2 * stu, Y1 = b2 * stv, Z1 = b2 * stw;
+  T HV = hb * sv, HW = hb * sw, QV = 0.25 * sv, QW = 0.25 * sw;
+  T du[3] = {A1, V1, W1};
+  T dth[3] = {T1, QW + Y1, QV + Z1};
+  T dth2[3] = {-T1, QW + (-Y1), QV + (-Z1)};
   rt_diag_r(R, du, B.uu);
   rt_diag_r(R, dth, B.th);
   rt_diag_r(R, dth2, B.thth2);
-  double P[9];
+  T P[9];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -445,19 +499,20 @@ __device__ __forceinline__ bool beam_blocks(const double x1[3], const double x2[
 // plate (structs/plate.rs, quadrilateral_4n_element_functions.rs)
 // ---------------------------------------------------------------------------
 // find_rotation_matrix_elements_of_quadrilateral, quad.rs:131-171 (false: nodes on a line)
-__device__ __forceinline__ bool plate_rotation(const double x2[3], const double x3[3], const double x4[3],
-                                               double abs_tol, double R[9]) {
-  double e34[3], e32[3], n[3];
+template <class T>
+__device__ __forceinline__ bool plate_rotation(const T x2[3], const T x3[3], const T x4[3],
+                                               double abs_tol, T R[9]) {
+  T e34[3], e32[3], n[3];
   sub3(x4, x3, e34);
   sub3(x2, x3, e32);
   cross3(e34, e32, n);
-  if (n[0] == 0.0 && n[1] == 0.0 && n[2] > 0.0) {
+  if (n[0] == 0.0 && n[1] == 0.0 && n[2] > 0.0 && !IsDual<T>::value) {
     set_identity(R);
     return true;
   }
-  double ln = norm3(n);
+  T ln = norm3(n);
   if (!(ln > 0.0)) return false;
-  double target[3] = {0.0, 0.0, ln};
+  T target[3] = {0.0, 0.0, ln};
   align_rotation(n, target, abs_tol, R);
   return true;
 }
@@ -465,13 +520,16 @@ __device__ __forceinline__ bool plate_rotation(const double x2[3], const double 
 // Everything the plate's 6x6 node-pair blocks are made of (see
 // plate_local_matrix in the oracle for the derivation; scaled Jacobian Jh = 4J,
 // D = det Jh, one reciprocal for the four determinants).
-struct PlateCore {
-  double Sxx[10], Syy[10], Sxy[16];  // upper-triangle index for Sxx/Syy
-  double cmq, cbq, gam, nu;
-  double F12[3], G12[3], F43[3];
-  double E12[3], E43[3];
-  double P14[6], P23[6], P1423[9];  // upper-triangle index for P14/P23
+template <class T>
+struct PlateCoreT {
+  T Sxx[10], Syy[10], Sxy[16];  // upper-triangle index for Sxx/Syy
+  T cmq, cbq, gam, nu;
+  T F12[3], G12[3], F43[3];
+  T E12[3], E43[3];
+  T P14[6], P23[6], P1423[9];  // upper-triangle index for P14/P23
 };
+
+using PlateCore = PlateCoreT<double>;
 
 __host__ __device__ constexpr int ut4(int i, int j) {  // 4x4 upper index, i <= j
   return i == 0 ? j : i == 1 ? 3 + j : i == 2 ? 5 + j : 9;
@@ -480,18 +538,19 @@ __host__ __device__ constexpr int ut3(int a, int b) {  // 3x3 upper index, a <= 
   return a == 0 ? b : a == 1 ? 2 + b : 5;
 }
 
-__device__ __forceinline__ void plate_core(const double xl[4], const double yl[4], double young, double poisson,
-                                           double thickness, double shear_factor, PlateCore& C) {
+template <class T>
+__device__ __forceinline__ void plate_core(const T xl[4], const T yl[4], T young, T poisson,
+                                           T thickness, T shear_factor, PlateCoreT<T>& C) {
   const double g = sqrt((double)(1.0f / 3.0f));
   const double al = 1.0 + g, be = 1.0 - g;
-  double x1 = xl[0], x2 = xl[1], x4 = xl[3];
-  double y1 = yl[0], y2 = yl[1], y4 = yl[3];
-  double d12x = x1 - x2, d12y = y1 - y2;
-  double ax = d12x + x4, bx = d12x - x4, cx = (x1 + x2) - x4;
-  double ay = d12y + y4, by = d12y - y4, cy = (y1 + y2) - y4;
-  double ipr[4] = {g * 1.0, g * -1.0, g * -1.0, g * 1.0};
-  double ips[4] = {g * 1.0, g * 1.0, g * -1.0, g * -1.0};
-  double J00[4], J01[4], J10[4], J11[4], D[4], q[4];
+  T x1 = xl[0], x2 = xl[1], x4 = xl[3];
+  T y1 = yl[0], y2 = yl[1], y4 = yl[3];
+  T d12x = x1 - x2, d12y = y1 - y2;
+  T ax = d12x + x4, bx = d12x - x4, cx = (x1 + x2) - x4;
+  T ay = d12y + y4, by = d12y - y4, cy = (y1 + y2) - y4;
+  const double ipr[4] = {g * 1.0, g * -1.0, g * -1.0, g * 1.0};
+  const double ips[4] = {g * 1.0, g * 1.0, g * -1.0, g * -1.0};
+  T J00[4], J01[4], J10[4], J11[4], D[4], q[4];
 #pragma unroll
   for (int ip = 0; ip < 4; ++ip) {
     J00[ip] = fma(ips[ip], bx, ax);
@@ -501,8 +560,8 @@ __device__ __forceinline__ void plate_core(const double xl[4], const double yl[4
     D[ip] = fma(J00[ip], J11[ip], -(J01[ip] * J10[ip]));
   }
   {
-    double D01 = D[0] * D[1], D23 = D[2] * D[3];
-    double inv = 1.0 / (D01 * D23);
+    T D01 = D[0] * D[1], D23 = D[2] * D[3];
+    T inv = 1.0 / (D01 * D23);
     q[0] = (D[1] * D23) * inv;
     q[1] = (D[0] * D23) * inv;
     q[2] = (D[3] * D01) * inv;
@@ -515,15 +574,15 @@ __device__ __forceinline__ void plate_core(const double xl[4], const double yl[4
   }
 #pragma unroll
   for (int k = 0; k < 16; ++k) C.Sxy[k] = 0.0;
-  double Wr[4], Ws[4];
+  T Wr[4], Ws[4];
 #pragma unroll
   for (int ip = 0; ip < 4; ++ip) {
-    double sp = 1.0 + ips[ip], sm = 1.0 - ips[ip], rp = 1.0 + ipr[ip], rm = 1.0 - ipr[ip];
-    double P1 = J11[ip] * sp, P2 = J11[ip] * sm, P3 = J01[ip] * rp, P4 = J01[ip] * rm;
-    double Q1 = J00[ip] * rp, Q2 = J00[ip] * rm, Q3 = J10[ip] * sp, Q4 = J10[ip] * sm;
-    double gx[4] = {P1 - P3, (-P1) - P4, P4 - P2, P2 + P3};
-    double gy[4] = {Q1 - Q3, Q2 + Q3, Q4 - Q2, (-Q1) - Q4};
-    double a[4], bq[4];
+    T sp = 1.0 + ips[ip], sm = 1.0 - ips[ip], rp = 1.0 + ipr[ip], rm = 1.0 - ipr[ip];
+    T P1 = J11[ip] * sp, P2 = J11[ip] * sm, P3 = J01[ip] * rp, P4 = J01[ip] * rm;
+    T Q1 = J00[ip] * rp, Q2 = J00[ip] * rm, Q3 = J10[ip] * sp, Q4 = J10[ip] * sm;
+    T gx[4] = {P1 - P3, (-P1) - P4, P4 - P2, P2 + P3};
+    T gy[4] = {Q1 - Q3, Q2 + Q3, Q4 - Q2, (-Q1) - Q4};
+    T a[4], bq[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       a[i] = q[ip] * gx[i];
@@ -543,28 +602,28 @@ __device__ __forceinline__ void plate_core(const double xl[4], const double yl[4
     Wr[ip] = fma(J11[ip], J11[ip], J10[ip] * J10[ip]) * q[ip];
     Ws[ip] = fma(J01[ip], J01[ip], J00[ip] * J00[ip]) * q[ip];
   }
-  double dinv = 1.0 / (1.0 - poisson * poisson);
-  double Et = young * thickness;
+  T dinv = 1.0 / (1.0 - poisson * poisson);
+  T Et = young * thickness;
   C.cmq = (Et * dinv) * 0.0625;
   C.cbq = ((C.cmq * thickness) * thickness) * 0x1.5555555555555p-4;
-  double omn = 1.0 - poisson;
-  double cq = ((Et * shear_factor) * omn) * (dinv * 0x1p-7);
+  T omn = 1.0 - poisson;
+  T cq = ((Et * shear_factor) * omn) * (dinv * 0x1p-7);
   C.gam = omn * 0.5;
   C.nu = poisson;
   const double al2 = al * al, be2 = be * be, ab = al * be;
-  double W0p = Wr[0] + Wr[1], W0m = Wr[2] + Wr[3];
-  double W1p = Ws[0] + Ws[3], W1m = Ws[1] + Ws[2];
-  double A12 = cq * fma(W0p, al2, W0m * be2);
-  double A1243 = cq * ((W0p + W0m) * ab);
-  double A43 = cq * fma(W0p, be2, W0m * al2);
-  double B14 = cq * fma(W1p, al2, W1m * be2);
-  double B1423 = cq * ((W1p + W1m) * ab);
-  double B23 = cq * fma(W1p, be2, W1m * al2);
+  T W0p = Wr[0] + Wr[1], W0m = Wr[2] + Wr[3];
+  T W1p = Ws[0] + Ws[3], W1m = Ws[1] + Ws[2];
+  T A12 = cq * fma(W0p, al2, W0m * be2);
+  T A1243 = cq * ((W0p + W0m) * ab);
+  T A43 = cq * fma(W0p, be2, W0m * al2);
+  T B14 = cq * fma(W1p, al2, W1m * be2);
+  T B1423 = cq * ((W1p + W1m) * ab);
+  T B23 = cq * fma(W1p, be2, W1m * al2);
   C.E12[0] = 2.0; C.E12[1] = -d12y; C.E12[2] = d12x;
   C.E43[0] = 2.0; C.E43[1] = -y4; C.E43[2] = x4;
-  double E14[3] = {2.0, -(y1 - y4), x1 - x4};
-  double E23[3] = {2.0, -y2, x2};
-  double F14[3], H14[3], F23[3];
+  T E14[3] = {2.0, -(y1 - y4), x1 - x4};
+  T E23[3] = {2.0, -y2, x2};
+  T F14[3], H14[3], F23[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     C.F12[k] = A12 * C.E12[k];
@@ -587,46 +646,47 @@ __device__ __forceinline__ void plate_core(const double xl[4], const double yl[4
 }
 
 // Local 6x6 block (i, j), i <= j, of the plate's 24x24 matrix, row-major.
-__device__ __forceinline__ void plate_local_block(const PlateCore& C, int i, int j, double blk[36]) {
+template <class T>
+__device__ __forceinline__ void plate_local_block(const PlateCoreT<T>& C, int i, int j, T blk[36]) {
 #pragma unroll
   for (int k = 0; k < 36; ++k) blk[k] = 0.0;
   int lo = i < j ? i : j, hi = i < j ? j : i;
-  double Sxx = C.Sxx[ut4(lo, hi)], Syy = C.Syy[ut4(lo, hi)];
-  double tuu = fma(C.gam, Syy, Sxx);
-  double tvv = fma(C.gam, Sxx, Syy);
-  double tuv_ij = fma(C.gam, C.Sxy[4 * j + i], C.nu * C.Sxy[4 * i + j]);
-  double tuv_ji = fma(C.gam, C.Sxy[4 * i + j], C.nu * C.Sxy[4 * j + i]);
+  T Sxx = C.Sxx[ut4(lo, hi)], Syy = C.Syy[ut4(lo, hi)];
+  T tuu = fma(C.gam, Syy, Sxx);
+  T tvv = fma(C.gam, Sxx, Syy);
+  T tuv_ij = fma(C.gam, C.Sxy[4 * j + i], C.nu * C.Sxy[4 * i + j]);
+  T tuv_ji = fma(C.gam, C.Sxy[4 * i + j], C.nu * C.Sxy[4 * j + i]);
   blk[0] = C.cmq * tuu;
   blk[7] = C.cmq * tvv;
-  double uv = C.cmq * tuv_ij;
+  T uv = C.cmq * tuv_ij;
   blk[1] = uv;
   blk[6] = (i == j) ? uv : C.cmq * tuv_ji;
   const int g0i = i < 2 ? 0 : 1, g0j = j < 2 ? 0 : 1;
-  const double s0i = (i == 1 || i == 2) ? -1.0 : 1.0, s0j = (j == 1 || j == 2) ? -1.0 : 1.0;
+  const T s0i = (i == 1 || i == 2) ? -1.0 : 1.0, s0j = (j == 1 || j == 2) ? -1.0 : 1.0;
   const int g1i = (i == 0 || i == 3) ? 0 : 1, g1j = (j == 0 || j == 3) ? 0 : 1;
-  const double s1i = i >= 2 ? -1.0 : 1.0, s1j = j >= 2 ? -1.0 : 1.0;
+  const T s1i = i >= 2 ? -1.0 : 1.0, s1j = j >= 2 ? -1.0 : 1.0;
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
       if (i == j && b < a) continue;
       int l3 = a < b ? a : b, h3 = a < b ? b : a;
-      double t1;
+      T t1;
       if (g1i == 0 && g1j == 0) t1 = C.P14[ut3(l3, h3)];
       else if (g1i == 1 && g1j == 1) t1 = C.P23[ut3(l3, h3)];
       else if (g1i == 0) t1 = C.P1423[3 * a + b];
       else t1 = C.P1423[3 * b + a];
-      double sg1 = (a == 0 ? s1i : 1.0) * (b == 0 ? s1j : 1.0);
+      T sg1 = (a == 0 ? s1i : 1.0) * (b == 0 ? s1j : 1.0);
       if (sg1 < 0) t1 = -t1;
-      double f, e;
+      T f, e;
       if (g0i == 0 && g0j == 0) { f = C.F12[l3]; e = C.E12[h3]; }
       else if (g0i == 1 && g0j == 1) { f = C.F43[l3]; e = C.E43[h3]; }
       else if (g0i == 0) { f = C.G12[a]; e = C.E43[b]; }
       else { f = C.G12[b]; e = C.E43[a]; }
-      double sg0 = (a == 0 ? s0i : 1.0) * (b == 0 ? s0j : 1.0);
+      T sg0 = (a == 0 ? s0i : 1.0) * (b == 0 ? s0j : 1.0);
       if (sg0 < 0) f = -f;
-      double sh = fma(f, e, t1);
-      double v = sh;
+      T sh = fma(f, e, t1);
+      T v = sh;
       if (a >= 1 && b >= 1) {
         if (a == 2 && b == 2) v = fma(C.cbq, tuu, sh);
         else if (a == 1 && b == 1) v = fma(C.cbq, tvv, sh);
@@ -643,8 +703,8 @@ __device__ __forceinline__ void plate_local_block(const PlateCore& C, int i, int
 // and sign of the assumed-strain shear terms folds to a constant, so the only
 // FP64 instructions left are the products and sums themselves (same operations,
 // same order, bit-identical to plate_local_block).
-template <int I, int J>
-__device__ __forceinline__ void plate_block_ct(const PlateCore& C, double blk[36]) {
+template <int I, int J, class T>
+__device__ __forceinline__ void plate_block_ct(const PlateCoreT<T>& C, T blk[36]) {
   static_assert(I <= J, "pairs are enumerated with I <= J");
   constexpr int g0i = I < 2 ? 0 : 1, g0j = J < 2 ? 0 : 1;
   constexpr bool n0i = I == 1 || I == 2, n0j = J == 1 || J == 2;
@@ -652,14 +712,14 @@ __device__ __forceinline__ void plate_block_ct(const PlateCore& C, double blk[36
   constexpr bool n1i = I >= 2, n1j = J >= 2;
 #pragma unroll
   for (int k = 0; k < 36; ++k) blk[k] = 0.0;
-  const double Sxx = C.Sxx[ut4(I, J)], Syy = C.Syy[ut4(I, J)];
-  const double tuu = fma(C.gam, Syy, Sxx);
-  const double tvv = fma(C.gam, Sxx, Syy);
-  const double tuv_ij = fma(C.gam, C.Sxy[4 * J + I], C.nu * C.Sxy[4 * I + J]);
-  const double tuv_ji = fma(C.gam, C.Sxy[4 * I + J], C.nu * C.Sxy[4 * J + I]);
+  const T Sxx = C.Sxx[ut4(I, J)], Syy = C.Syy[ut4(I, J)];
+  const T tuu = fma(C.gam, Syy, Sxx);
+  const T tvv = fma(C.gam, Sxx, Syy);
+  const T tuv_ij = fma(C.gam, C.Sxy[4 * J + I], C.nu * C.Sxy[4 * I + J]);
+  const T tuv_ji = fma(C.gam, C.Sxy[4 * I + J], C.nu * C.Sxy[4 * J + I]);
   blk[0] = C.cmq * tuu;
   blk[7] = C.cmq * tvv;
-  const double uv = C.cmq * tuv_ij;
+  const T uv = C.cmq * tuv_ij;
   blk[1] = uv;
   blk[6] = (I == J) ? uv : C.cmq * tuv_ji;
 #pragma unroll
@@ -668,22 +728,22 @@ __device__ __forceinline__ void plate_block_ct(const PlateCore& C, double blk[36
     for (int b = 0; b < 3; ++b) {
       if (I == J && b < a) continue;
       const int l3 = a < b ? a : b, h3 = a < b ? b : a;
-      double t1;
+      T t1;
       if (g1i == 0 && g1j == 0) t1 = C.P14[ut3(l3, h3)];
       else if (g1i == 1 && g1j == 1) t1 = C.P23[ut3(l3, h3)];
       else if (g1i == 0) t1 = C.P1423[3 * a + b];
       else t1 = C.P1423[3 * b + a];
       const bool neg1 = ((a == 0) && n1i) != ((b == 0) && n1j);
       if (neg1) t1 = -t1;
-      double f, e;
+      T f, e;
       if (g0i == 0 && g0j == 0) { f = C.F12[l3]; e = C.E12[h3]; }
       else if (g0i == 1 && g0j == 1) { f = C.F43[l3]; e = C.E43[h3]; }
       else if (g0i == 0) { f = C.G12[a]; e = C.E43[b]; }
       else { f = C.G12[b]; e = C.E43[a]; }
       const bool neg0 = ((a == 0) && n0i) != ((b == 0) && n0j);
       if (neg0) f = -f;
-      const double sh = fma(f, e, t1);
-      double v = sh;
+      const T sh = fma(f, e, t1);
+      T v = sh;
       if (a >= 1 && b >= 1) {
         if (a == 2 && b == 2) v = fma(C.cbq, tuu, sh);
         else if (a == 1 && b == 1) v = fma(C.cbq, tvv, sh);
@@ -697,13 +757,14 @@ __device__ __forceinline__ void plate_block_ct(const PlateCore& C, double blk[36
 }
 
 // rotate a local node-pair block to global axes: T^T K T restricted to (i, j)
-__device__ __forceinline__ void plate_rotate_block(const double R[9], bool diag, const double blk[36], double out[36]) {
+template <class T>
+__device__ __forceinline__ void plate_rotate_block(const T R[9], bool diag, const T blk[36], T out[36]) {
 #pragma unroll
   for (int p = 0; p < 2; ++p)
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       if (diag && p == 1 && q == 0) continue;
-      double M[9], o[9];
+      T M[9], o[9];
 #pragma unroll
       for (int a = 0; a < 3; ++a)
 #pragma unroll

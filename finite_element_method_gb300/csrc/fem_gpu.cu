@@ -1126,6 +1126,11 @@ struct fem_gpu {
   bool numeric_done = false;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   float t_elem_ms = 0, t_reduce_ms = 0;
+  // vector-Jacobian product
+  bool vjp_inc_valid = false;
+  DevBuf<int64_t> vjp_inc_off, vjp_inc;
+  DevBuf<double> vjp_in, vjp_uT, vjp_lT, vjp_W, vjp_gc, vjp_gp, vjp_gxyz;
+  float t_vjp_ms = 0;
 
   int fail(int code, const char* fmt, ...) {
     char b[1024];
@@ -1153,6 +1158,7 @@ struct fem_gpu {
     runs.push_back(Run{kind, begin, count, n_pairs});
     n_pairs += count * ppe;
     pattern_valid = false;
+    vjp_inc_valid = false;
     numeric_done = false;
   }
 };
@@ -1263,6 +1269,10 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   h->g_kind.release();
   h->flag.release();
   h->cub_tmp.release();
+  for (DevBuf<double>* v : {&h->vjp_in, &h->vjp_uT, &h->vjp_lT, &h->vjp_W, &h->vjp_gc, &h->vjp_gp, &h->vjp_gxyz})
+    v->release();
+  h->vjp_inc_off.release();
+  h->vjp_inc.release();
   h->vstatus.release();
   h->vfirst.release();
   for (auto& ev : h->ev)
@@ -2131,3 +2141,5 @@ extern "C" int fem_gpu_last_numeric_timing(fem_gpu_t* h, float* element_ms, floa
 
 // batched assembly of many structures (reuses the kernels and the handle above)
 #include "fem_batch.cuh"
+// vector-Jacobian product (reuses the element arithmetic and the handle above)
+#include "fem_adjoint.cuh"

@@ -252,6 +252,28 @@ class FEM:
                                                       ctypes.byref(d)))
         return a.value, b.value, c.value, d.value
 
+    def vjp(self, u, lam):
+        """Gradient of F = -sum_p lam_p^T K u_p for u, lam of shape (npairs, 6 * nodes_number):
+        returns dict(truss (n_truss, 3: E, A, A2), beam (n_beam, 5: E, A, I11, I22, It),
+        plate (n_plate, 2: E, t), xyz (n_nodes, 3))."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        if u.ndim == 1:
+            u, lam = u[None], lam[None]
+        assert u.shape == lam.shape and u.shape[1] == 6 * self.nodes_number
+        nt, nb, npl = self.element_counts()
+        out = dict(truss=np.zeros((nt, 3)), beam=np.zeros((nb, 5)), plate=np.zeros((npl, 2)),
+                   xyz=np.zeros((self.node_count(), 3)))
+        self._check(self._L.fem_gpu_vjp(self._h, ptr(u, c_double), ptr(lam, c_double), u.shape[0],
+                                        ptr(out["truss"], c_double), ptr(out["beam"], c_double),
+                                        ptr(out["plate"], c_double), ptr(out["xyz"], c_double)))
+        return out
+
+    def vjp_last_ms(self) -> float:
+        x = c_float(0)
+        self._check(self._L.fem_gpu_vjp_last_ms(self._h, ctypes.byref(x)))
+        return x.value
+
     def last_numeric_timing(self):
         """(element kernels ms, reduction ms) of the last numeric pass, CUDA events on the handle's stream."""
         a, b = c_float(0), c_float(0)

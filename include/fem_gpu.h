@@ -154,6 +154,23 @@ int fem_gpu_get_pattern_stats(fem_gpu_t* h, int64_t* n_blocks, int64_t* n_contri
  * handle's stream (milliseconds): element kernels (all types) and the reduction. */
 int fem_gpu_last_numeric_timing(fem_gpu_t* h, float* element_ms, float* reduce_ms);
 
+/* ---- vector-Jacobian product --------------------------------------------------
+ * No counterpart in the reference (it has no derivatives).  For npairs (u, lambda)
+ * pairs -- host arrays of npairs x (6 * nodes_number) doubles, pair-major, DOFs
+ * in the stiffness's row order -- the gradient of F = -sum_p lambda_p^T K u_p:
+ *   g_truss  n_truss x 3  (E, A, A2; A2 is 0 without a taper)
+ *   g_beam   n_beam x 5   (E, A, I11, I22, It)
+ *   g_plate  n_plate x 2  (E, thickness)
+ *   g_xyz    n_nodes x 3  (node coordinates, index order)
+ * i.e. dF/dtheta = -sum_p lambda_p^T (dK/dtheta) u_p, the adjoint sensitivity of
+ * a compliance-type objective.  Element matrices are recomputed in forward-mode
+ * dual arithmetic, one parameter per thread, and never stored.  Any output may be
+ * NULL.  1 <= npairs <= 512.  Requires a prior fem_gpu_assemble. */
+int fem_gpu_vjp(fem_gpu_t* h, const double* u, const double* lam, int npairs, double* g_truss, double* g_beam,
+                double* g_plate, double* g_xyz);
+/* device time of the last fem_gpu_vjp (transposes, element products, node sums), ms */
+int fem_gpu_vjp_last_ms(fem_gpu_t* h, float* ms);
+
 /* ---- batched assembly -------------------------------------------------------
  * No counterpart in the reference (it assembles one model per FEM value): a
  * batch assembles many independent, already assembled models in one numeric
