@@ -171,7 +171,7 @@ def run_batch(args):
     from finite_element_method_gb300 import Batch
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    structures = meshes.batch_structures()
+    structures = meshes.batch_structures(n_structures=64 if args.small else 512)
     models = []
     t0 = time.perf_counter()
     for m in structures:
@@ -247,7 +247,7 @@ def run_adjoint(args):
     import torch
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    mesh = meshes.adjoint_model()
+    mesh = meshes.adjoint_model(frame=(21, 21, 5), slab=(200, 200)) if args.small else meshes.adjoint_model()
     n_el = mesh.n_elements
     g = FEM(meshes.REL_TOL, meshes.ABS_TOL, mesh.nodes_number)
     meshes.load(g, mesh)
@@ -277,7 +277,8 @@ def run_adjoint(args):
     line = {"metric": "adjoint vjp elements/s (64 (u, lambda) pairs)", "value": n_el / (t_v * 1e-3),
             "unit": "elements/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_v,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"51x51x11 beam frame ({len(mesh.beams['numbers']):,} beams) + 500x500 plate "
+            "config": {"workload": f"{'x'.join(map(str, mesh.meta['frame']))} beam frame "
+                       f"({len(mesh.beams['numbers']):,} beams) + {'x'.join(map(str, mesh.meta['slab']))} plate "
                        f"slab ({len(mesh.plates['numbers']):,} plates), {args.pairs} (u, lambda) pairs ~ N(0, 1), "
                        f"{n_params:,} parameters (E, A, I11, I22, It per beam; E, t per plate; node xyz)"},
             "adjoint": {"vjp_ms": t_v, "forward_numeric_ms": t_f, "vjp_over_forward": t_v / t_f,
@@ -299,6 +300,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--nx", type=int, default=1000, help="plate mesh size (nx x nx); 1000 is the full workload")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--small", action="store_true",
+                    help="profiling-sized batch (64 structures) and adjoint (21x21x5 frame + 200x200 slab) cases")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
