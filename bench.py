@@ -49,6 +49,10 @@ WORK = {
 }
 # bytes per element read by the element kernel (connectivity, coordinates of its nodes, properties)
 IN_BYTES = {"plate": 4 * 4 + 4 * 24 + 4 * 8, "beam": 2 * 4 + 2 * 24 + 11 * 8, "truss": 2 * 4 + 2 * 24 + 3 * 8}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per element of one launch of the element kernel,
+# from an ncu capture of k_plate on the 500 x 500 plate mesh (250,000 plates: 55.7 MB read + 242.3 MB written),
+# scaled by the element count (the kernel's traffic is per element: its inputs and its packed blocks)
+TRAFFIC_PER_ELEMENT = {"plate": (55675392 + 242335232) / 250000}
 
 
 def measured_peaks():
@@ -389,7 +393,10 @@ def main():
                 "frac": frac_fp64}
     else:
         roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_gbs, "unit": "GB/s", "frac": frac_hbm}
-    roof.update({"kernel": dom, "traffic": None,
+    traffic = TRAFFIC_PER_ELEMENT.get(args.workload) if dom == "element" else None
+    roof.update({"kernel": dom, "traffic": None if traffic is None else int(traffic * n_el),
+                 "traffic_source": "ncu DRAM bytes of k_plate on the 500 x 500 mesh, scaled per plate"
+                 if traffic is not None else None,
                  "peak_source": f"hbm: {peak_src} copy bandwidth; fp64: 2 DFMA/clk/SM x 152 SMs x 2070 MHz",
                  "algorithmic": {k: {"bytes": int(v["bytes"]), "flops": int(v["flops"])} for k, v in kern.items()},
                  "per_kernel_ms": {k: v["ms"] for k, v in kern.items()},

@@ -245,12 +245,6 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
   if (!out || (n_models && !models)) return FEM_GPU_ERR_ARGUMENT;
   *out = nullptr;
   fem_gpu_batch* b = new fem_gpu_batch();
-  int code = FEM_GPU_OK;
-  auto bail = [&](int c) {
-    code = c;
-    return c;
-  };
-  (void)bail;
   for (size_t i = 0; i < n_models; ++i) {
     fem_gpu* m = models[i];
     if (!m || !m->pattern_valid || !m->stream) {
@@ -400,9 +394,7 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
     oz += m->nnz;
   }
   BCK(cudaStreamSynchronize(s));
-  int st = batch_make_graph(b);
-  (void)code;
-  return st;
+  return batch_make_graph(b);
 }
 
 extern "C" int fem_gpu_batch_destroy(fem_gpu_batch_t* b) {

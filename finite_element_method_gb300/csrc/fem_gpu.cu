@@ -91,6 +91,16 @@ struct NodesView {
   }
 };
 
+// interleaved (x, y, z) rows -> the structure-of-arrays coordinates
+__global__ void k_split_xyz(size_t n, const double* __restrict__ xyz, double* __restrict__ x, double* __restrict__ y,
+                            double* __restrict__ z) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x[i] = xyz[3 * i];
+  y[i] = xyz[3 * i + 1];
+  z[i] = xyz[3 * i + 2];
+}
+
 __global__ void k_validate_truss(NodesView nd, const int32_t* __restrict__ n1, const int32_t* __restrict__ n2,
                                  const double* __restrict__ E, const double* __restrict__ A,
                                  const double* __restrict__ A2, size_t begin, size_t count, int* status,
@@ -659,9 +669,6 @@ __device__ __forceinline__ int nth_set_bit(uint64_t m, int n) {
   return 32 + (int)__fns((uint32_t)(m >> 32), 0, n - plo + 1);
 }
 
-constexpr int kRedThreads = 256;
-constexpr int kRedLanes = 16;                        // lanes per global block
-constexpr int kRedBlocks = kRedThreads / kRedLanes;  // global blocks per CTA
 constexpr int kFlagPattern = 1;                      // bit of *flag: the exact-zero pattern changed
 
 // Block-sum slots.  A packed entry of a block with one contribution needs no
@@ -911,13 +918,6 @@ struct CoordKey {
   uint64_t a, b, c;
   bool operator==(const CoordKey& o) const { return a == o.a && b == o.b && c == o.c; }
 };
-struct CoordHash {
-  size_t operator()(const CoordKey& k) const {
-    uint64_t h = k.a * 0x9E3779B97F4A7C15ull ^ (k.b + 0x632BE59BD9B4E019ull) * 0xC2B2AE3D27D4EB4Full ^
-                 (k.c + 0x165667B19E3779F9ull) * 0xD6E8FEB86659FD93ull;
-    return (size_t)(h ^ (h >> 31));
-  }
-};
 CoordKey coord_key(double x, double y, double z) {
   if (x == 0.0) x = 0.0;
   if (y == 0.0) y = 0.0;
@@ -938,17 +938,26 @@ struct Set4 {
   uint32_t s[4];
   bool operator==(const Set4& o) const { return !memcmp(s, o.s, sizeof s); }
 };
-struct Set4Hash {
-  size_t operator()(const Set4& k) const {
-    uint64_t h = 1469598103934665603ull;
-    for (int i = 0; i < 4; ++i) h = (h ^ k.s[i]) * 1099511628211ull;
-    return (size_t)h;
-  }
-};
+// the four numbers in ascending order (a five-comparator sorting network)
 Set4 sorted4(const uint32_t n[4]) {
+  uint32_t a = n[0], b = n[1], c = n[2], d = n[3], t;
+#define FEM_CSWAP(x, y) \
+  if (y < x) {          \
+    t = x;              \
+    x = y;              \
+    y = t;              \
+  }
+  FEM_CSWAP(a, b)
+  FEM_CSWAP(c, d)
+  FEM_CSWAP(a, c)
+  FEM_CSWAP(b, d)
+  FEM_CSWAP(b, c)
+#undef FEM_CSWAP
   Set4 k;
-  memcpy(k.s, n, sizeof k.s);
-  std::sort(k.s, k.s + 4);
+  k.s[0] = a;
+  k.s[1] = b;
+  k.s[2] = c;
+  k.s[3] = d;
   return k;
 }
 
@@ -970,15 +979,18 @@ uint64_t mix64(uint64_t x) {
 // backward-shift deletion; several entries may share a key (the caller's
 // predicate tells them apart), so it serves as map, set and multimap.  The
 // registries behind add_node / add_* (duplicate numbers, node pairs, plate
-// node sets, exact coordinates) hold one entry per node or element.
+// node sets, exact coordinates) hold one entry per node or element.  Key and
+// value share a 16-byte slot (one cache line touch per probe), the load stays
+// at most 1/2, and bulk callers prefetch the home slot of an entry a few
+// iterations ahead.
 class FlatTable {
  public:
   FlatTable() { init(64); }
   template <class Eq>
   int64_t find(uint64_t key, Eq eq) const {
     size_t i = mix64(key) & mask_;
-    while (val_[i] >= 0) {
-      if (key_[i] == key && eq(val_[i])) return val_[i];
+    while (slot_[i].val >= 0) {
+      if (slot_[i].key == key && eq(slot_[i].val)) return slot_[i].val;
       i = (i + 1) & mask_;
     }
     return -1;
@@ -986,62 +998,101 @@ class FlatTable {
   int64_t find(uint64_t key) const {
     return find(key, [](int64_t) { return true; });
   }
+  void prefetch(uint64_t key) const { __builtin_prefetch(&slot_[mix64(key) & mask_]); }
   void insert(uint64_t key, int64_t v) {
-    if (2 * (len_ + 1) > key_.size()) grow();
+    if (2 * (len_ + 1) > slot_.size()) rehash(slot_.size());
     put(key, v);
   }
   void erase(uint64_t key, int64_t v) {
     size_t i = mix64(key) & mask_;
-    while (val_[i] >= 0 && !(key_[i] == key && val_[i] == v)) i = (i + 1) & mask_;
-    if (val_[i] < 0) return;
+    while (slot_[i].val >= 0 && !(slot_[i].key == key && slot_[i].val == v)) i = (i + 1) & mask_;
+    if (slot_[i].val < 0) return;
     // backward-shift deletion
     size_t j = i;
     for (;;) {
       j = (j + 1) & mask_;
-      if (val_[j] < 0) break;
-      size_t home = mix64(key_[j]) & mask_;
+      if (slot_[j].val < 0) break;
+      size_t home = mix64(slot_[j].key) & mask_;
       if (((j - home) & mask_) >= ((j - i) & mask_)) {
-        key_[i] = key_[j];
-        val_[i] = val_[j];
+        slot_[i] = slot_[j];
         i = j;
       }
     }
-    val_[i] = -1;
+    slot_[i].val = -1;
     --len_;
   }
   void reserve(size_t n) {
-    if (2 * n > key_.size()) rehash(n);
+    if (2 * n > slot_.size()) rehash(n);
   }
+  size_t size() const { return len_; }
 
  private:
-  void init(size_t cap) {
+  struct Slot {
+    uint64_t key;
+    int64_t val;
+  };
+  void init(size_t n) {
     size_t c = 64;
-    while (c < cap) c <<= 1;
-    key_.assign(c, 0);
-    val_.assign(c, -1);
+    while (c < 2 * n) c <<= 1;
+    slot_.assign(c, Slot{0, -1});
     mask_ = c - 1;
     len_ = 0;
   }
   void put(uint64_t key, int64_t v) {
     size_t i = mix64(key) & mask_;
-    while (val_[i] >= 0) i = (i + 1) & mask_;
-    key_[i] = key;
-    val_[i] = v;
+    while (slot_[i].val >= 0) i = (i + 1) & mask_;
+    slot_[i] = Slot{key, v};
     ++len_;
   }
   void rehash(size_t n) {
-    std::vector<uint64_t> k;
-    std::vector<int64_t> v;
-    k.swap(key_);
-    v.swap(val_);
-    init(4 * n);
-    for (size_t i = 0; i < k.size(); ++i)
-      if (v[i] >= 0) put(k[i], v[i]);
+    std::vector<Slot> old;
+    old.swap(slot_);
+    init(std::max(n, 2 * len_ + 2));
+    for (const Slot& s : old)
+      if (s.val >= 0) put(s.key, s.val);
   }
-  void grow() { rehash(len_ + 1); }
-  std::vector<uint64_t> key_;
-  std::vector<int64_t> val_;
+  std::vector<Slot> slot_;
   size_t mask_ = 0, len_ = 0;
+};
+
+// Number -> index registry (node and element numbers, unique keys).  Numbers
+// below a bound that follows the expected count (2 x reserved + 4096) live in
+// a direct array, so the usual dense numbering costs no hashing and no cache
+// miss per lookup; others fall back to a FlatTable.  A key stored in the table
+// before the array grew over it is still found there.
+class NumberMap {
+ public:
+  int64_t find(uint64_t key) const {
+    if (key < dense_.size() && dense_[key] >= 0) return dense_[key];
+    return table_.size() ? table_.find(key) : -1;
+  }
+  void prefetch(uint64_t key) const {
+    if (key < dense_.size()) __builtin_prefetch(&dense_[key]);
+    else if (table_.size()) table_.prefetch(key);
+  }
+  void reserve(size_t total) {
+    bound_ = std::max(bound_, 2 * total + 4096);
+  }
+  void insert(uint64_t key, int64_t v) {
+    if (key < bound_) {
+      if (key >= dense_.size()) dense_.resize(std::min<size_t>(bound_, std::max<size_t>(key + 1, 2 * dense_.size())), -1);
+      dense_[key] = v;
+    } else {
+      table_.insert(key, v);
+    }
+  }
+  void erase(uint64_t key, int64_t v) {
+    if (key < dense_.size() && dense_[key] == v) {
+      dense_[key] = -1;
+      return;
+    }
+    if (table_.size()) table_.erase(key, v);
+  }
+
+ private:
+  std::vector<int64_t> dense_;
+  FlatTable table_;
+  size_t bound_ = 4096;
 };
 
 uint64_t coord_hash(const CoordKey& k) { return mix64(k.a ^ mix64(k.b ^ mix64(k.c))); }
@@ -1065,30 +1116,31 @@ struct fem_gpu {
   size_t n_nodes = 0;
   std::vector<uint32_t> idx_number;
   std::vector<CoordKey> node_ck;  // normalised coordinate bits by index
-  FlatTable node_idx;             // number -> index
+  NumberMap node_idx;             // number -> index
   FlatTable node_coords;          // coordinate hash -> index
   DevBuf<double> dx, dy, dz;
+  DevBuf<double> stage;           // interleaved coordinates on their way in
   // elements
   std::vector<Run> runs;
   size_t n_pairs = 0;
   // truss
   size_t nt = 0;
   std::vector<uint32_t> t_num;
-  FlatTable t_by_num;  // number -> element index
+  NumberMap t_by_num;  // number -> element index
   FlatTable t_pairs;   // node pair -> element index
   DevBuf<int32_t> t_n1, t_n2;
   DevBuf<double> t_E, t_A, t_A2;
   // beam
   size_t nbm = 0;
   std::vector<uint32_t> b_num;
-  FlatTable b_by_num;
+  NumberMap b_by_num;
   FlatTable b_pairs;
   DevBuf<int32_t> b_n1, b_n2;
   DevBuf<double> b_E, b_nu, b_A, b_i11, b_i22, b_i12, b_it, b_ks, b_ax, b_ay, b_az;
   // plate
   size_t np = 0;
   std::vector<uint32_t> p_num, p_nodes;
-  FlatTable p_by_num;
+  NumberMap p_by_num;
   FlatTable p_sets;  // sorted node-number set hash -> element index
   DevBuf<int32_t> p_n1, p_n2, p_n3, p_n4;
   DevBuf<double> p_E, p_nu, p_t, p_ks;
@@ -1239,7 +1291,7 @@ extern "C" int fem_gpu_create(double rel_tol, double abs_tol, uint32_t nodes_num
 extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   if (!h) return FEM_GPU_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  DevBuf<double>* d[] = {&h->dx, &h->dy, &h->dz, &h->t_E, &h->t_A, &h->t_A2, &h->b_E, &h->b_nu, &h->b_A,
+  DevBuf<double>* d[] = {&h->dx, &h->dy, &h->dz, &h->stage, &h->t_E, &h->t_A, &h->t_A2, &h->b_E, &h->b_nu, &h->b_A,
                          &h->b_i11, &h->b_i22, &h->b_i12, &h->b_it, &h->b_ks, &h->b_ax, &h->b_ay, &h->b_az,
                          &h->p_E, &h->p_nu, &h->p_t, &h->p_ks, &h->V, &h->values};
   for (auto* b : d) b->release();
@@ -1296,11 +1348,16 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
   h->node_idx.reserve(h->n_nodes + n);
   h->node_coords.reserve(h->n_nodes + n);
   h->node_ck.reserve(h->n_nodes + n);
-  std::vector<double> xs, ys, zs;
-  xs.reserve(n);
-  ys.reserve(n);
-  zs.reserve(n);
+  h->idx_number.reserve(h->n_nodes + n);
+  constexpr size_t kAhead = 8;  // prefetch distance (entries) into the coordinate registry
+  for (size_t q = 0; q < std::min(n, kAhead); ++q)
+    h->node_coords.prefetch(coord_hash(coord_key(xyz[3 * q], xyz[3 * q + 1], xyz[3 * q + 2])));
   for (; k < n; ++k) {
+    if (k + kAhead < n) {
+      const double* f = xyz + 3 * (k + kAhead);
+      h->node_coords.prefetch(coord_hash(coord_key(f[0], f[1], f[2])));
+      h->node_idx.prefetch(numbers[k + kAhead]);
+    }
     uint32_t num = numbers[k];
     double x = xyz[3 * k], y = xyz[3 * k + 1], z = xyz[3 * k + 2];
     size_t index = h->n_nodes;
@@ -1326,17 +1383,16 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
     h->node_idx.insert(num, (int64_t)index);
     h->node_ck.push_back(ck);
     h->idx_number.push_back(num);
-    xs.push_back(x);
-    ys.push_back(y);
-    zs.push_back(z);
     h->n_nodes++;
   }
   if (n_added) *n_added = k;
   size_t m = h->n_nodes - start;
   if (m) {
-    CK(cudaMemcpyAsync(h->dx.p + start, xs.data(), m * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->dy.p + start, ys.data(), m * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->dz.p + start, zs.data(), m * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    // the accepted prefix of the caller's interleaved xyz goes up as is and is split on the device
+    CK(upload(h->stage, 0, xyz, 3 * m, h->stream));
+    k_split_xyz<<<grid_for(m, 256), 256, 0, h->stream>>>(m, h->stage.p, h->dx.p + start, h->dy.p + start,
+                                                         h->dz.p + start);
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
     h->pattern_valid = false;
     h->numeric_done = false;
@@ -1345,6 +1401,8 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
 }
 
 namespace {
+constexpr size_t kRegAhead = 8;  // prefetch distance (elements) into the registries of the bulk add_* loops
+
 int lookup_node(fem_gpu* h, uint32_t num, int32_t* idx) {
   int64_t i = h->node_idx.find(num);
   if (i < 0) return h->fail(FEM_GPU_ERR_NODE_NOT_EXIST, "Node with number %u does not exist!", num);
@@ -1368,7 +1426,15 @@ extern "C" int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const 
   int host_code = FEM_GPU_OK;
   std::string host_err;
   size_t k = 0;
+  h->t_by_num.reserve(h->nt + n);
+  h->t_pairs.reserve(h->nt + n);
   for (; k < n; ++k) {
+    if (k + kRegAhead < n) {
+      const uint32_t* f = nodes + 2 * (k + kRegAhead);
+      h->t_pairs.prefetch(pair_key(f[0], f[1]));
+      h->node_idx.prefetch(f[0]);
+      h->node_idx.prefetch(f[1]);
+    }
     uint32_t num = numbers[k], u = nodes[2 * k], v = nodes[2 * k + 1];
     int32_t a, b;
     if ((host_code = lookup_node(h, u, &a)) || (host_code = lookup_node(h, v, &b))) break;
@@ -1447,7 +1513,20 @@ extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const ui
   int host_code = FEM_GPU_OK;
   std::string host_err;
   size_t k = 0;
+  h->b_by_num.reserve(h->nbm + n);
+  h->b_pairs.reserve(h->nbm + n);
+  i1.reserve(n);
+  i2.reserve(n);
+  ax.reserve(n);
+  ay.reserve(n);
+  az.reserve(n);
   for (; k < n; ++k) {
+    if (k + kRegAhead < n) {
+      const uint32_t* f = nodes + 2 * (k + kRegAhead);
+      h->b_pairs.prefetch(pair_key(f[0], f[1]));
+      h->node_idx.prefetch(f[0]);
+      h->node_idx.prefetch(f[1]);
+    }
     uint32_t num = numbers[k], u = nodes[2 * k], v = nodes[2 * k + 1];
     int32_t a, b;
     if ((host_code = lookup_node(h, u, &a)) || (host_code = lookup_node(h, v, &b))) break;
@@ -1541,7 +1620,16 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
   int host_code = FEM_GPU_OK;
   std::string host_err;
   size_t k = 0;
+  h->p_by_num.reserve(h->np + n);
+  h->p_sets.reserve(h->np + n);
+  h->p_nodes.reserve(4 * (h->np + n));
+  h->p_num.reserve(h->np + n);
   for (; k < n; ++k) {
+    if (k + kRegAhead < n) {
+      const uint32_t* f = nodes + 4 * (k + kRegAhead);
+      h->p_sets.prefetch(set4_hash(sorted4(f)));
+      for (int q = 0; q < 4; ++q) h->node_idx.prefetch(f[q]);
+    }
     uint32_t num = numbers[k];
     const uint32_t* nn = nodes + 4 * k;
     int32_t ix[4];
@@ -2062,7 +2150,7 @@ extern "C" int fem_gpu_get_groups(fem_gpu_t* h, int32_t* row_node, int32_t* col_
 namespace {
 int rotation_of(fem_gpu* h, int kind, uint32_t number, double* r9) {
   if (!h || !r9) return FEM_GPU_ERR_ARGUMENT;
-  const FlatTable& m = kind == kTruss ? h->t_by_num : kind == kBeam ? h->b_by_num : h->p_by_num;
+  const NumberMap& m = kind == kTruss ? h->t_by_num : kind == kBeam ? h->b_by_num : h->p_by_num;
   const int64_t found = m.find(number);
   const char* nm = kind == kTruss ? "Truss" : kind == kBeam ? "Beam" : "Plate";
   if (found < 0) return h->fail(FEM_GPU_ERR_ARGUMENT, "%s element with number %u does not exist!", nm, number);
