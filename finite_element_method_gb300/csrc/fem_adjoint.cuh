@@ -90,68 +90,248 @@ __device__ __forceinline__ void seed3(Dual x[3], const double* v, int base, int 
   for (int c = 0; c < 3; ++c) x[c] = Dual(v[c], dir == base + c ? 1.0 : 0.0);
 }
 
-template <int I, int J>
-__device__ __forceinline__ double plate_pair_dual(const PlateCoreT<Dual>& C, const Dual R[9], bool rot,
-                                                  const double* __restrict__ W) {
-  Dual blk[36];
-  plate_block_ct<I, J>(C, blk);
-  if (rot) {
-    Dual o[36];
-    plate_rotate_block(R, I == J, blk, o);
-    return contract_pair<24>(o, 6 * I, 6 * J, I == J, W);
-  }
-  return contract_pair<24>(blk, 6 * I, 6 * J, I == J, W);
+// Plates, in the element's local frame.  With T = blockdiag(R) (eight 3x3
+// copies), S = T W_e T^T and Sh = S + S^T = T (W_e + W_e^T) T^T, the
+// contraction is f = <K_g, W_e> = <K_l, S> = 1/2 <K_l, Sh>, and its gradient
+// has two parts:
+//  * through K_l -- the local coordinates xl, yl of nodes 1, 2, 4 (node 3 is
+//    the local origin), E and t: eight forward-mode directions, one per lane
+//    of the plate's 8-lane group, each contracted with Sh on K_l's structural
+//    entries (13 or 14 of a node-pair block's 36; K_l is zero elsewhere, so
+//    no rotated dual blocks are formed);
+//  * through R -- with omega = dR R^T (dT = blockdiag(omega) T):
+//    df = <omega, M>, M = sum_k (K_l Sh)_kk over the eight 3x3 diagonal
+//    blocks, plus the local coordinates' own dependence on R, <H, dR> with
+//    rows 0, 1 of H = sum_i (df/dxl_i, df/dyl_i) (x_i - x_3)^T.
+//    R depends on nodes 2, 3, 4 through (x4 - x3) x (x2 - x3) only, so
+//    dR/dx3 = -(dR/dx2 + dR/dx4): six dual rotations.
+// The chain rule back to global coordinates then uses xl_i = R_0 . (x_i - x_3),
+// yl_i = R_1 . (x_i - x_3).  Lanes: 0..5 seed xl1, yl1, xl2, yl2, xl4, yl4;
+// 6 seeds t; 7 seeds E.
+constexpr int kPlateLanes = 8;
+constexpr int kPlatesPerCta = 4;  // one warp
+constexpr int kPlateKl = 134;     // structural entries of the ten upper node-pair blocks
+
+// upper node-pair block b (0..9) = (I, J): (0,0) (0,1) (0,2) (0,3) (1,1) (1,2) (1,3) (2,2) (2,3) (3,3)
+__host__ __device__ constexpr int plate_pair_i(int b) { return b < 4 ? 0 : b < 7 ? 1 : b < 9 ? 2 : 3; }
+__host__ __device__ constexpr int plate_pair_j(int b) { return b < 4 ? b : b < 7 ? b - 3 : b < 9 ? b - 5 : 3; }
+// first structural entry of block b in the packed list (diagonal blocks 14 entries, others 13)
+__host__ __device__ constexpr int plate_pair_off(int b) {
+  return 13 * b + (b > 0 ? 1 : 0) + (b > 4 ? 1 : 0) + (b > 7 ? 1 : 0);
+}
+// k-th structural entry (row-major index in the 6x6 block): u-v membrane, w-thx-thy plate, thz-thz drilling
+__host__ __device__ constexpr int plate_en(int k) {
+  return k < 2 ? k : k < 4 ? k + 4 : k < 7 ? k + 10 : k < 10 ? k + 13 : k < 13 ? k + 16 : 35;
 }
 
-// plates: directions 0..11 node coordinates (node k = dir / 3, axis dir % 3), 12 E, 13 t
-constexpr int kPlateDirs = 14;
-__global__ void __launch_bounds__(64) k_vjp_plate(size_t n_el, NodesView nd, PlateView pl, double abs_tol,
-                                                  const double* __restrict__ W, double* __restrict__ g_coord,
-                                                  double* __restrict__ g_prop) {
-  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (t >= n_el * kPlateDirs) return;
-  const size_t e = t / kPlateDirs;
-  const int dir = (int)(t - e * kPlateDirs);
-  const int nidx[4] = {pl.n1[e], pl.n2[e], pl.n3[e], pl.n4[e]};
-  Dual X[4][3];
+// <dK_l/dtheta, Sh> over block B's structural entries (halved on diagonal blocks); the block's
+// values go to Kl on the lane that owns the block
+template <int B>
+__device__ __forceinline__ double plate_local_pair(const PlateCoreT<Dual>& C, const double* __restrict__ Sh,
+                                                   double* __restrict__ Kl, bool owner) {
+  constexpr int I = plate_pair_i(B), J = plate_pair_j(B), NE = I == J ? 14 : 13;
+  Dual blk[36];
+  plate_block_ct<I, J>(C, blk);
+  double acc = 0.0;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    double v[3];
-    nd.get(nidx[k], v);
-    seed3(X[k], v, 3 * k, dir);
+  for (int k = 0; k < NE; ++k) {
+    const int en = plate_en(k);
+    acc = fma(blk[en].d, Sh[(6 * I + en / 6) * 24 + 6 * J + en % 6], acc);
+    if (owner) Kl[plate_pair_off(B) + k] = blk[en].v;
   }
-  Dual R[9];
+  return I == J ? 0.5 * acc : acc;
+}
+
+__global__ void __launch_bounds__(kPlateLanes* kPlatesPerCta) k_vjp_plate(size_t n_el, NodesView nd, PlateView pl,
+                                                                          double abs_tol, const double* __restrict__ W,
+                                                                          double* __restrict__ g_coord,
+                                                                          double* __restrict__ g_prop) {
+  __shared__ double s_sh[kPlatesPerCta][576];
+  __shared__ double s_kl[kPlatesPerCta][kPlateKl];
+  __shared__ double s_m[kPlatesPerCta][kPlateLanes][9];
+  __shared__ double s_phi[kPlatesPerCta][kPlateLanes];
+  __shared__ double s_rot[kPlatesPerCta][kPlateLanes];
+  const int grp = threadIdx.x / kPlateLanes, lane = threadIdx.x % kPlateLanes;
+  const size_t e = (size_t)blockIdx.x * kPlatesPerCta + grp;
+  const bool live = e < n_el;
+  const size_t ec = live ? e : n_el - 1;  // tail groups recompute the last plate and store nothing
+  double* Sh = s_sh[grp];
+  double* Kl = s_kl[grp];
+  const double* We = W + ec * 576;
+
+  // geometry (values): R with the forward kernel's identity fast path, local coordinates
+  const int nidx[4] = {pl.n1[ec], pl.n2[ec], pl.n3[ec], pl.n4[ec]};
+  double X[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) nd.get(nidx[k], X[k]);
+  double R[9];
   if (!plate_rotation(X[1], X[2], X[3], abs_tol, R)) set_identity(R);
-  Dual xl[4] = {0.0, 0.0, 0.0, 0.0}, yl[4] = {0.0, 0.0, 0.0, 0.0};
+  const bool ident = is_identity(R);
+  double xlv[4] = {0.0, 0.0, 0.0, 0.0}, ylv[4] = {0.0, 0.0, 0.0, 0.0}, dv[4][3];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
+    sub3(X[i], X[2], dv[i]);
     if (i == 2) continue;
-    Dual dd[3];
-    sub3(X[i], X[2], dd);
-    xl[i] = (R[0] * dd[0] + R[1] * dd[1]) + R[2] * dd[2];
-    yl[i] = (R[3] * dd[0] + R[4] * dd[1]) + R[5] * dd[2];
+    xlv[i] = (R[0] * dv[i][0] + R[1] * dv[i][1]) + R[2] * dv[i][2];
+    ylv[i] = (R[3] * dv[i][0] + R[4] * dv[i][1]) + R[5] * dv[i][2];
   }
-  const Dual E(pl.E[e], dir == 12 ? 1.0 : 0.0), th(pl.t[e], dir == 13 ? 1.0 : 0.0);
-  PlateCoreT<Dual> C;
-  plate_core(xl, yl, E, Dual(pl.nu[e]), th, Dual(pl.ks[e]), C);
-  // the rotation can be skipped only when it is the identity and does not move
-  bool rot = !is_identity(R);
+
+  // 1. Sh = R (W + W^T) R^T by 3x3 sub-blocks; lane p fills sub-block row p
+  {
+    const int p = lane;
+#pragma unroll 1
+    for (int q = 0; q < 8; ++q) {
+      double ws[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) rot = rot || R[k].d != 0.0;
-  const double* We = W + e * 576;
-  double s = 0.0;
-  s += plate_pair_dual<0, 0>(C, R, rot, We);
-  s += plate_pair_dual<0, 1>(C, R, rot, We);
-  s += plate_pair_dual<0, 2>(C, R, rot, We);
-  s += plate_pair_dual<0, 3>(C, R, rot, We);
-  s += plate_pair_dual<1, 1>(C, R, rot, We);
-  s += plate_pair_dual<1, 2>(C, R, rot, We);
-  s += plate_pair_dual<1, 3>(C, R, rot, We);
-  s += plate_pair_dual<2, 2>(C, R, rot, We);
-  s += plate_pair_dual<2, 3>(C, R, rot, We);
-  s += plate_pair_dual<3, 3>(C, R, rot, We);
-  if (dir < 12) g_coord[e * 12 + dir] = -s;
-  else g_prop[e * 2 + (dir - 12)] = -s;
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) ws[3 * a + b] = We[(3 * p + a) * 24 + 3 * q + b] + We[(3 * q + b) * 24 + 3 * p + a];
+      if (!ident) {
+        double t[9];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) t[3 * a + c] = (ws[3 * a] * R[3 * c] + ws[3 * a + 1] * R[3 * c + 1]) + ws[3 * a + 2] * R[3 * c + 2];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) ws[3 * a + c] = (R[3 * a] * t[c] + R[3 * a + 1] * t[3 + c]) + R[3 * a + 2] * t[6 + c];
+      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) Sh[(3 * p + a) * 24 + 3 * q + b] = ws[3 * a + b];
+    }
+  }
+  __syncthreads();
+
+  // 2. one forward-mode direction per lane through K_l, contracted with Sh
+  {
+    Dual xl[4], yl[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int s = i == 3 ? 2 : i;  // seed slot of node i (node 3 is the origin: none)
+      xl[i] = Dual(xlv[i], (i != 2 && lane == 2 * s) ? 1.0 : 0.0);
+      yl[i] = Dual(ylv[i], (i != 2 && lane == 2 * s + 1) ? 1.0 : 0.0);
+    }
+    const Dual E(pl.E[ec], lane == 7 ? 1.0 : 0.0), th(pl.t[ec], lane == 6 ? 1.0 : 0.0);
+    PlateCoreT<Dual> C;
+    plate_core(xl, yl, E, Dual(pl.nu[ec]), th, Dual(pl.ks[ec]), C);
+    double phi = 0.0;
+    phi += plate_local_pair<0>(C, Sh, Kl, lane == 0);
+    phi += plate_local_pair<1>(C, Sh, Kl, lane == 1);
+    phi += plate_local_pair<2>(C, Sh, Kl, lane == 2);
+    phi += plate_local_pair<3>(C, Sh, Kl, lane == 3);
+    phi += plate_local_pair<4>(C, Sh, Kl, lane == 4);
+    phi += plate_local_pair<5>(C, Sh, Kl, lane == 5);
+    phi += plate_local_pair<6>(C, Sh, Kl, lane == 6);
+    phi += plate_local_pair<7>(C, Sh, Kl, lane == 7);
+    phi += plate_local_pair<8>(C, Sh, Kl, lane == 0);
+    phi += plate_local_pair<9>(C, Sh, Kl, lane == 1);
+    s_phi[grp][lane] = phi;
+  }
+  __syncthreads();
+
+  // 3. M = sum_k (K_l Sh)_kk: lane l takes the structural entries of blocks l and l + 8
+  {
+    double* M = s_m[grp][lane];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) M[k] = 0.0;
+#pragma unroll 1
+    for (int B = lane; B < 10; B += kPlateLanes) {
+      const int I = plate_pair_i(B), J = plate_pair_j(B), ne = I == J ? 14 : 13, off = plate_pair_off(B);
+#pragma unroll 1
+      for (int k = 0; k < ne; ++k) {
+        const int en = plate_en(k), r = en / 6, c = en % 6;
+        const double kv = Kl[off + k];
+        const int p = 2 * I + r / 3, q = 2 * J + c / 3, a = r % 3, cc = c % 3;
+        // K{p,q}[a][cc] = kv adds kv Sh{q,p}[cc][:] to row a
+#pragma unroll
+        for (int b = 0; b < 3; ++b) M[3 * a + b] = fma(kv, Sh[(3 * q + cc) * 24 + 3 * p + b], M[3 * a + b]);
+        // off-diagonal blocks: K{q,p}[cc][a] = kv adds kv Sh{p,q}[a][:] to row cc
+        if (I != J)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) M[3 * cc + b] = fma(kv, Sh[(3 * p + a) * 24 + 3 * q + b], M[3 * cc + b]);
+      }
+    }
+  }
+  __syncthreads();
+
+  // 4. rotation directions: lanes 0..5 = x, y, z of node 2, then of node 4 (lanes 6, 7 repeat lane 0)
+  {
+    const int dir = lane < 6 ? lane : 0;
+    const int node = dir < 3 ? 1 : 3, axis = dir % 3;
+    double Mt[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      double s = 0.0;
+#pragma unroll
+      for (int l = 0; l < kPlateLanes; ++l) s += s_m[grp][l][k];
+      Mt[k] = s;
+    }
+    const double* phi = s_phi[grp];
+    const int slot_of[3] = {0, 1, 3};
+    double H[6];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      double hx = 0.0, hy = 0.0;
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        hx = fma(phi[2 * s], dv[slot_of[s]][j], hx);
+        hy = fma(phi[2 * s + 1], dv[slot_of[s]][j], hy);
+      }
+      H[j] = hx;
+      H[3 + j] = hy;
+    }
+    Dual Xd[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Xd[k][c] = Dual(X[k + 1][c], (k + 1 == node && c == axis) ? 1.0 : 0.0);
+    Dual Rd[9];
+    if (!plate_rotation(Xd[0], Xd[1], Xd[2], abs_tol, Rd)) set_identity(Rd);
+    double r = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        // omega = dR R^T
+        const double om = (Rd[3 * a].d * R[3 * b] + Rd[3 * a + 1].d * R[3 * b + 1]) + Rd[3 * a + 2].d * R[3 * b + 2];
+        r = fma(om, Mt[3 * a + b], r);
+      }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) r = fma(H[j], Rd[j].d, fma(H[3 + j], Rd[3 + j].d, r));
+    s_rot[grp][lane] = r;
+  }
+  __syncthreads();
+
+  // 5. outputs: lane l writes entries l and l + 8 of (12 coordinates, E, t)
+  if (live) {
+    const double* phi = s_phi[grp];
+    const double* rot = s_rot[grp];
+#pragma unroll
+    for (int o = lane; o < 14; o += kPlateLanes) {
+      double v;
+      if (o >= 12) {
+        v = phi[o == 12 ? 7 : 6];
+        g_prop[e * 2 + (o - 12)] = -v;
+        continue;
+      }
+      const int node = o / 3, j = o % 3;
+      if (node == 2) {
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) s += phi[2 * q] * R[j] + phi[2 * q + 1] * R[3 + j];
+        v = -s - (rot[j] + rot[3 + j]);
+      } else {
+        const int slot = node == 3 ? 2 : node;
+        v = phi[2 * slot] * R[j] + phi[2 * slot + 1] * R[3 + j];
+        if (node == 1) v += rot[j];
+        if (node == 3) v += rot[3 + j];
+      }
+      g_coord[e * 12 + o] = -v;
+    }
+  }
 }
 
 // beams: directions 0..5 node coordinates, 6 E, 7 A, 8 I11, 9 I22, 10 It
@@ -355,7 +535,8 @@ int vjp_launch(fem_gpu* h, const double* d_u, const double* d_lam, int P) {
     CK(cudaFuncSetAttribute(k_vjp_w<24, 4, 6, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_vjp_w<24, 4, 6, 1><<<grid_for(h->np, 1), kVjpThreads, smem, s>>>(h->np, h->p_n1.p, h->p_n2.p, h->p_n3.p,
                                                                       h->p_n4.p, h->vjp_lT.p, h->vjp_uT.p, P, Wp);
-    k_vjp_plate<<<grid_for(h->np * kPlateDirs, 64), 64, 0, s>>>(h->np, nd, h->plates(), h->abs_tol, Wp, gcp, gpp);
+    k_vjp_plate<<<grid_for(h->np, kPlatesPerCta), kPlateLanes * kPlatesPerCta, 0, s>>>(h->np, nd, h->plates(),
+                                                                                       h->abs_tol, Wp, gcp, gpp);
   }
   CK(h->vjp_gxyz.reserve(h->n_nodes * 3 + 1, s));
   if (h->n_nodes)
