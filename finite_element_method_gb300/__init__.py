@@ -4,6 +4,6 @@ Rust crate `finite_element_method`, behind a C ABI (include/fem_gpu.h).
 `FEM` mirrors the crate's FEM::create / add_node / add_truss / add_beam /
 add_plate API; `meshes` generates the seeded synthetic workloads.
 """
-from .fem import FEM, Batch, FEMError  # noqa: F401
+from .fem import FEM, Batch, FEMError, SeparatedStiffnessSparse  # noqa: F401
 
-__all__ = ["FEM", "Batch", "FEMError"]
+__all__ = ["FEM", "Batch", "FEMError", "SeparatedStiffnessSparse"]

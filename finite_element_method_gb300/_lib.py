@@ -60,6 +60,12 @@ SIGNATURES = {
     "fem_gpu_batch_last_ms": (c_int, [hp, fp]),
     "fem_gpu_batch_autotune": (c_int, [hp, c_int, c_char_p, c_char_p, c_size_t]),
     "fem_gpu_batch_configure": (c_int, [hp, c_int, c_int, c_int, c_int, c_int, c_int, c_int]),
+    "fem_gpu_separate_sparse": (c_int, [hp, u8p]),
+    "fem_gpu_get_separation_sizes": (c_int, [hp, i64p, i64p, i64p]),
+    "fem_gpu_get_separation_indexes": (c_int, [hp, i64p, i64p]),
+    "fem_gpu_get_separation_block": (c_int, [hp, c_int, i64p, i32p, dp]),
+    "fem_gpu_get_separation_block_device": (c_int, [hp, c_int, POINTER(c_void_p), POINTER(c_void_p),
+                                                    POINTER(c_void_p)]),
     "fem_gpu_assemble_dense_noalloc": (c_int, [c_uint32, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p,
                                                c_void_p, c_size_t, c_void_p, c_void_p, c_double, c_double, c_void_p,
                                                c_void_p]),

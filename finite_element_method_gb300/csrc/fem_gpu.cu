@@ -1144,6 +1144,17 @@ struct fem_gpu {
   FlatTable p_sets;  // sorted node-number set hash -> element index
   DevBuf<int32_t> p_n1, p_n2, p_n3, p_n4;
   DevBuf<double> p_E, p_nu, p_t, p_ks;
+  // sparse separation (K_aa, K_ab, K_ba, K_bb)
+  bool sep_valid = false;
+  DevBuf<uint8_t> sep_imposed, sep_cls;
+  DevBuf<uint32_t> sep_u32;             // class flags, local positions, per-row counts
+  DevBuf<unsigned long long> sep_scan;  // per block: row starts by global row (n + 1 each)
+  DevBuf<unsigned long long> sep_err;
+  DevBuf<int64_t> sep_idx;              // a list, then b list
+  DevBuf<int64_t> sep_rp[4];
+  DevBuf<int32_t> sep_ci[4];
+  DevBuf<double> sep_v[4];
+  int64_t sep_n[2] = {0, 0}, sep_nnz[4] = {0, 0, 0, 0};
   // validation scratch
   DevBuf<int> vstatus;
   DevBuf<unsigned long long> vfirst;
@@ -1327,6 +1338,17 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   h->vjp_inc.release();
   h->vstatus.release();
   h->vfirst.release();
+  h->sep_imposed.release();
+  h->sep_cls.release();
+  h->sep_u32.release();
+  h->sep_scan.release();
+  h->sep_err.release();
+  h->sep_idx.release();
+  for (int b = 0; b < 4; ++b) {
+    h->sep_rp[b].release();
+    h->sep_ci[b].release();
+    h->sep_v[b].release();
+  }
   for (auto& ev : h->ev)
     if (ev) cudaEventDestroy(ev);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -1736,6 +1758,7 @@ int launch_elements(fem_gpu* h, BlockSink sink_t, BlockSink sink_b, BlockSink si
 }
 
 int numeric_launch(fem_gpu* h) {
+  h->sep_valid = false;  // a separation describes the stiffness it was taken from
   CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->stream));
   CK(cudaEventRecord(h->ev[0], h->stream));
   BlockSink st{nullptr, h->V.p, h->off_t.p, h->flag.p};
@@ -2231,3 +2254,5 @@ extern "C" int fem_gpu_last_numeric_timing(fem_gpu_t* h, float* element_ms, floa
 #include "fem_batch.cuh"
 // vector-Jacobian product (reuses the element arithmetic and the handle above)
 #include "fem_adjoint.cuh"
+// sparse separation of the assembled stiffness by the imposed displacements
+#include "fem_separate.cuh"

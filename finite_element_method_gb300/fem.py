@@ -28,6 +28,8 @@ import numpy as np
 from . import _lib
 from ._lib import ptr
 
+FEM_GPU_ERR_NODE_NOT_EXIST = 5
+FEM_GPU_ERR_ARGUMENT = 30
 FEM_GPU_ERR_CUDA = 40
 
 
@@ -269,6 +271,57 @@ class FEM:
                                         ptr(out["plate"], c_double), ptr(out["xyz"], c_double)))
         return out
 
+    # -- boundary conditions and sparse separation ---------------------------------
+    DOF_PARAMETERS = ("X", "Y", "Z", "ThX", "ThY", "ThZ")
+
+    def add_displacement(self, node_number: int, dof_parameter, value: float = 0.0) -> None:
+        """add_displacement (methods_for_bc_data_handle.rs:176-203): impose a displacement on one DOF."""
+        dof = dof_parameter if isinstance(dof_parameter, int) else self.DOF_PARAMETERS.index(dof_parameter)
+        index = self._node_index(node_number)
+        if index is None:
+            raise FEMError(FEM_GPU_ERR_NODE_NOT_EXIST, f"Node with number {node_number} does not exist!")
+        imp = self._imposed()
+        k = 6 * index + dof
+        if imp[k]:
+            raise FEMError(FEM_GPU_ERR_ARGUMENT,
+                           f"Displacement {self.DOF_PARAMETERS[dof]} already applied to node {node_number}!")
+        imp[k] = 1
+        self._displacements[k] = value
+
+    def _imposed(self):
+        if getattr(self, "_imposed_arr", None) is None:
+            self._imposed_arr = np.zeros(6 * self.nodes_number, np.uint8)
+            self._displacements = np.zeros(6 * self.nodes_number)
+        return self._imposed_arr
+
+    def _node_index(self, number):
+        numbers = self.index_node_numbers()
+        hit = np.flatnonzero(numbers == number)
+        return int(hit[0]) if hit.size else None
+
+    def separate_stiffness_matrix_sparse_iterative(self, imposed=None) -> "SeparatedStiffnessSparse":
+        """separate_stiffness_matrix_sparse_iterative (methods_for_separate_stiffness_matrix.rs:217-320) on the
+        GPU: the imposed displacements (from add_displacement, or `imposed`, 6 * nodes_number flags) split the
+        assembled stiffness into K_aa, K_ab, K_ba, K_bb, each a CSR matrix sorted by (row, column)."""
+        imp = self._imposed() if imposed is None else np.ascontiguousarray(imposed, dtype=np.uint8)
+        assert imp.shape == (6 * self.nodes_number,)
+        self._check(self._L.fem_gpu_separate_sparse(self._h, ptr(imp, c_uint8)))
+        n_aa, n_bb, nnz = c_int64(0), c_int64(0), (c_int64 * 4)()
+        self._check(self._L.fem_gpu_get_separation_sizes(self._h, ctypes.byref(n_aa), ctypes.byref(n_bb), nnz))
+        aa = np.zeros(n_aa.value, np.int64)
+        bb = np.zeros(n_bb.value, np.int64)
+        self._check(self._L.fem_gpu_get_separation_indexes(self._h, ptr(aa, c_int64), ptr(bb, c_int64)))
+        blocks = {}
+        for which, name in enumerate(SeparatedStiffnessSparse.BLOCKS):
+            rows = n_aa.value if which < 2 else n_bb.value
+            rp = np.zeros(rows + 1, np.int64)
+            ci = np.zeros(nnz[which], np.int32)
+            va = np.zeros(nnz[which], np.float64)
+            self._check(self._L.fem_gpu_get_separation_block(self._h, which, ptr(rp, c_int64), ptr(ci, c_int32),
+                                                             ptr(va, c_double)))
+            blocks[name] = (rp, ci, va)
+        return SeparatedStiffnessSparse(aa, bb, blocks)
+
     def vjp_last_ms(self) -> float:
         x = c_float(0)
         self._check(self._L.fem_gpu_vjp_last_ms(self._h, ctypes.byref(x)))
@@ -279,6 +332,21 @@ class FEM:
         a, b = c_float(0), c_float(0)
         self._check(self._L.fem_gpu_last_numeric_timing(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+
+class SeparatedStiffnessSparse:
+    """SeparatedStiffnessMatrixSparse (structs/separated_stiffness_matrix_sparse.rs): the free (a) and restrained (b)
+    DOF index lists and the four blocks as CSR (row_ptr, col_idx, values) with local indices."""
+    BLOCKS = ("k_aa", "k_ab", "k_ba", "k_bb")
+
+    def __init__(self, k_aa_indexes, k_bb_indexes, blocks):
+        self.k_aa_indexes, self.k_bb_indexes, self.blocks = k_aa_indexes, k_bb_indexes, blocks
+        self.n_aa, self.n_bb = len(k_aa_indexes), len(k_bb_indexes)
+
+    def triplets(self, name):
+        """the block as (row, column, value) arrays, row-major order"""
+        rp, ci, va = self.blocks[name]
+        return np.repeat(np.arange(len(rp) - 1), np.diff(rp)), ci.astype(np.int64), va
 
 
 class Batch:

@@ -62,6 +62,9 @@ enum {
   FEM_GPU_ERR_NOT_ON_PLANE = 19,
   FEM_GPU_ERR_NOT_CONVEX = 20,
   FEM_GPU_ERR_ZERO_LENGTH = 21,    /* two-node element whose nodes coincide */
+  FEM_GPU_ERR_SEP_DISPLACEMENT = 22, /* "There are no stiffness to withstand displacement D applied to node N!" */
+  FEM_GPU_ERR_SEP_NO_RESTRAINTS = 23, /* "No restraints" */
+  FEM_GPU_ERR_SEP_EMPTY_KAA = 24,  /* "Sparse separation: K_aa is empty (structure has no free stiffness?)" */
   FEM_GPU_ERR_ARGUMENT = 30,       /* null pointer / size out of range */
   FEM_GPU_ERR_STATE = 31,          /* e.g. CSR requested before fem_gpu_assemble */
   FEM_GPU_ERR_CUDA = 40,           /* CUDA runtime failure or no device */
@@ -200,6 +203,28 @@ int fem_gpu_batch_autotune(fem_gpu_batch_t* b, int reps, const char* cache_path,
 /* apply a configuration read back from that table */
 int fem_gpu_batch_configure(fem_gpu_batch_t* b, int persistent, int block, int ctas_per_sm, int tile_truss,
                             int tile_beam, int tile_plate, int sum_block);
+
+/* ---- sparse separation ----------------------------------------------------
+ * separate_stiffness_matrix_sparse_iterative (methods_for_separate_stiffness_
+ * matrix.rs:217-320) of the assembled stiffness.  imposed: 6 * nodes_number
+ * bytes, non-zero where a displacement is imposed (the reference's
+ * imposed_constraints, set by add_displacement).  DOFs in ascending order:
+ * diagonal 0 -> excluded (FEM_GPU_ERR_SEP_DISPLACEMENT if a displacement is
+ * imposed on it), else restrained (b, imposed) or free (a).  Every non-zero
+ * K(i, j) with both DOFs kept goes to K_aa, K_ab, K_ba or K_bb (which = 0..3)
+ * with local row / column indices; each block is CSR sorted by (row, column),
+ * the reference's triplets in a fixed order.  FEM_GPU_ERR_SEP_NO_RESTRAINTS
+ * without restrained DOFs, FEM_GPU_ERR_SEP_EMPTY_KAA when K_aa has no entry.
+ * The blocks stay on the device with the handle until the next numeric pass. */
+int fem_gpu_separate_sparse(fem_gpu_t* h, const uint8_t* imposed);
+/* number of free and restrained DOFs, and nnz of K_aa, K_ab, K_ba, K_bb (nnz4[4]) */
+int fem_gpu_get_separation_sizes(fem_gpu_t* h, int64_t* n_aa, int64_t* n_bb, int64_t* nnz4);
+/* the DOF indexes of the a and b lists (host arrays of n_aa and n_bb) */
+int fem_gpu_get_separation_indexes(fem_gpu_t* h, int64_t* aa_indexes, int64_t* bb_indexes);
+/* block `which` (0 K_aa, 1 K_ab, 2 K_ba, 3 K_bb) to host arrays (rows + 1, nnz, nnz) or as device pointers */
+int fem_gpu_get_separation_block(fem_gpu_t* h, int which, int64_t* row_ptr, int32_t* col_idx, double* values);
+int fem_gpu_get_separation_block_device(fem_gpu_t* h, int which, const int64_t** row_ptr, const int32_t** col_idx,
+                                        const double** values);
 
 /* Dense assembly of one small structure without any device allocation.
  * No counterpart in the reference: it serves callers that cannot call
