@@ -4,17 +4,18 @@
 // For (u_p, lambda_p), p < P, the gradient of F = -sum_p lambda_p^T K u_p with
 // respect to every element property theta_e and nodal coordinate is
 //     dF/dtheta = -<dK_e/dtheta, W_e>,   W_e = sum_p lambda_{p,e} u_{p,e}^T,
-// where lambda_{p,e}, u_{p,e} are the element's DOF slices (global axes).
+// where lambda_{p,e}, u_{p,e} are the element's DOF slices (global axes).  K_e
+// is symmetric, so only Ws = W + W^T matters, and Ws restricted to an element
+// is a set of global node-pair blocks: Ws(I, J) = sum_p (lambda_I u_J^T +
+// u_I lambda_J^T), shared by every element that couples nodes I and J.
 //   1. u and lambda are transposed to DOF-major (pairs contiguous per DOF);
-//   2. W_e is formed per element in shared memory (a small P-deep product);
-//   3. one thread per (element, parameter) recomputes the element matrix in
-//      forward-mode dual arithmetic seeded on that parameter -- the element
-//      matrices are recomputed, never stored -- and contracts dK_e/dtheta with
-//      W_e on the fly;
+//   2. Ws is formed once per block of the stiffness pattern (a sampled
+//      dense-dense product: 36 entries x 2P fused multiply-adds per block);
+//   3. the element kernels recompute their element matrices in forward-mode
+//      dual arithmetic -- recomputed, never stored -- and contract the
+//      derivatives with their blocks of Ws;
 //   4. coordinate contributions are summed per node in a fixed (element) order.
 // Parameters: truss E, A, A2; beam E, A, I11, I22, It; plate E, t; nodes x, y, z.
-
-constexpr int kVjpThreads = 128;
 
 // [P][N] -> [N][P] through 32 x 32 shared tiles
 __global__ void k_transpose_pairs(const double* __restrict__ in, size_t P, size_t N, double* __restrict__ out) {
@@ -31,58 +32,75 @@ __global__ void k_transpose_pairs(const double* __restrict__ in, size_t P, size_
   }
 }
 
-// W_e for EPB elements per CTA: ND DOFs per element (NN nodes x NDN DOFs of each node's 6).
-template <int ND, int NN, int NDN, int EPB>
-__global__ void __launch_bounds__(kVjpThreads) k_vjp_w(size_t n_el, const int32_t* __restrict__ n1,
-                                                       const int32_t* __restrict__ n2, const int32_t* __restrict__ n3,
-                                                       const int32_t* __restrict__ n4, const double* __restrict__ lamT,
-                                                       const double* __restrict__ uT, int P, double* __restrict__ W) {
-  extern __shared__ double s_lu[];  // [EPB][2][P][ND]
-  const size_t e0 = (size_t)blockIdx.x * EPB;
-  const int nloc = (int)min((size_t)EPB, n_el - e0);
-  const int32_t* nd[4] = {n1, n2, n3, n4};
-  // gather the element DOF slices of lambda and u: (element, array, node, dof, pair), pair fastest
-  const int per_el = 2 * NN * NDN * P;
-  for (int t = threadIdx.x; t < nloc * per_el; t += blockDim.x) {
-    const int el = t / per_el;
-    int r = t - el * per_el;
-    const int arr = r / (NN * NDN * P);
-    r -= arr * NN * NDN * P;
-    const int k = r / (NDN * P);
-    r -= k * NDN * P;
-    const int a = r / P, p = r - a * P;
-    const size_t node = (size_t)nd[k][e0 + el];
-    const double* src = arr == 0 ? lamT : uT;
-    s_lu[(((size_t)el * 2 + arr) * P + p) * ND + k * NDN + a] = src[(6 * node + a) * (size_t)P + p];
+// the stiffness block of every element node pair: the block whose sorted range holds the pair's slot
+__global__ void k_pair_blocks(size_t n, const uint32_t* __restrict__ slot, const uint32_t* __restrict__ blk_start,
+                              size_t n_blocks, uint32_t* __restrict__ pblk) {
+  const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t s = slot[k];
+  size_t lo = 0, hi = n_blocks;  // last block with blk_start <= s
+  while (hi - lo > 1) {
+    const size_t mid = (lo + hi) >> 1;
+    if (blk_start[mid] <= s) lo = mid;
+    else hi = mid;
   }
-  __syncthreads();
-  for (int t = threadIdx.x; t < nloc * ND * ND; t += blockDim.x) {
-    const int el = t / (ND * ND);
-    const int ij = t - el * ND * ND;
-    const int i = ij / ND, j = ij - i * ND;
-    const double* L = s_lu + (size_t)el * 2 * P * ND;
-    const double* U = L + (size_t)P * ND;
-    double acc = 0.0;
-    for (int p = 0; p < P; ++p) acc = fma(L[p * ND + i], U[p * ND + j], acc);
-    W[(e0 + el) * (size_t)(ND * ND) + ij] = acc;
-  }
+  pblk[k] = (uint32_t)lo;
 }
 
-// <dK/dtheta, W> of one node-pair block (element orientation), both (i, j) and (j, i)
-template <int ND>
-__device__ __forceinline__ double contract_pair(const Dual blk[36], int i0, int j0, bool diag,
-                                                const double* __restrict__ W) {
+// Ws(I, J) for every pattern block, one thread per entry (a, c), rows the DOFs of I = blk_I <= J = blk_J:
+//   Ws[b][6a + c] = sum_p lambda[6I + a][p] u[6J + c][p] + u[6I + a][p] lambda[6J + c][p]
+constexpr int kWsBlocksPerCta = 8;
+__global__ void __launch_bounds__(36 * kWsBlocksPerCta) k_vjp_ws(size_t n_blocks, const int32_t* __restrict__ blk_I,
+                                                                 const int32_t* __restrict__ blk_J,
+                                                                 const double* __restrict__ lamT,
+                                                                 const double* __restrict__ uT, int P,
+                                                                 double* __restrict__ Ws) {
+  const size_t b = (size_t)blockIdx.x * kWsBlocksPerCta + threadIdx.x / 36;
+  if (b >= n_blocks) return;
+  const int ac = threadIdx.x % 36, a = ac / 6, c = ac % 6;
+  const size_t I = (size_t)blk_I[b], J = (size_t)blk_J[b];
+  const double* li = lamT + (6 * I + a) * (size_t)P;
+  const double* ui = uT + (6 * I + a) * (size_t)P;
+  const double* lj = lamT + (6 * J + c) * (size_t)P;
+  const double* uj = uT + (6 * J + c) * (size_t)P;
+  double acc0 = 0.0, acc1 = 0.0;
+  int p = 0;
+  if ((P & 1) == 0) {  // rows start 16-byte aligned when P is even
+    for (; p < P; p += 2) {
+      const double2 l2 = __ldg(reinterpret_cast<const double2*>(li + p));
+      const double2 u2 = __ldg(reinterpret_cast<const double2*>(ui + p));
+      const double2 m2 = __ldg(reinterpret_cast<const double2*>(lj + p));
+      const double2 v2 = __ldg(reinterpret_cast<const double2*>(uj + p));
+      acc0 = fma(l2.x, v2.x, acc0);
+      acc1 = fma(u2.x, m2.x, acc1);
+      acc0 = fma(l2.y, v2.y, acc0);
+      acc1 = fma(u2.y, m2.y, acc1);
+    }
+  } else {
+    for (; p < P; ++p) {
+      acc0 = fma(li[p], uj[p], acc0);
+      acc1 = fma(ui[p], lj[p], acc1);
+    }
+  }
+  Ws[b * 36 + ac] = acc0 + acc1;
+}
+
+// entry (a, c) of Ws between DOF a of global node gi and DOF c of global node gj, from the stored block
+// (rows = the lower node index); Ws is symmetric, so the other orientation is the transpose
+__device__ __forceinline__ double ws_at(const double* __restrict__ blk, int32_t gi, int32_t gj, int a, int c) {
+  return gi <= gj ? blk[6 * a + c] : blk[6 * c + a];
+}
+
+// <dK/dtheta, W> of one node-pair block (element orientation, element nodes gi, gj): sum d Ws over the
+// block, halved on the diagonal (there d is symmetric and Ws counts both orientations)
+__device__ __forceinline__ double contract_ws(const Dual blk[36], const double* __restrict__ ws, int32_t gi,
+                                              int32_t gj, bool diag) {
   double acc = 0.0;
 #pragma unroll
   for (int a = 0; a < 6; ++a)
 #pragma unroll
-    for (int b = 0; b < 6; ++b) {
-      const double d = blk[6 * a + b].d;
-      double w = W[(i0 + a) * ND + j0 + b];
-      if (!diag) w += W[(j0 + b) * ND + i0 + a];
-      acc = fma(d, w, acc);
-    }
-  return acc;
+    for (int c = 0; c < 6; ++c) acc = fma(blk[6 * a + c].d, ws_at(ws, gi, gj, a, c), acc);
+  return diag ? 0.5 * acc : acc;
 }
 
 __device__ __forceinline__ void seed3(Dual x[3], const double* v, int base, int dir) {
@@ -143,7 +161,8 @@ __device__ __forceinline__ double plate_local_pair(const PlateCoreT<Dual>& C, co
 }
 
 __global__ void __launch_bounds__(kPlateLanes* kPlatesPerCta) k_vjp_plate(size_t n_el, NodesView nd, PlateView pl,
-                                                                          double abs_tol, const double* __restrict__ W,
+                                                                          double abs_tol, const double* __restrict__ Ws,
+                                                                          const uint32_t* __restrict__ pblk,
                                                                           double* __restrict__ g_coord,
                                                                           double* __restrict__ g_prop) {
   __shared__ double s_sh[kPlatesPerCta][576];
@@ -157,7 +176,6 @@ __global__ void __launch_bounds__(kPlateLanes* kPlatesPerCta) k_vjp_plate(size_t
   const size_t ec = live ? e : n_el - 1;  // tail groups recompute the last plate and store nothing
   double* Sh = s_sh[grp];
   double* Kl = s_kl[grp];
-  const double* We = W + ec * 576;
 
   // geometry (values): R with the forward kernel's identity fast path, local coordinates
   const int nidx[4] = {pl.n1[ec], pl.n2[ec], pl.n3[ec], pl.n4[ec]};
@@ -176,16 +194,18 @@ __global__ void __launch_bounds__(kPlateLanes* kPlatesPerCta) k_vjp_plate(size_t
     ylv[i] = (R[3] * dv[i][0] + R[4] * dv[i][1]) + R[5] * dv[i][2];
   }
 
-  // 1. Sh = R (W + W^T) R^T by 3x3 sub-blocks; lane p fills sub-block row p
+  // 1. Sh = R Ws R^T by 3x3 sub-blocks, Ws from the element's stiffness blocks; lane p fills sub-block row p
   {
     const int p = lane;
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) {
+      const int ie = p / 2, je = q / 2;
+      const double* wb = Ws + (size_t)pblk[ec * 10 + (ie <= je ? ut4(ie, je) : ut4(je, ie))] * 36;
       double ws[9];
 #pragma unroll
       for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int b = 0; b < 3; ++b) ws[3 * a + b] = We[(3 * p + a) * 24 + 3 * q + b] + We[(3 * q + b) * 24 + 3 * p + a];
+        for (int b = 0; b < 3; ++b) ws[3 * a + b] = ws_at(wb, nidx[ie], nidx[je], 3 * (p % 2) + a, 3 * (q % 2) + b);
       if (!ident) {
         double t[9];
 #pragma unroll
@@ -337,15 +357,17 @@ __global__ void __launch_bounds__(kPlateLanes* kPlatesPerCta) k_vjp_plate(size_t
 // beams: directions 0..5 node coordinates, 6 E, 7 A, 8 I11, 9 I22, 10 It
 constexpr int kBeamDirs = 11;
 __global__ void __launch_bounds__(128) k_vjp_beam(size_t n_el, NodesView nd, BeamView b, double rel_tol,
-                                                  double abs_tol, const double* __restrict__ W,
-                                                  double* __restrict__ g_coord, double* __restrict__ g_prop) {
+                                                  double abs_tol, const double* __restrict__ Ws,
+                                                  const uint32_t* __restrict__ pblk, double* __restrict__ g_coord,
+                                                  double* __restrict__ g_prop) {
   const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (t >= n_el * kBeamDirs) return;
   const size_t e = t / kBeamDirs;
   const int dir = (int)(t - e * kBeamDirs);
+  const int32_t g1 = b.n1[e], g2 = b.n2[e];
   double v1[3], v2[3];
-  nd.get(b.n1[e], v1);
-  nd.get(b.n2[e], v2);
+  nd.get(g1, v1);
+  nd.get(g2, v2);
   Dual x1[3], x2[3];
   seed3(x1, v1, 0, dir);
   seed3(x2, v2, 3, dir);
@@ -358,7 +380,9 @@ __global__ void __launch_bounds__(128) k_vjp_beam(size_t n_el, NodesView nd, Bea
     else g_prop[e * 5 + (dir - 6)] = 0.0;
     return;
   }
-  const double* We = W + e * 144;
+  const double* w11 = Ws + (size_t)pblk[e * 3 + 0] * 36;
+  const double* w12 = Ws + (size_t)pblk[e * 3 + 1] * 36;
+  const double* w22 = Ws + (size_t)pblk[e * 3 + 2] * 36;
   Dual blk[36];
   double s = 0.0;
   // node block (1,1): [uu ut; ut^T th]
@@ -371,7 +395,7 @@ __global__ void __launch_bounds__(128) k_vjp_beam(size_t n_el, NodesView nd, Bea
       blk[6 * (3 + a) + c] = B.ut[3 * c + a];
       blk[6 * (3 + a) + 3 + c] = B.th[3 * a + c];
     }
-  s += contract_pair<12>(blk, 0, 0, true, We);
+  s += contract_ws(blk, w11, g1, g1, true);
   // node block (1,2): [-uu ut; tu thth2]
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -382,7 +406,7 @@ __global__ void __launch_bounds__(128) k_vjp_beam(size_t n_el, NodesView nd, Bea
       blk[6 * (3 + a) + c] = B.tu[3 * a + c];
       blk[6 * (3 + a) + 3 + c] = B.thth2[3 * a + c];
     }
-  s += contract_pair<12>(blk, 0, 6, false, We);
+  s += contract_ws(blk, w12, g1, g2, false);
   // node block (2,2): [uu -ut; -ut^T th]
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -393,7 +417,7 @@ __global__ void __launch_bounds__(128) k_vjp_beam(size_t n_el, NodesView nd, Bea
       blk[6 * (3 + a) + c] = -B.ut[3 * c + a];
       blk[6 * (3 + a) + 3 + c] = B.th[3 * a + c];
     }
-  s += contract_pair<12>(blk, 6, 6, true, We);
+  s += contract_ws(blk, w22, g2, g2, true);
   if (dir < 6) g_coord[e * 6 + dir] = -s;
   else g_prop[e * 5 + (dir - 6)] = -s;
 }
@@ -401,29 +425,32 @@ __global__ void __launch_bounds__(128) k_vjp_beam(size_t n_el, NodesView nd, Bea
 // trusses (3 DOFs per node): directions 0..5 node coordinates, 6 E, 7 A, 8 A2
 constexpr int kTrussDirs = 9;
 __global__ void __launch_bounds__(128) k_vjp_truss(size_t n_el, NodesView nd, TrussView tv, double abs_tol,
-                                                   const double* __restrict__ W, double* __restrict__ g_coord,
-                                                   double* __restrict__ g_prop) {
+                                                   const double* __restrict__ Ws, const uint32_t* __restrict__ pblk,
+                                                   double* __restrict__ g_coord, double* __restrict__ g_prop) {
   const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (t >= n_el * kTrussDirs) return;
   const size_t e = t / kTrussDirs;
   const int dir = (int)(t - e * kTrussDirs);
+  const int32_t g1 = tv.n1[e], g2 = tv.n2[e];
   double v1[3], v2[3];
-  nd.get(tv.n1[e], v1);
-  nd.get(tv.n2[e], v2);
+  nd.get(g1, v1);
+  nd.get(g2, v2);
   Dual x1[3], x2[3], g[9];
   seed3(x1, v1, 0, dir);
   seed3(x2, v2, 3, dir);
   double s = 0.0;
   if (truss_block(x1, x2, Dual(tv.E[e], dir == 6 ? 1.0 : 0.0), Dual(tv.A[e], dir == 7 ? 1.0 : 0.0),
                   Dual(tv.A2[e], dir == 8 ? 1.0 : 0.0), abs_tol, g)) {
-    const double* We = W + e * 36;
-    // blocks (1,1) = g, (1,2) = (2,1) = -g, (2,2) = g over 3 DOFs per node
+    const double* w11 = Ws + (size_t)pblk[e * 3 + 0] * 36;
+    const double* w12 = Ws + (size_t)pblk[e * 3 + 1] * 36;
+    const double* w22 = Ws + (size_t)pblk[e * 3 + 2] * 36;
+    // translational blocks (1,1) = g, (1,2) = (2,1)^T = -g, (2,2) = g; diagonal blocks count Ws at one half
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const double d = g[3 * a + c].d;
-        const double w = We[a * 6 + c] + We[(3 + a) * 6 + 3 + c] - We[a * 6 + 3 + c] - We[(3 + a) * 6 + c];
+        const double w = 0.5 * (w11[6 * a + c] + w22[6 * a + c]) - ws_at(w12, g1, g2, a, c);
         s = fma(d, w, s);
       }
   }
@@ -500,14 +527,24 @@ int vjp_launch(fem_gpu* h, const double* d_u, const double* d_lam, int P) {
   const dim3 tb(32, 8), tg((unsigned)((N + 31) / 32), (unsigned)((P + 31) / 32));
   k_transpose_pairs<<<tg, tb, 0, s>>>(d_u, (size_t)P, N, h->vjp_uT.p);
   k_transpose_pairs<<<tg, tb, 0, s>>>(d_lam, (size_t)P, N, h->vjp_lT.p);
-  const size_t wt = h->nt * 36, wb = h->nbm * 144, wp = h->np * 576;
-  CK(h->vjp_W.reserve(wt + wb + wp + 1, s));
+  // Ws per stiffness block, and the block of every element node pair
+  const size_t nb = h->n_blocks;
+  CK(h->vjp_Ws.reserve(nb * 36 + 1, s));
+  if (nb)
+    k_vjp_ws<<<grid_for(nb, kWsBlocksPerCta), 36 * kWsBlocksPerCta, 0, s>>>(nb, h->blk_I.p, h->blk_J.p, h->vjp_lT.p,
+                                                                          h->vjp_uT.p, P, h->vjp_Ws.p);
+  const size_t pt = h->nt * kPairs2, pb = h->nbm * kPairs2, pp = h->np * kPairs4;
+  CK(h->vjp_pblk.reserve(pt + pb + pp + 1, s));
+  uint32_t* bt = h->vjp_pblk.p;
+  uint32_t* bb = bt + pt;
+  uint32_t* bp = bb + pb;
+  if (pt) k_pair_blocks<<<grid_for(pt, 256), 256, 0, s>>>(pt, h->slot_t.p, h->blk_start.p, nb, bt);
+  if (pb) k_pair_blocks<<<grid_for(pb, 256), 256, 0, s>>>(pb, h->slot_b.p, h->blk_start.p, nb, bb);
+  if (pp) k_pair_blocks<<<grid_for(pp, 256), 256, 0, s>>>(pp, h->slot_p.p, h->blk_start.p, nb, bp);
   const size_t ct = h->nt * 6, cb = h->nbm * 6, cp = h->np * 12;
   CK(h->vjp_gc.reserve(ct + cb + cp + 1, s));
   CK(h->vjp_gp.reserve(h->nt * 3 + h->nbm * 5 + h->np * 2 + 1, s));
-  double* Wt = h->vjp_W.p;
-  double* Wb = Wt + wt;
-  double* Wp = Wb + wb;
+  const double* Ws = h->vjp_Ws.p;
   double* gct = h->vjp_gc.p;
   double* gcb = gct + ct;
   double* gcp = gcb + cb;
@@ -515,29 +552,15 @@ int vjp_launch(fem_gpu* h, const double* d_u, const double* d_lam, int P) {
   double* gpb = gpt + h->nt * 3;
   double* gpp = gpb + h->nbm * 5;
   const NodesView nd = h->nodes();
-  if (h->nt) {
-    const size_t smem = (size_t)4 * 2 * P * 6 * sizeof(double);
-    CK(cudaFuncSetAttribute(k_vjp_w<6, 2, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_vjp_w<6, 2, 3, 4><<<grid_for(h->nt, 4), kVjpThreads, smem, s>>>(h->nt, h->t_n1.p, h->t_n2.p, nullptr, nullptr,
-                                                                     h->vjp_lT.p, h->vjp_uT.p, P, Wt);
-    k_vjp_truss<<<grid_for(h->nt * kTrussDirs, 128), 128, 0, s>>>(h->nt, nd, h->trusses(), h->abs_tol, Wt, gct, gpt);
-  }
-  if (h->nbm) {
-    const size_t smem = (size_t)2 * 2 * P * 12 * sizeof(double);
-    CK(cudaFuncSetAttribute(k_vjp_w<12, 2, 6, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_vjp_w<12, 2, 6, 2><<<grid_for(h->nbm, 2), kVjpThreads, smem, s>>>(h->nbm, h->b_n1.p, h->b_n2.p, nullptr,
-                                                                       nullptr, h->vjp_lT.p, h->vjp_uT.p, P, Wb);
-    k_vjp_beam<<<grid_for(h->nbm * kBeamDirs, 128), 128, 0, s>>>(h->nbm, nd, h->beams(), h->rel_tol, h->abs_tol, Wb,
-                                                                  gcb, gpb);
-  }
-  if (h->np) {
-    const size_t smem = (size_t)1 * 2 * P * 24 * sizeof(double);
-    CK(cudaFuncSetAttribute(k_vjp_w<24, 4, 6, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_vjp_w<24, 4, 6, 1><<<grid_for(h->np, 1), kVjpThreads, smem, s>>>(h->np, h->p_n1.p, h->p_n2.p, h->p_n3.p,
-                                                                      h->p_n4.p, h->vjp_lT.p, h->vjp_uT.p, P, Wp);
+  if (h->nt)
+    k_vjp_truss<<<grid_for(h->nt * kTrussDirs, 128), 128, 0, s>>>(h->nt, nd, h->trusses(), h->abs_tol, Ws, bt, gct,
+                                                                   gpt);
+  if (h->nbm)
+    k_vjp_beam<<<grid_for(h->nbm * kBeamDirs, 128), 128, 0, s>>>(h->nbm, nd, h->beams(), h->rel_tol, h->abs_tol, Ws,
+                                                                  bb, gcb, gpb);
+  if (h->np)
     k_vjp_plate<<<grid_for(h->np, kPlatesPerCta), kPlateLanes * kPlatesPerCta, 0, s>>>(h->np, nd, h->plates(),
-                                                                                       h->abs_tol, Wp, gcp, gpp);
-  }
+                                                                                       h->abs_tol, Ws, bp, gcp, gpp);
   CK(h->vjp_gxyz.reserve(h->n_nodes * 3 + 1, s));
   if (h->n_nodes)
     k_vjp_nodes<<<grid_for(h->n_nodes, 256), 256, 0, s>>>(h->n_nodes, h->vjp_inc_off.p, h->vjp_inc.p, h->vjp_gc.p,
@@ -553,6 +576,7 @@ extern "C" int fem_gpu_vjp(fem_gpu_t* h, const double* u, const double* lam, int
   if (!h || !u || !lam || npairs < 1 || npairs > 512) return FEM_GPU_ERR_ARGUMENT;
   int st = ensure_ready(h);
   if (st) return st;
+  if (!h->pattern_valid) return h->fail(FEM_GPU_ERR_STATE, "call fem_gpu_assemble first");
   st = vjp_incidence(h);
   if (st) return st;
   const size_t N = (size_t)h->nodes_number * 6, P = (size_t)npairs;

@@ -1192,7 +1192,8 @@ struct fem_gpu {
   // vector-Jacobian product
   bool vjp_inc_valid = false;
   DevBuf<int64_t> vjp_inc_off, vjp_inc;
-  DevBuf<double> vjp_in, vjp_uT, vjp_lT, vjp_W, vjp_gc, vjp_gp, vjp_gxyz;
+  DevBuf<double> vjp_in, vjp_uT, vjp_lT, vjp_Ws, vjp_gc, vjp_gp, vjp_gxyz;
+  DevBuf<uint32_t> vjp_pblk;  // stiffness block of every element node pair
   float t_vjp_ms = 0;
 
   int fail(int code, const char* fmt, ...) {
@@ -1332,7 +1333,8 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   h->g_kind.release();
   h->flag.release();
   h->cub_tmp.release();
-  for (DevBuf<double>* v : {&h->vjp_in, &h->vjp_uT, &h->vjp_lT, &h->vjp_W, &h->vjp_gc, &h->vjp_gp, &h->vjp_gxyz})
+  h->vjp_pblk.release();
+  for (DevBuf<double>* v : {&h->vjp_in, &h->vjp_uT, &h->vjp_lT, &h->vjp_Ws, &h->vjp_gc, &h->vjp_gp, &h->vjp_gxyz})
     v->release();
   h->vjp_inc_off.release();
   h->vjp_inc.release();
