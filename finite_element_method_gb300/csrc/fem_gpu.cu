@@ -24,6 +24,7 @@
 #include <string>
 #include <unordered_map>
 #include <unordered_set>
+#include <thread>
 #include <vector>
 
 #include "../../include/fem_gpu.h"
@@ -975,13 +976,36 @@ uint64_t mix64(uint64_t x) {
   return x;
 }
 
+// A std::vector whose resize leaves new elements default-initialised (no zero fill), so that the
+// first touch of a large host array happens in the threads that write it.
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = NoInitAlloc<U>;
+  };
+  NoInitAlloc() = default;
+  template <class U>
+  NoInitAlloc(const NoInitAlloc<U>&) {}
+  template <class U>
+  void construct(U* p) noexcept {
+    ::new ((void*)p) U;
+  }
+  template <class U, class... A>
+  void construct(U* p, A&&... a) {
+    ::new ((void*)p) U(std::forward<A>(a)...);
+  }
+};
+template <class T>
+using HostVec = std::vector<T, NoInitAlloc<T>>;
+
 // Open-addressing table of (64-bit key, value) with linear probing and
 // backward-shift deletion; several entries may share a key (the caller's
 // predicate tells them apart), so it serves as map, set and multimap.  The
 // registries behind add_node / add_* (duplicate numbers, node pairs, plate
 // node sets, exact coordinates) hold one entry per node or element.  Key and
 // value share a 16-byte slot (one cache line touch per probe), the load stays
-// at most 1/2, and bulk callers prefetch the home slot of an entry a few
+// at most 5/8, and bulk callers prefetch the home slot of an entry a few
 // iterations ahead.
 class FlatTable {
  public:
@@ -1000,7 +1024,7 @@ class FlatTable {
   }
   void prefetch(uint64_t key) const { __builtin_prefetch(&slot_[mix64(key) & mask_]); }
   void insert(uint64_t key, int64_t v) {
-    if (2 * (len_ + 1) > slot_.size()) rehash(slot_.size());
+    if (8 * (len_ + 1) > 5 * slot_.size()) rehash(slot_.size());
     put(key, v);
   }
   void erase(uint64_t key, int64_t v) {
@@ -1022,9 +1046,13 @@ class FlatTable {
     --len_;
   }
   void reserve(size_t n) {
-    if (2 * n > slot_.size()) rehash(n);
+    if (8 * n > 5 * slot_.size()) rehash(n);
   }
-  size_t size() const { return len_; }
+  template <class F>
+  void for_each(F f) const {
+    for (const Slot& s : slot_)
+      if (s.val >= 0) f(s.key, s.val);
+  }
 
  private:
   struct Slot {
@@ -1033,7 +1061,7 @@ class FlatTable {
   };
   void init(size_t n) {
     size_t c = 64;
-    while (c < 2 * n) c <<= 1;
+    while (5 * c < 8 * n) c <<= 1;
     slot_.assign(c, Slot{0, -1});
     mask_ = c - 1;
     len_ = 0;
@@ -1055,6 +1083,49 @@ class FlatTable {
   size_t mask_ = 0, len_ = 0;
 };
 
+// A registry split into kRegParts FlatTables by the top bits of its key's hash
+// (the tables' slots use the low bits), so that host threads can check and
+// insert the keys of different partitions at the same time.
+constexpr int kRegParts = 16;
+inline int reg_part(uint64_t key) { return (int)(mix64(key) >> 60); }
+
+class PartTable {
+ public:
+  template <class Eq>
+  int64_t find(uint64_t key, Eq eq) const {
+    return part_[reg_part(key)].t.find(key, eq);
+  }
+  int64_t find(uint64_t key) const { return part_[reg_part(key)].t.find(key); }
+  void prefetch(uint64_t key) const { part_[reg_part(key)].t.prefetch(key); }
+  void insert(uint64_t key, int64_t v) { part_[reg_part(key)].t.insert(key, v); }
+  void erase(uint64_t key, int64_t v) { part_[reg_part(key)].t.erase(key, v); }
+  template <class F>
+  void for_each(F f) const {
+    for (const Part& p : part_) p.t.for_each(f);
+  }
+  // room for n entries spread over the partitions (a partition holds about n / kRegParts of them, within a
+  // few percent for n in the thousands and up); large tables are set up by several threads
+  void reserve(size_t n) {
+    const size_t per = n / kRegParts + n / (32 * kRegParts) + 256;
+    if (n < (size_t(1) << 16)) {
+      for (Part& p : part_) p.t.reserve(per);
+      return;
+    }
+    std::vector<std::thread> th;
+    for (int p = 1; p < kRegParts; ++p) th.emplace_back([this, p, per] { part_[p].t.reserve(per); });
+    part_[0].t.reserve(per);
+    for (auto& x : th) x.join();
+  }
+
+ private:
+  // one partition per cache-line pair: the threads inserting into different partitions never write
+  // the same line (a table's entry count changes on every insert)
+  struct alignas(128) Part {
+    FlatTable t;
+  };
+  Part part_[kRegParts];
+};
+
 // Number -> index registry (node and element numbers, unique keys).  Numbers
 // below a bound that follows the expected count (2 x reserved + 4096) live in
 // a direct array, so the usual dense numbering costs no hashing and no cache
@@ -1064,15 +1135,41 @@ class NumberMap {
  public:
   int64_t find(uint64_t key) const {
     if (key < dense_.size() && dense_[key] >= 0) return dense_[key];
-    return table_.size() ? table_.find(key) : -1;
+    return table_.find(key);
   }
   void prefetch(uint64_t key) const {
     if (key < dense_.size()) __builtin_prefetch(&dense_[key]);
-    else if (table_.size()) table_.prefetch(key);
+    else table_.prefetch(key);
   }
   void reserve(size_t total) {
     bound_ = std::max(bound_, 2 * total + 4096);
   }
+  // Size the direct array for keys up to max_key before threads insert (inserts then never resize it).
+  // Table entries whose keys the array now covers move into it, so a key below the array's size is
+  // never in the table and each key has one home: its direct slot or its table partition.
+  void fit(uint64_t max_key) {
+    const size_t want = (size_t)std::min<uint64_t>(bound_, max_key + 1), have = dense_.size();
+    if (want <= have) return;
+    std::vector<std::pair<uint64_t, int64_t>> moved;
+    table_.for_each([&](uint64_t k, int64_t v) {
+      if (k < want) moved.emplace_back(k, v);
+    });
+    for (const auto& kv : moved) table_.erase(kv.first, kv.second);
+    dense_.resize(want);  // no fill: the new slots are set to -1 by several threads
+    const unsigned T = want - have >= (size_t(1) << 18) ? 8u : 1u;
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < T; ++t)
+      th.emplace_back([this, t, T, have, want] {
+        std::fill(dense_.begin() + have + (want - have) * t / T, dense_.begin() + have + (want - have) * (t + 1) / T,
+                  -1);
+      });
+    std::fill(dense_.begin() + have, dense_.begin() + have + (want - have) / T, -1);
+    for (auto& x : th) x.join();
+    for (const auto& kv : moved) dense_[kv.first] = kv.second;
+  }
+  // the partition of a key for threaded inserts: blocks of 1024 direct slots (so that threads write
+  // disjoint cache lines of the array), the table's hash partition beyond it
+  int part(uint64_t key) const { return key < dense_.size() ? (int)((key >> 10) & (kRegParts - 1)) : reg_part(key); }
   void insert(uint64_t key, int64_t v) {
     if (key < bound_) {
       if (key >= dense_.size()) dense_.resize(std::min<size_t>(bound_, std::max<size_t>(key + 1, 2 * dense_.size())), -1);
@@ -1086,12 +1183,12 @@ class NumberMap {
       dense_[key] = -1;
       return;
     }
-    if (table_.size()) table_.erase(key, v);
+    table_.erase(key, v);
   }
 
  private:
-  std::vector<int64_t> dense_;
-  FlatTable table_;
+  HostVec<int64_t> dense_;
+  PartTable table_;
   size_t bound_ = 4096;
 };
 
@@ -1114,10 +1211,10 @@ struct fem_gpu {
   std::string err;
   // nodes
   size_t n_nodes = 0;
-  std::vector<uint32_t> idx_number;
-  std::vector<CoordKey> node_ck;  // normalised coordinate bits by index
+  HostVec<uint32_t> idx_number;
+  HostVec<CoordKey> node_ck;  // normalised coordinate bits by index
   NumberMap node_idx;             // number -> index
-  FlatTable node_coords;          // coordinate hash -> index
+  PartTable node_coords;          // coordinate hash -> index
   DevBuf<double> dx, dy, dz;
   DevBuf<double> stage;           // interleaved coordinates on their way in
   // elements
@@ -1127,21 +1224,21 @@ struct fem_gpu {
   size_t nt = 0;
   std::vector<uint32_t> t_num;
   NumberMap t_by_num;  // number -> element index
-  FlatTable t_pairs;   // node pair -> element index
+  PartTable t_pairs;   // node pair -> element index
   DevBuf<int32_t> t_n1, t_n2;
   DevBuf<double> t_E, t_A, t_A2;
   // beam
   size_t nbm = 0;
   std::vector<uint32_t> b_num;
   NumberMap b_by_num;
-  FlatTable b_pairs;
+  PartTable b_pairs;
   DevBuf<int32_t> b_n1, b_n2;
   DevBuf<double> b_E, b_nu, b_A, b_i11, b_i22, b_i12, b_it, b_ks, b_ax, b_ay, b_az;
   // plate
   size_t np = 0;
   std::vector<uint32_t> p_num, p_nodes;
   NumberMap p_by_num;
-  FlatTable p_sets;  // sorted node-number set hash -> element index
+  PartTable p_sets;  // sorted node-number set hash -> element index
   DevBuf<int32_t> p_n1, p_n2, p_n3, p_n4;
   DevBuf<double> p_E, p_nu, p_t, p_ks;
   // sparse separation (K_aa, K_ab, K_ba, K_bb)
@@ -1360,6 +1457,83 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
 
 extern "C" const char* fem_gpu_last_error(const fem_gpu_t* h) { return h ? h->err.c_str() : "null handle"; }
 
+namespace {
+// Bulk add_* calls of at least this many items check their registries on several host threads.
+constexpr size_t kParallelAdd = size_t(1) << 15;
+
+unsigned add_threads() {
+  const unsigned hw = std::thread::hardware_concurrency();
+  return std::max(1u, std::min<unsigned>(hw ? hw : 1u, kRegParts));
+}
+
+// f(t) on threads t = 0 .. T-1 (t = 0 on the calling thread)
+template <class F>
+void run_threads(unsigned T, F f) {
+  std::vector<std::thread> th;
+  for (unsigned t = 1; t < T; ++t) th.emplace_back(f, t);
+  f(0u);
+  for (auto& x : th) x.join();
+}
+
+// f(t, begin, end) over [0, n) in T contiguous chunks, chunk t on thread t
+template <class F>
+void parallel_chunks(unsigned T, size_t n, F f) {
+  run_threads(T, [&](unsigned t) { f(t, n * t / T, n * (t + 1) / T); });
+}
+
+// the thread (of T) that owns a registry partition; 0xff for an item without a key
+struct PartOwner {
+  uint8_t of[kRegParts];
+  explicit PartOwner(unsigned T) {
+    for (int p = 0; p < kRegParts; ++p) of[p] = (uint8_t)(p % T);
+  }
+  uint8_t operator()(uint64_t key) const { return of[reg_part(key)]; }
+  uint8_t of_part(int p) const { return of[p]; }
+};
+
+// The duplicate checks of a bulk add, in call order, on T host threads.  Item k has up to two
+// registry keys (roles A and B); own_a[k], own_b[k] are the threads owning their partitions (0xff:
+// no key).  The owner checks and inserts its partitions' keys in item order -- fa(k) / fb(k) return
+// false on a duplicate, else insert -- so every check sees the entries of exactly the earlier items
+// and calls, as one sequential pass would.  A thread stops at its first duplicate; the first failing
+// item is the smallest of those (role A before role B on the same item), items from `limit` on are
+// not looked at.  Returns that item (or limit) and sets *role to 1 (A), 2 (B) or 0.
+// pa(k) / pb(k) prefetch the registry slots of item k's keys, issued a few of the thread's own items ahead.
+template <class FA, class FB, class PA, class PB>
+size_t registry_pass(unsigned T, size_t limit, const uint8_t* own_a, const uint8_t* own_b, FA fa, FB fb, PA pa,
+                     PB pb, int* role) {
+  std::vector<size_t> first(T, limit);
+  std::vector<int> which(T, 0);
+  const size_t ahead = 8 * (size_t)T;  // about 8 own items ahead
+  run_threads(T, [&](unsigned t) {
+    for (size_t k = 0; k < limit; ++k) {
+      if (k + ahead < limit) {
+        if (own_a[k + ahead] == t) pa(k + ahead);
+        if (own_b[k + ahead] == t) pb(k + ahead);
+      }
+      if (own_a[k] == t && !fa(k)) {
+        first[t] = k;
+        which[t] = 1;
+        return;
+      }
+      if (own_b[k] == t && !fb(k)) {
+        first[t] = k;
+        which[t] = 2;
+        return;
+      }
+    }
+  });
+  size_t f = limit;
+  *role = 0;
+  for (unsigned t = 0; t < T; ++t)
+    if (first[t] < f || (first[t] == f && which[t] && (*role == 0 || which[t] < *role))) {
+      f = first[t];
+      *role = which[t];
+    }
+  return f;
+}
+}  // namespace
+
 // add_node, methods_for_node_data_handle.rs:39-79
 extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const double* xyz, size_t n,
                                  size_t* n_added) {
@@ -1373,10 +1547,80 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
   h->node_coords.reserve(h->n_nodes + n);
   h->node_ck.reserve(h->n_nodes + n);
   h->idx_number.reserve(h->n_nodes + n);
+  if (n >= kParallelAdd) {
+    // keys of every node, then the registry pass on host threads (same checks, same first failure)
+    const unsigned T = add_threads();
+    const size_t room = h->nodes_number > start ? (size_t)h->nodes_number - start : 0;
+    const size_t limit = std::min(n, room);
+    const PartOwner owner(T);
+    HostVec<uint64_t> chash(n);
+    HostVec<uint8_t> pa(n), pb(n);
+    std::vector<uint32_t> tmax(T, 0);
+    h->node_ck.resize(start + n);
+    h->idx_number.resize(start + n);
+    parallel_chunks(T, n, [&](unsigned t, size_t b, size_t e) {
+      uint32_t mx = 0;
+      for (size_t q = b; q < e; ++q) {
+        const double x = xyz[3 * q], y = xyz[3 * q + 1], z = xyz[3 * q + 2];
+        const CoordKey ck = coord_key(x, y, z);
+        h->node_ck[start + q] = ck;
+        h->idx_number[start + q] = numbers[q];
+        if (x == x && y == y && z == z) {
+          chash[q] = coord_hash(ck);
+          pb[q] = owner(chash[q]);
+        } else {
+          pb[q] = 0xff;  // NaN coordinates are never equal to any
+        }
+        mx = std::max(mx, numbers[q]);
+      }
+      tmax[t] = mx;
+    });
+    h->node_idx.fit(*std::max_element(tmax.begin(), tmax.end()));
+    parallel_chunks(T, n, [&](unsigned, size_t b, size_t e) {
+      for (size_t q = b; q < e; ++q) pa[q] = owner.of_part(h->node_idx.part(numbers[q]));
+    });
+    const HostVec<CoordKey>& known = h->node_ck;
+    int role = 0;
+    const size_t f = registry_pass(
+        T, limit, pa.data(), pb.data(),
+        [&](size_t q) {
+          if (h->node_idx.find(numbers[q]) >= 0) return false;
+          h->node_idx.insert(numbers[q], (int64_t)(start + q));
+          return true;
+        },
+        [&](size_t q) {
+          const CoordKey& ck = known[start + q];
+          if (h->node_coords.find(chash[q], [&](int64_t i) { return known[(size_t)i] == ck; }) >= 0) return false;
+          h->node_coords.insert(chash[q], (int64_t)(start + q));
+          return true;
+        },
+        [&](size_t q) { h->node_idx.prefetch(numbers[q]); }, [&](size_t q) { h->node_coords.prefetch(chash[q]); },
+        &role);
+    for (size_t q = f; q < limit; ++q) {  // entries of items at or after the first failure go again
+      h->node_idx.erase(numbers[q], (int64_t)(start + q));
+      if (pb[q] != 0xff) h->node_coords.erase(chash[q], (int64_t)(start + q));
+    }
+    h->node_ck.resize(start + f);
+    h->idx_number.resize(start + f);
+    h->n_nodes = start + f;
+    k = f;
+    if (f < n) {
+      if (role == 1) {
+        code = h->fail(FEM_GPU_ERR_NODE_NUMBER, "Node with number %u already exists!", numbers[f]);
+      } else if (role == 2) {
+        code = h->fail(FEM_GPU_ERR_NODE_COORDS, "Node with coordinates x: %s, y: %s, z: %s already exists!",
+                       rust_f64(xyz[3 * f]).c_str(), rust_f64(xyz[3 * f + 1]).c_str(),
+                       rust_f64(xyz[3 * f + 2]).c_str());
+      } else {
+        code = h->fail(FEM_GPU_ERR_NODE_LIMIT, "Nodes number could not be greater than %u!", h->nodes_number);
+      }
+    }
+  }
   constexpr size_t kAhead = 8;  // prefetch distance (entries) into the coordinate registry
-  for (size_t q = 0; q < std::min(n, kAhead); ++q)
-    h->node_coords.prefetch(coord_hash(coord_key(xyz[3 * q], xyz[3 * q + 1], xyz[3 * q + 2])));
-  for (; k < n; ++k) {
+  if (n < kParallelAdd)
+    for (size_t q = 0; q < std::min(n, kAhead); ++q)
+      h->node_coords.prefetch(coord_hash(coord_key(xyz[3 * q], xyz[3 * q + 1], xyz[3 * q + 2])));
+  for (; k < n && n < kParallelAdd; ++k) {
     if (k + kAhead < n) {
       const double* f = xyz + 3 * (k + kAhead);
       h->node_coords.prefetch(coord_hash(coord_key(f[0], f[1], f[2])));
@@ -1396,7 +1640,7 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
     CoordKey ck = coord_key(x, y, z);
     if (x == x && y == y && z == z) {
       uint64_t hk = coord_hash(ck);
-      const std::vector<CoordKey>& known = h->node_ck;
+      const HostVec<CoordKey>& known = h->node_ck;
       if (h->node_coords.find(hk, [&](int64_t i) { return known[(size_t)i] == ck; }) >= 0) {
         code = h->fail(FEM_GPU_ERR_NODE_COORDS, "Node with coordinates x: %s, y: %s, z: %s already exists!",
                        rust_f64(x).c_str(), rust_f64(y).c_str(), rust_f64(z).c_str());
@@ -1427,10 +1671,153 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
 namespace {
 constexpr size_t kRegAhead = 8;  // prefetch distance (elements) into the registries of the bulk add_* loops
 
+
 int lookup_node(fem_gpu* h, uint32_t num, int32_t* idx) {
   int64_t i = h->node_idx.find(num);
   if (i < 0) return h->fail(FEM_GPU_ERR_NODE_NOT_EXIST, "Node with number %u does not exist!", num);
   *idx = (int32_t)i;
+  return FEM_GPU_OK;
+}
+
+// The host checks of a bulk add of two-node elements (trusses, beams) on host threads, in the
+// sequential loop's order: both nodes exist, the number is new, the node pair is new.  Returns the
+// status of the first failing item (message set as the sequential loop would set it); *passed is
+// the number of items before it, whose node indices are in i1, i2.
+int two_node_checks(fem_gpu* h, const char* kind, NumberMap& by_num, PartTable& pairs, size_t base,
+                    const uint32_t* numbers, const uint32_t* nodes, size_t n, HostVec<int32_t>& i1,
+                    HostVec<int32_t>& i2, size_t* passed) {
+  const unsigned T = add_threads();
+  i1.resize(n);
+  i2.resize(n);
+  const PartOwner owner(T);
+  HostVec<uint64_t> pk(n);
+  HostVec<uint8_t> pa(n), pb(n);
+  std::vector<size_t> tmiss(T, n);
+  std::vector<uint32_t> tmax(T, 0);
+  parallel_chunks(T, n, [&](unsigned t, size_t b, size_t e) {
+    uint32_t mx = 0;
+    for (size_t q = b; q < e; ++q) {
+      const int64_t a = h->node_idx.find(nodes[2 * q]), c = h->node_idx.find(nodes[2 * q + 1]);
+      if ((a < 0 || c < 0) && tmiss[t] == n) tmiss[t] = q;
+      i1[q] = (int32_t)a;
+      i2[q] = (int32_t)c;
+      pk[q] = pair_key(nodes[2 * q], nodes[2 * q + 1]);
+      pb[q] = owner(pk[q]);
+      mx = std::max(mx, numbers[q]);
+    }
+    tmax[t] = mx;
+  });
+  const size_t limit = *std::min_element(tmiss.begin(), tmiss.end());
+  by_num.fit(*std::max_element(tmax.begin(), tmax.end()));
+  parallel_chunks(T, n, [&](unsigned, size_t b, size_t e) {
+    for (size_t q = b; q < e; ++q) pa[q] = owner.of_part(by_num.part(numbers[q]));
+  });
+  int role = 0;
+  const size_t f = registry_pass(
+      T, limit, pa.data(), pb.data(),
+      [&](size_t q) {
+        if (by_num.find(numbers[q]) >= 0) return false;
+        by_num.insert(numbers[q], (int64_t)(base + q));
+        return true;
+      },
+      [&](size_t q) {
+        if (pairs.find(pk[q]) >= 0) return false;
+        pairs.insert(pk[q], (int64_t)(base + q));
+        return true;
+      },
+      [&](size_t q) { by_num.prefetch(numbers[q]); }, [&](size_t q) { pairs.prefetch(pk[q]); }, &role);
+  for (size_t q = f; q < limit; ++q) {
+    by_num.erase(numbers[q], (int64_t)(base + q));
+    pairs.erase(pk[q], (int64_t)(base + q));
+  }
+  i1.resize(f);
+  i2.resize(f);
+  *passed = f;
+  if (f == n) return FEM_GPU_OK;
+  if (role == 1) return h->fail(FEM_GPU_ERR_ELEM_NUMBER, "%s element with number %u already exists!", kind, numbers[f]);
+  if (role == 2)
+    return h->fail(FEM_GPU_ERR_ELEM_SAME_NODES, "%s element with node number %u and %u already exists!", kind,
+                   nodes[2 * f], nodes[2 * f + 1]);
+  int32_t idx;
+  const int c = lookup_node(h, nodes[2 * f], &idx);
+  return c ? c : lookup_node(h, nodes[2 * f + 1], &idx);
+}
+
+// The same for plates: the four nodes exist, the number is new, the node set is new.  Returns -1
+// (nothing changed) when an item before the first missing node repeats a node number: those take
+// the sequential loop's subset test.
+int plate_checks(fem_gpu* h, const uint32_t* numbers, const uint32_t* nodes, size_t n, HostVec<int32_t>* id,
+                 size_t* passed) {
+  const unsigned T = add_threads();
+  const size_t base = h->np;
+  for (int q = 0; q < 4; ++q) id[q].resize(n);
+  const PartOwner owner(T);
+  HostVec<uint64_t> hs(n);
+  HostVec<uint8_t> pa(n), pb(n);
+  std::vector<size_t> tmiss(T, n), trep(T, n);
+  std::vector<uint32_t> tmax(T, 0);
+  parallel_chunks(T, n, [&](unsigned t, size_t b, size_t e) {
+    uint32_t mx = 0;
+    for (size_t q = b; q < e; ++q) {
+      const uint32_t* nn = nodes + 4 * q;
+      bool miss = false;
+      for (int c = 0; c < 4; ++c) {
+        const int64_t i = h->node_idx.find(nn[c]);
+        miss = miss || i < 0;
+        id[c][q] = (int32_t)i;
+      }
+      if (miss && tmiss[t] == n) tmiss[t] = q;
+      const Set4 key = sorted4(nn);
+      if ((key.s[0] == key.s[1] || key.s[1] == key.s[2] || key.s[2] == key.s[3]) && trep[t] == n) trep[t] = q;
+      hs[q] = set4_hash(key);
+      pb[q] = owner(hs[q]);
+      mx = std::max(mx, numbers[q]);
+    }
+    tmax[t] = mx;
+  });
+  const size_t limit = *std::min_element(tmiss.begin(), tmiss.end());
+  if (*std::min_element(trep.begin(), trep.end()) < limit) return -1;
+  h->p_by_num.fit(*std::max_element(tmax.begin(), tmax.end()));
+  parallel_chunks(T, n, [&](unsigned, size_t b, size_t e) {
+    for (size_t q = b; q < e; ++q) pa[q] = owner.of_part(h->p_by_num.part(numbers[q]));
+  });
+  const size_t np0 = h->np;
+  int role = 0;
+  const size_t f = registry_pass(
+      T, limit, pa.data(), pb.data(),
+      [&](size_t q) {
+        if (h->p_by_num.find(numbers[q]) >= 0) return false;
+        h->p_by_num.insert(numbers[q], (int64_t)(base + q));
+        return true;
+      },
+      [&](size_t q) {
+        const Set4 key = sorted4(nodes + 4 * q);
+        const bool same = h->p_sets.find(hs[q], [&](int64_t e) {
+          const uint32_t* mm = (size_t)e < np0 ? &h->p_nodes[4 * (size_t)e] : nodes + 4 * ((size_t)e - np0);
+          return sorted4(mm) == key;
+        }) >= 0;
+        if (same) return false;
+        h->p_sets.insert(hs[q], (int64_t)(base + q));
+        return true;
+      },
+      [&](size_t q) { h->p_by_num.prefetch(numbers[q]); }, [&](size_t q) { h->p_sets.prefetch(hs[q]); }, &role);
+  for (size_t q = f; q < limit; ++q) {
+    h->p_by_num.erase(numbers[q], (int64_t)(base + q));
+    h->p_sets.erase(hs[q], (int64_t)(base + q));
+  }
+  for (int c = 0; c < 4; ++c) id[c].resize(f);
+  *passed = f;
+  if (f == n) return FEM_GPU_OK;
+  const uint32_t* nn = nodes + 4 * f;
+  if (role == 1) return h->fail(FEM_GPU_ERR_ELEM_NUMBER, "Plate element with number %u already exists!", numbers[f]);
+  if (role == 2)
+    return h->fail(FEM_GPU_ERR_ELEM_SAME_NODES, "Plate element with nodes numbers [%u, %u, %u, %u] already exists!",
+                   nn[0], nn[1], nn[2], nn[3]);
+  int32_t idx;
+  for (int c = 0; c < 4; ++c) {
+    const int st = lookup_node(h, nn[c], &idx);
+    if (st) return st;
+  }
   return FEM_GPU_OK;
 }
 }  // namespace
@@ -1442,8 +1829,8 @@ extern "C" int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const 
   if (!h || (n && (!numbers || !nodes || !young || !area))) return FEM_GPU_ERR_ARGUMENT;
   int st = ensure_ready(h);
   if (st) return st;
-  std::vector<int32_t> i1, i2;
-  std::vector<double> a2v;
+  HostVec<int32_t> i1, i2;
+  HostVec<double> a2v;
   i1.reserve(n);
   i2.reserve(n);
   a2v.reserve(n);
@@ -1452,7 +1839,12 @@ extern "C" int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const 
   size_t k = 0;
   h->t_by_num.reserve(h->nt + n);
   h->t_pairs.reserve(h->nt + n);
-  for (; k < n; ++k) {
+  if (n >= kParallelAdd) {
+    host_code = two_node_checks(h, "Truss", h->t_by_num, h->t_pairs, h->nt, numbers, nodes, n, i1, i2, &k);
+    a2v.resize(k);
+    for (size_t q = 0; q < k; ++q) a2v[q] = area2 ? area2[q] : NAN;
+  }
+  for (; k < n && n < kParallelAdd; ++k) {
     if (k + kRegAhead < n) {
       const uint32_t* f = nodes + 2 * (k + kRegAhead);
       h->t_pairs.prefetch(pair_key(f[0], f[1]));
@@ -1497,7 +1889,7 @@ extern "C" int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const 
     h->t_by_num.erase(numbers[j], (int64_t)(base + j));
     h->t_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]), (int64_t)(base + j));
   }
-  for (size_t j = 0; j < accepted; ++j) h->t_num.push_back(numbers[j]);
+  h->t_num.insert(h->t_num.end(), numbers, numbers + accepted);
   h->nt += accepted;
   h->append_run(kTruss, base, accepted);
   if (n_added) *n_added = accepted;
@@ -1532,8 +1924,8 @@ extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const ui
     return FEM_GPU_ERR_ARGUMENT;
   int st = ensure_ready(h);
   if (st) return st;
-  std::vector<int32_t> i1, i2;
-  std::vector<double> ax, ay, az;
+  HostVec<int32_t> i1, i2;
+  HostVec<double> ax, ay, az;
   int host_code = FEM_GPU_OK;
   std::string host_err;
   size_t k = 0;
@@ -1544,7 +1936,20 @@ extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const ui
   ax.reserve(n);
   ay.reserve(n);
   az.reserve(n);
-  for (; k < n; ++k) {
+  if (n >= kParallelAdd) {
+    host_code = two_node_checks(h, "Beam", h->b_by_num, h->b_pairs, h->nbm, numbers, nodes, n, i1, i2, &k);
+    ax.resize(k);
+    ay.resize(k);
+    az.resize(k);
+    parallel_chunks(add_threads(), k, [&](unsigned, size_t b, size_t e) {
+      for (size_t q = b; q < e; ++q) {
+        ax[q] = local_axis[3 * q];
+        ay[q] = local_axis[3 * q + 1];
+        az[q] = local_axis[3 * q + 2];
+      }
+    });
+  }
+  for (; k < n && n < kParallelAdd; ++k) {
     if (k + kRegAhead < n) {
       const uint32_t* f = nodes + 2 * (k + kRegAhead);
       h->b_pairs.prefetch(pair_key(f[0], f[1]));
@@ -1598,7 +2003,7 @@ extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const ui
     h->b_by_num.erase(numbers[j], (int64_t)(base + j));
     h->b_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]), (int64_t)(base + j));
   }
-  for (size_t j = 0; j < accepted; ++j) h->b_num.push_back(numbers[j]);
+  h->b_num.insert(h->b_num.end(), numbers, numbers + accepted);
   h->nbm += accepted;
   h->append_run(kBeam, base, accepted);
   if (n_added) *n_added = accepted;
@@ -1639,7 +2044,7 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
     return FEM_GPU_ERR_ARGUMENT;
   int st = ensure_ready(h);
   if (st) return st;
-  std::vector<int32_t> id[4];
+  HostVec<int32_t> id[4];
   for (auto& v : id) v.reserve(n);
   int host_code = FEM_GPU_OK;
   std::string host_err;
@@ -1648,7 +2053,17 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
   h->p_sets.reserve(h->np + n);
   h->p_nodes.reserve(4 * (h->np + n));
   h->p_num.reserve(h->np + n);
-  for (; k < n; ++k) {
+  bool sequential = n < kParallelAdd;
+  if (!sequential) {
+    host_code = plate_checks(h, numbers, nodes, n, id, &k);
+    if (host_code < 0) {  // repeated node numbers: the sequential loop's subset test
+      host_code = FEM_GPU_OK;
+      sequential = true;
+      k = 0;
+      for (auto& v : id) v.clear();
+    }
+  }
+  for (; k < n && sequential; ++k) {
     if (k + kRegAhead < n) {
       const uint32_t* f = nodes + 4 * (k + kRegAhead);
       h->p_sets.prefetch(set4_hash(sorted4(f)));
@@ -1717,10 +2132,8 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
     h->p_by_num.erase(numbers[j], (int64_t)(base + j));
     h->p_sets.erase(set4_hash(sorted4(nodes + 4 * j)), (int64_t)(base + j));
   }
-  for (size_t j = 0; j < accepted; ++j) {
-    h->p_num.push_back(numbers[j]);
-    for (int q = 0; q < 4; ++q) h->p_nodes.push_back(nodes[4 * j + q]);
-  }
+  h->p_num.insert(h->p_num.end(), numbers, numbers + accepted);
+  h->p_nodes.insert(h->p_nodes.end(), nodes, nodes + 4 * accepted);
   h->np += accepted;
   h->append_run(kPlate, base, accepted);
   if (n_added) *n_added = accepted;

@@ -1,0 +1,143 @@
+"""Bulk add_* calls large enough for the threaded registry checks (>= 32768 items): the first
+failure, its message and the state after it match the oracle's sequential calls, for every kind of
+duplicate the reference rejects; after the failure the rest of the model is added and the CSR
+compared bit for bit."""
+import numpy as np
+import pytest
+
+from finite_element_method_gb300 import FEM, FEMError, meshes
+from oracle import fem_oracle as fo
+
+pytestmark = pytest.mark.gpu
+
+N = 201  # 201 x 201 = 40,401 nodes, 40,000 plates, 80,400 grid bars
+
+
+def grid():
+    ii, jj = np.meshgrid(np.arange(N), np.arange(N), indexing="xy")
+    xyz = np.stack([ii.ravel() * 0.5, jj.ravel() * 0.5, np.zeros(N * N)], -1)
+    numbers = np.arange(1, N * N + 1, dtype=np.uint32)
+    node = lambda i, j: 1 + i + N * j
+    j, i = np.meshgrid(np.arange(N - 1), np.arange(N - 1), indexing="ij")
+    quads = np.stack([node(i + 1, j + 1), node(i, j + 1), node(i, j), node(i + 1, j)], -1).reshape(-1, 4)
+    bars = np.concatenate([np.stack([node(i, j), node(i + 1, j)], -1).reshape(-1, 2),
+                           np.stack([node(i, j), node(i, j + 1)], -1).reshape(-1, 2)])
+    return numbers, xyz, quads.astype(np.uint32), bars.astype(np.uint32)
+
+
+def both(n_nodes):
+    return FEM(1e-12, 1e-12, n_nodes), fo.OracleFEM(1e-12, 1e-12, n_nodes)
+
+
+def expect_same_failure(call_g, call_o):
+    with pytest.raises(FEMError) as eg:
+        call_g()
+    with pytest.raises(fo.OracleError) as eo:
+        call_o()
+    assert str(eg.value) == str(eo.value)
+    return str(eg.value)
+
+
+@pytest.mark.parametrize("case", ["number", "coords", "number_before_coords", "limit", "nan"])
+def test_bulk_nodes(case):
+    numbers, xyz, quads, _ = grid()
+    numbers, xyz = numbers.copy(), xyz.copy()
+    n_nodes = len(numbers)
+    if case == "number":
+        numbers[30000] = numbers[123]
+    elif case == "coords":
+        xyz[30000] = xyz[456]
+        numbers[35000] = numbers[7]
+    elif case == "number_before_coords":
+        numbers[30000] = numbers[5]
+        xyz[30000] = xyz[9]
+    elif case == "limit":
+        n_nodes = 33333
+    else:  # two NaN coordinates never collide; a duplicate after them still fails
+        xyz[31000] = np.nan
+        xyz[31001] = np.nan
+        xyz[36000] = xyz[31002]
+    g, o = both(n_nodes)
+    msg = expect_same_failure(lambda: g.add_nodes(numbers, xyz), lambda: o.add_nodes(numbers, xyz))
+    assert g.node_count() == len(o.index_node_numbers())
+    np.testing.assert_array_equal(g.index_node_numbers(), o.index_node_numbers())
+    assert msg
+
+
+def test_bulk_nodes_then_continue_and_assemble():
+    numbers, xyz, quads, _ = grid()
+    bad = numbers.copy()
+    bad[25000] = bad[10]
+    g, o = both(len(numbers))
+    expect_same_failure(lambda: g.add_nodes(bad, xyz), lambda: o.add_nodes(bad, xyz))
+    k = g.node_count()
+    assert k == 25000
+    g.add_nodes(numbers[k:], xyz[k:])
+    o.add_nodes(numbers[k:], xyz[k:])
+    E, nu, t, ks = 70e9, 0.3, 0.02, 5 / 6
+    g.add_plates(np.arange(1, len(quads) + 1), quads, E, nu, t, ks)
+    o.add_plates(np.arange(1, len(quads) + 1), quads, E, nu, t, ks)
+    g.assemble()
+    for a, b in zip(g.stiffness_csr(), o.csr()):
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+@pytest.mark.parametrize("kind", ["truss", "beam"])
+@pytest.mark.parametrize("case", ["number", "pair", "reversed_pair", "missing_node", "order"])
+def test_bulk_two_node_elements(kind, case):
+    numbers, xyz, _, bars = grid()
+    bars = bars.copy()
+    m = len(bars)
+    enums = np.arange(1, m + 1, dtype=np.uint32)
+    if case == "number":
+        enums[40000] = enums[3]
+    elif case == "pair":
+        bars[40000] = bars[77]
+    elif case == "reversed_pair":
+        bars[40000] = bars[77][::-1]
+    elif case == "missing_node":
+        bars[40000, 1] = 10 ** 7
+    else:  # a pair duplicate before a number duplicate
+        bars[50000] = bars[1]
+        enums[60000] = enums[2]
+    g, o = both(len(numbers))
+    g.add_nodes(numbers, xyz)
+    o.add_nodes(numbers, xyz)
+    if kind == "truss":
+        add_g = lambda: g.add_trusses(enums, bars, 200e9, 3e-4)
+        add_o = lambda: o.add_trusses(enums, bars, 200e9, 3e-4)
+    else:
+        args = (210e9, 0.3, 1e-2, 3e-5, 8e-5, 0.0, 2e-5, 5 / 6, [0.0, 0.0, 1.0])
+        add_g = lambda: g.add_beams(enums, bars, *args)
+        add_o = lambda: o.add_beams(enums, bars, *args)
+    expect_same_failure(add_g, add_o)
+    counts = g.element_counts()
+    assert counts[0 if kind == "truss" else 1] == (50000 if case == "order" else 40000)
+    g.assemble()
+    for a, b in zip(g.stiffness_csr(), o.csr()):
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+@pytest.mark.parametrize("case", ["number", "same_nodes", "missing_node", "repeated_node_numbers"])
+def test_bulk_plates(case):
+    numbers, xyz, quads, _ = grid()
+    quads = quads.copy()
+    m = len(quads)
+    pnums = np.arange(1, m + 1, dtype=np.uint32)
+    if case == "number":
+        pnums[35000] = pnums[100]
+    elif case == "same_nodes":
+        quads[35000] = quads[100][[2, 3, 0, 1]]
+    elif case == "missing_node":
+        quads[35000, 2] = 10 ** 7
+    else:  # a plate whose node list repeats a number (the subset rule): the sequential path decides
+        quads[20000] = [quads[5][0], quads[5][1], quads[5][1], quads[5][2]]
+    g, o = both(len(numbers))
+    g.add_nodes(numbers, xyz)
+    o.add_nodes(numbers, xyz)
+    E, nu, t, ks = 70e9, 0.3, 0.02, 5 / 6
+    expect_same_failure(lambda: g.add_plates(pnums, quads, E, nu, t, ks),
+                        lambda: o.add_plates(pnums, quads, E, nu, t, ks))
+    g.assemble()
+    for a, b in zip(g.stiffness_csr(), o.csr()):
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
