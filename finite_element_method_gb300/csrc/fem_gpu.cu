@@ -551,12 +551,11 @@ __device__ __forceinline__ uint32_t kinds_of(uint64_t m) {
   return ((m & q0) ? 1u : 0u) | ((m & q1) ? 2u : 0u) | ((m & q2) ? 4u : 0u) | ((m & q3) ? 8u : 0u);
 }
 
-// per row node: column positions of each adjacency entry in its 6 rows, row
-// lengths and group counts
+// per row node: the lengths of its 6 rows and its group count
 __global__ void k_row_counts(size_t n_nodes, const int32_t* __restrict__ seg_begin,
                              const int32_t* __restrict__ seg_end, const uint32_t* __restrict__ avals,
                              const uint64_t* __restrict__ blk_mask, const uint64_t* __restrict__ blk_maskT,
-                             int32_t* blk_colpos, int64_t* row_nnz, int64_t* gcount) {
+                             int64_t* row_nnz, int64_t* gcount) {
   size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (r >= n_nodes) return;
   int32_t run[6] = {0, 0, 0, 0, 0, 0};
@@ -566,52 +565,11 @@ __global__ void k_row_counts(size_t n_nodes, const int32_t* __restrict__ seg_beg
     uint32_t v = avals[k];
     uint32_t b = v >> 1, t = v & 1u;
     uint64_t m = t ? blk_maskT[b] : blk_mask[b];
-    for (int a = 0; a < 6; ++a) {
-      blk_colpos[(size_t)b * 12 + (t ? 6 : 0) + a] = run[a];
-      run[a] += __popcll((m >> (6 * a)) & 63ull);
-    }
+    for (int a = 0; a < 6; ++a) run[a] += __popcll((m >> (6 * a)) & 63ull);
     ng += __popc(kinds_of(m));
   }
   for (int a = 0; a < 6; ++a) row_nnz[6 * r + a] = run[a];
   gcount[r] = ng;
-}
-
-__global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin, const int32_t* __restrict__ seg_end,
-                           const uint64_t* __restrict__ akeys, const uint32_t* __restrict__ avals,
-                           const uint64_t* __restrict__ blk_mask, const uint64_t* __restrict__ blk_maskT,
-                           const int32_t* __restrict__ blk_colpos, const int64_t* __restrict__ row_ptr,
-                           const int64_t* __restrict__ gbase, int32_t* col_idx, int32_t* nnz_group, int32_t* g_row,
-                           int32_t* g_col, uint8_t* g_kind) {
-  size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (r >= n_nodes) return;
-  int32_t s = seg_begin[r], e = seg_end[r];
-  int64_t g = gbase[r];
-  for (int32_t k = s; k < e && s >= 0; ++k) {
-    uint32_t v = avals[k];
-    uint32_t b = v >> 1, t = v & 1u;
-    uint32_t J = (uint32_t)(akeys[k] & 0xffffffffu);
-    uint64_t m = t ? blk_maskT[b] : blk_mask[b];
-    uint32_t km = kinds_of(m);
-    int32_t kg[4] = {-1, -1, -1, -1};
-    for (int kd = 0; kd < 4; ++kd)
-      if (km & (1u << kd)) {
-        g_row[g] = (int32_t)r;
-        g_col[g] = (int32_t)J;
-        g_kind[g] = (uint8_t)kd;
-        kg[kd] = (int32_t)g;
-        ++g;
-      }
-    for (int a = 0; a < 6; ++a) {
-      int64_t pos = row_ptr[6 * r + a] + blk_colpos[(size_t)b * 12 + (t ? 6 : 0) + a];
-      uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
-      for (int c = 0; c < 6; ++c)
-        if (rowbits & (1u << c)) {
-          col_idx[pos] = (int32_t)(6 * J + c);
-          nnz_group[pos] = kg[2 * (a / 3) + c / 3];
-          ++pos;
-        }
-    }
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -662,14 +620,6 @@ __global__ void k_pair_offsets(const uint32_t* __restrict__ svals, const uint32_
 // ---------------------------------------------------------------------------
 // kernel: deterministic block reduction into CSR
 // ---------------------------------------------------------------------------
-// position of the n-th (0-based) set bit of a 36-bit mask
-__device__ __forceinline__ int nth_set_bit(uint64_t m, int n) {
-  uint32_t lo = (uint32_t)m;
-  int plo = __popc(lo);
-  if (n < plo) return (int)__fns(lo, 0, n + 1);
-  return 32 + (int)__fns((uint32_t)(m >> 32), 0, n - plo + 1);
-}
-
 constexpr int kFlagPattern = 1;                      // bit of *flag: the exact-zero pattern changed
 
 // Block-sum slots.  A packed entry of a block with one contribution needs no
@@ -711,40 +661,59 @@ __device__ __forceinline__ int packed_pos(uint32_t lay, int en) {
   return p;
 }
 
-// Symbolic, once per pattern: the source of every CSR entry -- the scratch
-// position of its packed entry when its block has one contribution, otherwise
-// its S slot (both in one buffer: S starts at vs_off), for the (I, J) block
-// entry and for the transposed entry of the (J, I) block below the diagonal.
-__global__ void k_csr_sources(size_t nb, const uint64_t* __restrict__ blk_mask, const uint64_t* __restrict__ blk_maskT,
-                              const uint8_t* __restrict__ blk_lay, const uint32_t* __restrict__ blk_count,
-                              const unsigned long long* __restrict__ blk_voff, SlotLayout L,
-                              const int32_t* __restrict__ blk_I, const int32_t* __restrict__ blk_J,
-                              const int32_t* __restrict__ blk_colpos, const int64_t* __restrict__ row_ptr,
-                              uint32_t* src_map) {
-  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (t >= nb * 36) return;
-  const size_t b = t / 36;
-  const int j = (int)(t - 36 * b);
-  const uint64_t m = blk_mask[b];
-  if (j >= __popcll(m)) return;
-  const uint32_t lay = blk_lay[b];
-  const int cat = slot_cat(blk_count[b]);
-  const unsigned long long sb =
-      cat == 0 ? blk_voff[b] : L.vs_off + L.off[cat] + L.base[(size_t)cat * L.stride + b];
-  const int32_t I = blk_I[b], J = blk_J[b];
-  const int en = nth_set_bit(m, j);
-  const int a = en / 6, c = en - 6 * (en / 6);
-  const uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
-  const int64_t pos = row_ptr[6 * (int64_t)I + a] + blk_colpos[b * 12 + a] + __popc(rowbits & ((1u << c) - 1u));
-  src_map[pos] = (uint32_t)(sb + (unsigned long long)packed_pos(lay, en));
-  if (I != J) {
-    const uint64_t mT = blk_maskT[b];
-    const int enT = nth_set_bit(mT, j);  // j-th entry of the transposed block, row-major
-    const int cT = enT / 6, aT = enT - 6 * (enT / 6);
-    const uint32_t rowbitsT = (uint32_t)((mT >> (6 * cT)) & 63ull);
-    const int64_t pos2 =
-        row_ptr[6 * (int64_t)J + cT] + blk_colpos[b * 12 + 6 + cT] + __popc(rowbitsT & ((1u << aT) - 1u));
-    src_map[pos2] = (uint32_t)(sb + (unsigned long long)packed_pos(lay, 6 * aT + cT));
+// Symbolic, once per pattern: CSR row 6r + a, one thread per row.  Walking the
+// row node's adjacency (its blocks in column-node order) it writes, in column
+// order, every entry's column, stiffness group and value source: the scratch
+// position of a block with one contribution, else the entry's block-sum slot
+// in S (both in one buffer: S starts at vs_off).  A block stored with the row
+// node second (t = 1) is read transposed.  The a = 0 thread of each node also
+// writes the node's groups.
+__global__ void k_row_fill(size_t n_rows, const int32_t* __restrict__ seg_begin, const int32_t* __restrict__ seg_end,
+                           const uint64_t* __restrict__ akeys, const uint32_t* __restrict__ avals,
+                           const uint64_t* __restrict__ blk_mask, const uint64_t* __restrict__ blk_maskT,
+                           const uint8_t* __restrict__ blk_lay, const uint32_t* __restrict__ blk_count,
+                           const unsigned long long* __restrict__ blk_voff, SlotLayout L,
+                           const int64_t* __restrict__ row_ptr, const int64_t* __restrict__ gbase,
+                           int32_t* __restrict__ col_idx, int32_t* __restrict__ nnz_group,
+                           uint32_t* __restrict__ src_map, int32_t* __restrict__ g_row, int32_t* __restrict__ g_col,
+                           uint8_t* __restrict__ g_kind) {
+  const size_t row = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (row >= n_rows) return;
+  const size_t r = row / 6;
+  const int a = (int)(row - 6 * r);
+  const int32_t s = seg_begin[r], e = seg_end[r];
+  int64_t g = gbase[r];
+  int64_t pos = row_ptr[row];
+  for (int32_t k = s; k < e && s >= 0; ++k) {
+    const uint32_t v = avals[k];
+    const uint32_t b = v >> 1, t = v & 1u;
+    const uint32_t J = (uint32_t)(akeys[k] & 0xffffffffu);
+    const uint64_t m = t ? blk_maskT[b] : blk_mask[b];
+    const uint32_t km = kinds_of(m);
+    int32_t kg[4] = {-1, -1, -1, -1};
+    for (int kd = 0; kd < 4; ++kd)
+      if (km & (1u << kd)) {
+        if (a == 0) {
+          g_row[g] = (int32_t)r;
+          g_col[g] = (int32_t)J;
+          g_kind[g] = (uint8_t)kd;
+        }
+        kg[kd] = (int32_t)g;
+        ++g;
+      }
+    const uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
+    if (!rowbits) continue;
+    const uint32_t lay = blk_lay[b];
+    const int cat = slot_cat(blk_count[b]);
+    const unsigned long long sb =
+        cat == 0 ? blk_voff[b] : L.vs_off + L.off[cat] + L.base[(size_t)cat * L.stride + b];
+    for (int c = 0; c < 6; ++c)
+      if (rowbits & (1u << c)) {
+        col_idx[pos] = (int32_t)(6 * J + c);
+        nnz_group[pos] = kg[2 * (a / 3) + c / 3];
+        src_map[pos] = (uint32_t)(sb + (unsigned long long)packed_pos(lay, t ? 6 * c + a : 6 * a + c));
+        ++pos;
+      }
   }
 }
 
@@ -755,26 +724,25 @@ __global__ void k_csr_sources(size_t nb, const uint64_t* __restrict__ blk_mask, 
 __global__ void k_slot_desc(size_t nb, const uint32_t* __restrict__ blk_count, const uint64_t* __restrict__ blk_pmask,
                             const uint8_t* __restrict__ blk_lay, const unsigned long long* __restrict__ blk_voff,
                             SlotLayout L, uint2* desc, int* too_many) {
-  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (t >= nb * 36) return;
-  const size_t b = t / 36;
-  const int j = (int)(t - 36 * b);
+  const size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (b >= nb) return;
   const int c = lay_size(blk_lay[b]);
-  if (j >= c) return;
   const uint32_t cnt = blk_count[b];
   if (cnt >= (1u << 24)) atomicOr(too_many, 1);
   const uint64_t pm = blk_pmask[b];
-  const uint32_t inpat = (uint32_t)((pm >> j) & 1ull);
   const int cat = slot_cat(cnt);
-  unsigned long long at;
+  const unsigned long long voff = blk_voff[b];
+  const uint32_t hi = (cnt & 0xffffffu) | ((uint32_t)c << 24);
   if (cat == 0) {
-    if (inpat) return;  // gathered straight from the scratch
-    at = L.off[0] + L.base[b] + (unsigned long long)__popcll(~pm & ((1ull << j) - 1ull));
+    // one contribution: pattern entries are gathered straight from the scratch; the others get a check
+    unsigned long long at = L.off[0] + L.base[b];
+    for (int j = 0; j < c; ++j)
+      if (!((pm >> j) & 1ull)) desc[at++] = make_uint2((uint32_t)(voff + (unsigned long long)j), hi);
   } else {
-    at = L.off[cat] + L.base[(size_t)cat * L.stride + b] + (unsigned long long)j;
+    const unsigned long long at = L.off[cat] + L.base[(size_t)cat * L.stride + b];
+    for (int j = 0; j < c; ++j)
+      desc[at + j] = make_uint2((uint32_t)(voff + (unsigned long long)j), hi | ((uint32_t)((pm >> j) & 1ull) << 31));
   }
-  desc[at] = make_uint2((uint32_t)(blk_voff[b] + (unsigned long long)j), (cnt & 0xffffffu) | ((uint32_t)c << 24) |
-                                                                              (inpat << 31));
 }
 
 // Numeric pass, part 1: one thread per descriptor.  Slots in S (descriptors
@@ -1274,7 +1242,7 @@ struct fem_gpu {
   DevBuf<double> V;
   DevBuf<uint32_t> blk_start, blk_count;
   DevBuf<uint64_t> blk_mask, blk_maskT;
-  DevBuf<int32_t> blk_I, blk_J, blk_colpos;
+  DevBuf<int32_t> blk_I, blk_J;
   DevBuf<int64_t> row_ptr;
   DevBuf<int32_t> col_idx;
   DevBuf<double> values;
@@ -1405,7 +1373,7 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
                          &h->p_E, &h->p_nu, &h->p_t, &h->p_ks, &h->V, &h->values};
   for (auto* b : d) b->release();
   DevBuf<int32_t>* i[] = {&h->t_n1, &h->t_n2, &h->b_n1, &h->b_n2, &h->p_n1, &h->p_n2, &h->p_n3, &h->p_n4,
-                          &h->blk_I, &h->blk_J, &h->blk_colpos, &h->col_idx, &h->g_row, &h->g_col, &h->nnz_group};
+                          &h->blk_I, &h->blk_J, &h->col_idx, &h->g_row, &h->g_col, &h->nnz_group};
   for (auto* b : i) b->release();
   h->slot_t.release();
   h->slot_b.release();
@@ -2281,7 +2249,6 @@ int symbolic(fem_gpu* h) {
   CK(h->blk_maskT.reserve(nb, s));
   CK(h->blk_I.reserve(nb, s));
   CK(h->blk_J.reserve(nb, s));
-  CK(h->blk_colpos.reserve(nb * 12, s));
   k_block_starts<<<grid_for(np, 256), 256, 0, s>>>(incl.p, np, h->blk_start.p);
   DevBuf<uint32_t> adj_n, adj_off;
   CK(adj_n.reserve(nb, s));
@@ -2348,7 +2315,7 @@ int symbolic(fem_gpu* h) {
   CK(cudaMemsetAsync(gcount.p, 0, (nn + 1) * sizeof(int64_t), s));
   k_row_segments<<<grid_for(na, 256), 256, 0, s>>>(sakeys.p, na, seg_b.p, seg_e.p);
   k_row_counts<<<grid_for(nn, 128), 128, 0, s>>>(nn, seg_b.p, seg_e.p, savals.p, h->blk_mask.p, h->blk_maskT.p,
-                                                 h->blk_colpos.p, row_nnz.p, gcount.p);
+                                                 row_nnz.p, gcount.p);
   st = cub_call(h, [&](void* tmp, size_t& bytes) {
     return cub::DeviceScan::ExclusiveSum(tmp, bytes, row_nnz.p, h->row_ptr.p, (int64_t)(nrows + 1), s);
   });
@@ -2366,14 +2333,11 @@ int symbolic(fem_gpu* h) {
   CK(h->col_idx.reserve(nnz + 1, s));
   CK(h->values.reserve(nnz + 1, s));
   CK(h->nnz_group.reserve(nnz + 1, s));
+  CK(h->src_map.reserve(nnz + 1, s));
   CK(h->g_row.reserve(ng + 1, s));
   CK(h->g_col.reserve(ng + 1, s));
   CK(h->g_kind.reserve(ng + 1, s));
-  k_row_fill<<<grid_for(nn, 128), 128, 0, s>>>(nn, seg_b.p, seg_e.p, sakeys.p, savals.p, h->blk_mask.p,
-                                               h->blk_maskT.p, h->blk_colpos.p, h->row_ptr.p, gbase.p, h->col_idx.p,
-                                               h->nnz_group.p, h->g_row.p, h->g_col.p, h->g_kind.p);
-  CK(cudaGetLastError());
-  // block-sum slots by contribution count, their descriptors and the source of every CSR entry
+  // block-sum slots by contribution count, their descriptors, then the CSR rows with the source of every entry
   {
     const size_t st_ = nb + 1;
     DevBuf<unsigned long long> sz;
@@ -2410,14 +2374,14 @@ int symbolic(fem_gpu* h) {
     L.stride = st_;
     for (int g = 0; g < kSlotCats; ++g) L.off[g] = h->slot_off[g];
     L.vs_off = h->vs_off;
-    CK(h->src_map.reserve(nnz + 1, s));
-    k_csr_sources<<<grid_for(nb * 36, 256), 256, 0, s>>>(nb, h->blk_mask.p, h->blk_maskT.p, h->blk_lay.p,
-                                                         h->blk_count.p, h->blk_voff.p, L, h->blk_I.p, h->blk_J.p,
-                                                         h->blk_colpos.p, h->row_ptr.p, h->src_map.p);
     CK(h->slot_desc.reserve(h->n_desc + 1, s));
     CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), s));
-    k_slot_desc<<<grid_for(nb * 36, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_pmask.p, h->blk_lay.p,
-                                                       h->blk_voff.p, L, h->slot_desc.p, h->flag.p);
+    k_slot_desc<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_pmask.p, h->blk_lay.p, h->blk_voff.p, L,
+                                                  h->slot_desc.p, h->flag.p);
+    k_row_fill<<<grid_for(nrows, 128), 128, 0, s>>>(nrows, seg_b.p, seg_e.p, sakeys.p, savals.p, h->blk_mask.p,
+                                                    h->blk_maskT.p, h->blk_lay.p, h->blk_count.p, h->blk_voff.p, L,
+                                                    h->row_ptr.p, gbase.p, h->col_idx.p, h->nnz_group.p,
+                                                    h->src_map.p, h->g_row.p, h->g_col.p, h->g_kind.p);
     CK(cudaGetLastError());
     int too_many = 0;
     CK(cudaMemcpyAsync(&too_many, h->flag.p, sizeof too_many, cudaMemcpyDeviceToHost, s));
