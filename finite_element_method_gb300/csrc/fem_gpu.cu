@@ -652,23 +652,34 @@ struct SlotLayout {
 };
 
 // position of a block entry in its packing (-1: not packed)
+// (the packed entries are listed in ascending entry order, so the position is the number of set entries below)
 __device__ __forceinline__ int packed_pos(uint32_t lay, int en) {
   if (lay == kLayFull) return en;
-  const int n = lay_size(lay);
-  int p = -1;
-  for (int q = 0; q < n; ++q)
-    if (c_lay_en[lay][q] == en) p = q;
-  return p;
+  const uint64_t set = lay == kLayDiag14 ? kSetDiag14 : kSetOff13;
+  return ((set >> en) & 1ull) ? __popcll(set & ((1ull << en) - 1ull)) : -1;
 }
 
-// Symbolic, once per pattern: CSR row 6r + a, one thread per row.  Walking the
-// row node's adjacency (its blocks in column-node order) it writes, in column
-// order, every entry's column, stiffness group and value source: the scratch
-// position of a block with one contribution, else the entry's block-sum slot
-// in S (both in one buffer: S starts at vs_off).  A block stored with the row
-// node second (t = 1) is read transposed.  The a = 0 thread of each node also
-// writes the node's groups.
-__global__ void k_row_fill(size_t n_rows, const int32_t* __restrict__ seg_begin, const int32_t* __restrict__ seg_end,
+// inclusive prefix sum over the lanes of a warp
+__device__ __forceinline__ int warp_inclusive_sum(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, v, d);
+    if (lane >= d) v += u;
+  }
+  return v;
+}
+
+// Symbolic, once per pattern: the CSR rows of a node, one warp per node.  Lane
+// k takes the k-th block of the node's adjacency (blocks in column-node order,
+// 32 at a time); for each of the node's 6 rows a warp prefix sum of the
+// blocks' entry counts gives every lane the place of its entries, which it
+// writes in column order: column, stiffness group and value source (the
+// scratch position of a block with one contribution, else the entry's
+// block-sum slot in S -- both in one buffer, S starting at vs_off).  A block
+// stored with the row node second (t = 1) is read transposed.  The node's
+// groups are placed the same way.
+__global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin, const int32_t* __restrict__ seg_end,
                            const uint64_t* __restrict__ akeys, const uint32_t* __restrict__ avals,
                            const uint64_t* __restrict__ blk_mask, const uint64_t* __restrict__ blk_maskT,
                            const uint8_t* __restrict__ blk_lay, const uint32_t* __restrict__ blk_count,
@@ -677,43 +688,65 @@ __global__ void k_row_fill(size_t n_rows, const int32_t* __restrict__ seg_begin,
                            int32_t* __restrict__ col_idx, int32_t* __restrict__ nnz_group,
                            uint32_t* __restrict__ src_map, int32_t* __restrict__ g_row, int32_t* __restrict__ g_col,
                            uint8_t* __restrict__ g_kind) {
-  const size_t row = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (row >= n_rows) return;
-  const size_t r = row / 6;
-  const int a = (int)(row - 6 * r);
+  const size_t r = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (r >= n_nodes) return;
   const int32_t s = seg_begin[r], e = seg_end[r];
-  int64_t g = gbase[r];
-  int64_t pos = row_ptr[row];
-  for (int32_t k = s; k < e && s >= 0; ++k) {
-    const uint32_t v = avals[k];
-    const uint32_t b = v >> 1, t = v & 1u;
-    const uint32_t J = (uint32_t)(akeys[k] & 0xffffffffu);
-    const uint64_t m = t ? blk_maskT[b] : blk_mask[b];
+  if (s < 0) return;
+  int64_t gnext = gbase[r];
+  int64_t next[6];
+#pragma unroll
+  for (int a = 0; a < 6; ++a) next[a] = row_ptr[6 * r + a];
+  for (int32_t k0 = s; k0 < e; k0 += 32) {
+    const int32_t k = k0 + lane;
+    uint64_t m = 0;
+    uint32_t J = 0, lay = 0, t = 0;
+    unsigned long long sb = 0;
+    if (k < e) {
+      const uint32_t v = avals[k];
+      const uint32_t b = v >> 1;
+      t = v & 1u;
+      J = (uint32_t)(akeys[k] & 0xffffffffu);
+      m = t ? blk_maskT[b] : blk_mask[b];
+      lay = blk_lay[b];
+      const int cat = slot_cat(blk_count[b]);
+      sb = cat == 0 ? blk_voff[b] : L.vs_off + L.off[cat] + L.base[(size_t)cat * L.stride + b];
+    }
+    // groups
     const uint32_t km = kinds_of(m);
-    int32_t kg[4] = {-1, -1, -1, -1};
-    for (int kd = 0; kd < 4; ++kd)
+    const int ng = __popc(km);
+    const int gin = warp_inclusive_sum(ng);
+    int64_t g = gnext + gin - ng;
+    int32_t kg[4];
+#pragma unroll
+    for (int kd = 0; kd < 4; ++kd) {
+      kg[kd] = -1;
       if (km & (1u << kd)) {
-        if (a == 0) {
-          g_row[g] = (int32_t)r;
-          g_col[g] = (int32_t)J;
-          g_kind[g] = (uint8_t)kd;
-        }
+        g_row[g] = (int32_t)r;
+        g_col[g] = (int32_t)J;
+        g_kind[g] = (uint8_t)kd;
         kg[kd] = (int32_t)g;
         ++g;
       }
-    const uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
-    if (!rowbits) continue;
-    const uint32_t lay = blk_lay[b];
-    const int cat = slot_cat(blk_count[b]);
-    const unsigned long long sb =
-        cat == 0 ? blk_voff[b] : L.vs_off + L.off[cat] + L.base[(size_t)cat * L.stride + b];
-    for (int c = 0; c < 6; ++c)
-      if (rowbits & (1u << c)) {
-        col_idx[pos] = (int32_t)(6 * J + c);
-        nnz_group[pos] = kg[2 * (a / 3) + c / 3];
-        src_map[pos] = (uint32_t)(sb + (unsigned long long)packed_pos(lay, t ? 6 * c + a : 6 * a + c));
-        ++pos;
-      }
+    }
+    gnext += __shfl_sync(0xffffffffu, gin, 31);
+    // rows
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+      const uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
+      const int cnt = __popc(rowbits);
+      const int inc = warp_inclusive_sum(cnt);
+      int64_t pos = next[a] + inc - cnt;
+#pragma unroll
+      for (int c = 0; c < 6; ++c)
+        if (rowbits & (1u << c)) {
+          col_idx[pos] = (int32_t)(6 * J + c);
+          nnz_group[pos] = kg[2 * (a / 3) + c / 3];
+          src_map[pos] = (uint32_t)(sb + (unsigned long long)packed_pos(lay, t ? 6 * c + a : 6 * a + c));
+          ++pos;
+        }
+      next[a] += __shfl_sync(0xffffffffu, inc, 31);
+    }
   }
 }
 
@@ -2378,7 +2411,7 @@ int symbolic(fem_gpu* h) {
     CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), s));
     k_slot_desc<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_pmask.p, h->blk_lay.p, h->blk_voff.p, L,
                                                   h->slot_desc.p, h->flag.p);
-    k_row_fill<<<grid_for(nrows, 128), 128, 0, s>>>(nrows, seg_b.p, seg_e.p, sakeys.p, savals.p, h->blk_mask.p,
+    k_row_fill<<<grid_for(nn * 32, 256), 256, 0, s>>>(nn, seg_b.p, seg_e.p, sakeys.p, savals.p, h->blk_mask.p,
                                                     h->blk_maskT.p, h->blk_lay.p, h->blk_count.p, h->blk_voff.p, L,
                                                     h->row_ptr.p, gbase.p, h->col_idx.p, h->nnz_group.p,
                                                     h->src_map.p, h->g_row.p, h->g_col.p, h->g_kind.p);
