@@ -343,6 +343,48 @@ def run_separate(args):
     print(json.dumps(line), flush=True)
 
 
+def run_loads(args):
+    """A uniformly distributed surface load on every plate of the 1000 x 1000 mesh (1 M loads, 4 M nodal
+    contributions): the GPU conversion and call-ordered summation into the forces vector, against the
+    CPU restatement on a 100,000-plate sample."""
+    import torch
+
+    from oracle.loads import forces_vector
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    mesh = meshes.plate_mesh(args.nx, args.nx)
+    n = len(mesh.plates["numbers"])
+    dofs = np.full(n, 2, np.uint8)
+    q = np.random.default_rng(7).uniform(-2e3, -1e3, n)
+    ms = []
+    with ClockSampler(0) as clocks:
+        for it in range(args.warmup + args.steps):
+            g = FEM(meshes.REL_TOL, meshes.ABS_TOL, mesh.nodes_number)
+            meshes.load(g, mesh)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            g.add_uniformly_distributed_surface_loads(mesh.plates["numbers"], dofs, q)
+            f = g.forces_vector()
+            if it >= args.warmup:
+                ms.append((time.perf_counter() - t0) * 1e3)
+            g.close()
+    t = float(np.median(ms))
+    k = min(n, 100000)
+    pn = mesh.plates["nodes"].astype(np.int64) - 1
+    t0 = time.perf_counter()
+    forces_vector(mesh.nodes_number, mesh.xyz, [("surface", i, 2, q[i]) for i in range(k)], plate_nodes=pn)
+    t_cpu = time.perf_counter() - t0
+    line = {"metric": "surface loads converted and summed into the forces vector per second", "value": n / (t * 1e-3),
+            "unit": "loads/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"plate_mesh_{args.nx}x{args.nx}: one surface load (Z) per plate, {n:,} loads",
+                       "timing": "host wall time of the bulk call and the forces read-back (6 M doubles)"},
+            "cpu_baseline": {"value": k / t_cpu, "unit": "loads/s", "cores": 1, "kind": "port",
+                             "sample": f"the first {k:,} loads, Python loop over the C element restatement"},
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def ptr_u8(a):
     import ctypes
 
@@ -355,7 +397,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="plate", choices=["plate", "beam", "truss", "batch", "adjoint", "separate"])
+    ap.add_argument("--workload", default="plate", choices=["plate", "beam", "truss", "batch", "adjoint", "separate", "loads"])
     ap.add_argument("--pairs", type=int, default=64, help="(u, lambda) pairs of the adjoint workload")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--nx", type=int, default=1000, help="plate mesh size (nx x nx); 1000 is the full workload")
@@ -375,6 +417,9 @@ def main():
         return
     if args.workload == "separate":
         run_separate(args)
+        return
+    if args.workload == "loads":
+        run_loads(args)
         return
 
     import torch

@@ -60,6 +60,11 @@ SIGNATURES = {
     "fem_gpu_batch_last_ms": (c_int, [hp, fp]),
     "fem_gpu_batch_autotune": (c_int, [hp, c_int, c_char_p, c_char_p, c_size_t]),
     "fem_gpu_batch_configure": (c_int, [hp, c_int, c_int, c_int, c_int, c_int, c_int, c_int]),
+    "fem_gpu_add_concentrated_loads": (c_int, [hp, u32p, u8p, dp, c_size_t, szp]),
+    "fem_gpu_add_line_loads": (c_int, [hp, u32p, u8p, dp, c_size_t, szp]),
+    "fem_gpu_add_surface_loads": (c_int, [hp, u32p, u8p, dp, c_size_t, szp]),
+    "fem_gpu_get_forces": (c_int, [hp, dp]),
+    "fem_gpu_get_forces_device": (c_int, [hp, POINTER(c_void_p)]),
     "fem_gpu_separate_sparse": (c_int, [hp, u8p]),
     "fem_gpu_get_separation_sizes": (c_int, [hp, i64p, i64p, i64p]),
     "fem_gpu_get_separation_indexes": (c_int, [hp, i64p, i64p]),

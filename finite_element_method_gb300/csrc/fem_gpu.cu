@@ -1242,6 +1242,11 @@ struct fem_gpu {
   PartTable p_sets;  // sorted node-number set hash -> element index
   DevBuf<int32_t> p_n1, p_n2, p_n3, p_n4;
   DevBuf<double> p_E, p_nu, p_t, p_ks;
+  // loads: nodal contributions (DOF, value) in call order and the forces vector they sum to
+  DevBuf<unsigned long long> ld_key;
+  DevBuf<double> ld_val, forces;
+  size_t n_ld = 0;
+  bool forces_valid = false;
   // sparse separation (K_aa, K_ab, K_ba, K_bb)
   bool sep_valid = false;
   DevBuf<uint8_t> sep_imposed, sep_cls;
@@ -1438,6 +1443,9 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   h->vjp_inc.release();
   h->vstatus.release();
   h->vfirst.release();
+  h->ld_key.release();
+  h->ld_val.release();
+  h->forces.release();
   h->sep_imposed.release();
   h->sep_cls.release();
   h->sep_u32.release();
@@ -2668,3 +2676,5 @@ extern "C" int fem_gpu_last_numeric_timing(fem_gpu_t* h, float* element_ms, floa
 #include "fem_adjoint.cuh"
 // sparse separation of the assembled stiffness by the imposed displacements
 #include "fem_separate.cuh"
+// concentrated, line and surface loads and the forces vector
+#include "fem_loads.cuh"

@@ -288,6 +288,56 @@ class FEM:
         imp[k] = 1
         self._displacements[k] = value
 
+    def _dof(self, dof_parameter):
+        return dof_parameter if isinstance(dof_parameter, (int, np.integer)) else self.DOF_PARAMETERS.index(dof_parameter)
+
+    def _loads(self, fn, numbers, dofs, values) -> int:
+        numbers = _u32(numbers, (-1,))
+        m = len(numbers)
+        d = np.ascontiguousarray(np.broadcast_to(np.asarray([self._dof(x) for x in np.atleast_1d(dofs)]
+                                                            if np.asarray(dofs).dtype.kind in "OU"
+                                                            else np.asarray(dofs), dtype=np.uint8), (m,)))
+        v = _f64(values, m)
+        n = c_size_t(0)
+        self._check(fn(self._h, ptr(numbers, c_uint32), ptr(d, c_uint8), ptr(v, c_double), m, ctypes.byref(n)))
+        return n.value
+
+    def add_concentrated_load(self, node_number: int, dof_parameter, value: float) -> None:
+        """add_concentrated_load (methods_for_bc_data_handle.rs:30-56)"""
+        self.add_concentrated_loads([node_number], [self._dof(dof_parameter)], [value])
+
+    def add_concentrated_loads(self, node_numbers, dofs, values) -> int:
+        return self._loads(self._L.fem_gpu_add_concentrated_loads, node_numbers, dofs, values)
+
+    def add_uniformly_distributed_line_load(self, beam_number: int, dof_parameter, value: float) -> None:
+        """add_uniformly_distributed_line_load (methods_for_bc_data_handle.rs:58-101)"""
+        self.add_uniformly_distributed_line_loads([beam_number], [self._dof(dof_parameter)], [value])
+
+    def add_uniformly_distributed_line_loads(self, beam_numbers, dofs, values) -> int:
+        return self._loads(self._L.fem_gpu_add_line_loads, beam_numbers, dofs, values)
+
+    def add_uniformly_distributed_surface_load(self, plate_number: int, dof_parameter, value: float) -> None:
+        """add_uniformly_distributed_surface_load (methods_for_bc_data_handle.rs:103-175)"""
+        self.add_uniformly_distributed_surface_loads([plate_number], [self._dof(dof_parameter)], [value])
+
+    def add_uniformly_distributed_surface_loads(self, plate_numbers, dofs, values) -> int:
+        return self._loads(self._L.fem_gpu_add_surface_loads, plate_numbers, dofs, values)
+
+    def forces_vector(self):
+        """the forces vector (6 * nodes_number, DOF order): every load's nodal contributions summed in call order"""
+        f = np.zeros(6 * self.nodes_number)
+        self._check(self._L.fem_gpu_get_forces(self._h, ptr(f, c_double)))
+        return f
+
+    def compose_r_a_vector(self, k_aa_indexes):
+        """compose_r_a_vector (methods_for_separate_stiffness_matrix.rs:322-331): forces at the free DOFs"""
+        return self.forces_vector()[np.asarray(k_aa_indexes, np.int64)]
+
+    def compose_u_b_vector(self, k_bb_indexes):
+        """compose_u_b_vector (methods_for_separate_stiffness_matrix.rs:333-342): imposed displacements"""
+        self._imposed()
+        return self._displacements[np.asarray(k_bb_indexes, np.int64)].copy()
+
     def _imposed(self):
         if getattr(self, "_imposed_arr", None) is None:
             self._imposed_arr = np.zeros(6 * self.nodes_number, np.uint8)

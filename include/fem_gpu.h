@@ -65,6 +65,7 @@ enum {
   FEM_GPU_ERR_SEP_DISPLACEMENT = 22, /* "There are no stiffness to withstand displacement D applied to node N!" */
   FEM_GPU_ERR_SEP_NO_RESTRAINTS = 23, /* "No restraints" */
   FEM_GPU_ERR_SEP_EMPTY_KAA = 24,  /* "Sparse separation: K_aa is empty (structure has no free stiffness?)" */
+  FEM_GPU_ERR_ELEM_NOT_EXIST = 25, /* "<Kind> element with number N does not exist!" */
   FEM_GPU_ERR_ARGUMENT = 30,       /* null pointer / size out of range */
   FEM_GPU_ERR_STATE = 31,          /* e.g. CSR requested before fem_gpu_assemble */
   FEM_GPU_ERR_CUDA = 40,           /* CUDA runtime failure or no device */
@@ -203,6 +204,25 @@ int fem_gpu_batch_autotune(fem_gpu_batch_t* b, int reps, const char* cache_path,
 /* apply a configuration read back from that table */
 int fem_gpu_batch_configure(fem_gpu_batch_t* b, int persistent, int block, int ctas_per_sm, int tile_truss,
                             int tile_beam, int tile_plate, int sum_block);
+
+/* ---- loads ----------------------------------------------------------------
+ * add_concentrated_load, add_uniformly_distributed_line_load and
+ * add_uniformly_distributed_surface_load (methods_for_bc_data_handle.rs:20-175),
+ * bulk: loads in call order, stopping at the first whose node or element does
+ * not exist (FEM_GPU_ERR_NODE_NOT_EXIST / FEM_GPU_ERR_ELEM_NOT_EXIST with the
+ * reference's messages).  dofs[k] is the DOFParameter (0 X, 1 Y, 2 Z, 3 ThX,
+ * 4 ThY, 5 ThZ).  Element loads are converted to nodal loads with the element's
+ * geometry at the time of the call (beam.rs:775-797, plate.rs:1145-1185) and
+ * added, like the reference's `+=`, in call order. */
+int fem_gpu_add_concentrated_loads(fem_gpu_t* h, const uint32_t* node_numbers, const uint8_t* dofs,
+                                   const double* values, size_t n, size_t* n_added);
+int fem_gpu_add_line_loads(fem_gpu_t* h, const uint32_t* beam_numbers, const uint8_t* dofs, const double* values,
+                           size_t n, size_t* n_added);
+int fem_gpu_add_surface_loads(fem_gpu_t* h, const uint32_t* plate_numbers, const uint8_t* dofs, const double* values,
+                              size_t n, size_t* n_added);
+/* the forces vector (6 * nodes_number doubles, DOF order), to host or as a device pointer */
+int fem_gpu_get_forces(fem_gpu_t* h, double* forces);
+int fem_gpu_get_forces_device(fem_gpu_t* h, const double** forces);
 
 /* ---- sparse separation ----------------------------------------------------
  * separate_stiffness_matrix_sparse_iterative (methods_for_separate_stiffness_

@@ -692,6 +692,61 @@ static void rt_m_r(const double R[9], const double M[9], double out[9], int sym)
     }
 }
 
+/* equivalent nodal loads of a uniformly distributed line load q on a two-node
+ * element (beam.rs:775-797): one Gauss point r = 0, alpha = 2, h1 = h2 = 0.5,
+ * det J = L / 2 (bar_2n_element_functions.rs:35-83); out[i] = 0 + (h_i q) (detJ alpha) */
+int orc_beam_line_load(const double x1[3], const double x2[3], double q, double* out2) {
+  double d[3];
+  sub3(x2, x1, d);
+  const double L = norm3(d);
+  const double jac = L * 0.5;
+  const double h1 = 0.5 * (1.0 - 0.0), h2 = 0.5 * (1.0 + 0.0);
+  out2[0] = 0.0 + (h1 * q) * (jac * 2.0);
+  out2[1] = 0.0 + (h2 * q) * (jac * 2.0);
+  return ORC_OK;
+}
+
+/* equivalent nodal loads of a uniformly distributed surface load q on a plate
+ * (plate.rs:1145-1185): 2 x 2 Gauss points in the order of plate.rs:1066-1091,
+ * alpha_r = alpha_s = 1, h_i(r, s) = (0.25 (1 +- r)) (1 +- s)
+ * (quadrilateral_4n_element_functions.rs:585-611), det J(r, s) from the local
+ * coordinates (quad.rs:380-505) as det(4 J) / 16 -- the same determinant the
+ * stiffness uses; out[i] = sum over the points, in order, from 0. */
+int orc_plate_surface_load(const double x1[3], const double x2[3], const double x3[3], const double x4[3], double q,
+                           double rel_tol, double abs_tol, double* out4) {
+  double R[9];
+  int st = orc_plate_rotation(x2, x3, x4, rel_tol, abs_tol, R);
+  if (st) return st;
+  const double* X[4] = {x1, x2, x3, x4};
+  double xl[4] = {0, 0, 0, 0}, yl[4] = {0, 0, 0, 0};
+  for (int i = 0; i < 4; ++i) {
+    if (i == 2) continue;
+    double dd[3];
+    sub3(X[i], x3, dd);
+    xl[i] = (R[0] * dd[0] + R[1] * dd[1]) + R[2] * dd[2];
+    yl[i] = (R[3] * dd[0] + R[4] * dd[1]) + R[5] * dd[2];
+  }
+  const double g = plate_gauss_g();
+  const double ipr[4] = {g * 1.0, g * -1.0, g * -1.0, g * 1.0};
+  const double ips[4] = {g * 1.0, g * 1.0, g * -1.0, g * -1.0};
+  double x1l = xl[0], x2l = xl[1], x4l = xl[3];
+  double y1l = yl[0], y2l = yl[1], y4l = yl[3];
+  double d12x = x1l - x2l, d12y = y1l - y2l;
+  double ax = d12x + x4l, bx = d12x - x4l, cx = (x1l + x2l) - x4l;
+  double ay = d12y + y4l, by = d12y - y4l, cy = (y1l + y2l) - y4l;
+  for (int i = 0; i < 4; ++i) out4[i] = 0.0;
+  for (int ip = 0; ip < 4; ++ip) {
+    const double r = ipr[ip], s = ips[ip];
+    const double J00 = fma(s, bx, ax), J01 = fma(s, by, ay), J10 = fma(r, bx, cx), J11 = fma(r, by, cy);
+    const double detj = fma(J00, J11, -(J01 * J10)) * 0.0625;
+    const double w = (detj * 1.0) * 1.0;
+    const double h[4] = {(0.25 * (1.0 + r)) * (1.0 + s), (0.25 * (1.0 - r)) * (1.0 + s),
+                         (0.25 * (1.0 - r)) * (1.0 - s), (0.25 * (1.0 + r)) * (1.0 - s)};
+    for (int i = 0; i < 4; ++i) out4[i] = out4[i] + (h[i] * q) * w;
+  }
+  return ORC_OK;
+}
+
 int orc_plate_global_matrix(const double x1[3], const double x2[3], const double x3[3], const double x4[3],
                             double young, double poisson, double thickness, double shear_factor, double rel_tol,
                             double abs_tol, double* out576) {

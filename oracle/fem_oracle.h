@@ -111,6 +111,10 @@ int orc_truss_global_matrix(const double x1[3], const double x2[3], double young
 int orc_beam_global_matrix(const double x1[3], const double x2[3], double young, double poisson,
                            double area, double i11, double i22, double i12, double it, double shear_factor,
                            const double axis[3], double rel_tol, double abs_tol, double* out144);
+/* equivalent nodal loads (beam.rs:775-797, plate.rs:1145-1185) */
+int orc_beam_line_load(const double x1[3], const double x2[3], double q, double* out2);
+int orc_plate_surface_load(const double x1[3], const double x2[3], const double x3[3], const double x4[3], double q,
+                           double rel_tol, double abs_tol, double* out4);
 int orc_plate_global_matrix(const double x1[3], const double x2[3], const double x3[3], const double x4[3],
                             double young, double poisson, double thickness, double shear_factor,
                             double rel_tol, double abs_tol, double* out576);

@@ -62,6 +62,8 @@ def lib():
         L.orc_truss_rotation.argtypes = [dp, dp, c_double, c_double, dp]
         L.orc_beam_rotation.argtypes = [dp, dp, c_double, c_double, c_double, dp, c_double, c_double, dp, dp, dp]
         L.orc_plate_rotation.argtypes = [dp, dp, dp, c_double, c_double, dp]
+        L.orc_beam_line_load.argtypes = [dp, dp, c_double, dp]
+        L.orc_plate_surface_load.argtypes = [dp, dp, dp, dp, c_double, c_double, c_double, dp]
         for f in ("orc_sin", "orc_cos", "orc_atan", "orc_acos"):
             getattr(L, f).restype = c_double
             getattr(L, f).argtypes = [c_double]
@@ -221,6 +223,24 @@ def plate_global_matrix(x1, x2, x3, x4, young, poisson, thickness, shear_factor,
     if st:
         raise OracleError(st, "plate matrix failed")
     return out.reshape(24, 24)
+
+
+def beam_line_load(x1, x2, q):
+    """equivalent nodal loads of a uniformly distributed line load (beam.rs:775-797)"""
+    out = np.zeros(2)
+    a, b = _v3(x1), _v3(x2)
+    lib().orc_beam_line_load(_p(a, c_double), _p(b, c_double), q, _p(out, c_double))
+    return out
+
+
+def plate_surface_load(x1, x2, x3, x4, q, rel_tol=1e-12, abs_tol=1e-12):
+    """equivalent nodal loads of a uniformly distributed surface load (plate.rs:1145-1185)"""
+    out = np.zeros(4)
+    p = [_v3(x) for x in (x1, x2, x3, x4)]
+    st = lib().orc_plate_surface_load(*[_p(x, c_double) for x in p], q, rel_tol, abs_tol, _p(out, c_double))
+    if st:
+        raise OracleError(st, "plate load failed")
+    return out
 
 
 def beam_rotation(x1, x2, i11, i22, i12, axis, rel_tol=1e-12, abs_tol=1e-12):

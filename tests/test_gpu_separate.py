@@ -81,7 +81,7 @@ def test_plate_mesh_edge_fixed_and_tilted():
     edge = np.flatnonzero(m.xyz[:, 0] == 0.0)
     check_same(g, o, imposed_for(m, edge, range(6)))
     q, _ = np.linalg.qr(np.random.default_rng(7).normal(size=(3, 3)))
-    mt = meshes.plate_mesh(20, 20, rotation=q)
+    mt = meshes.plate_mesh(20, 20, size=3.0, rotation=q)
     gt, ot = build_pair(mt)
     check_same(gt, ot, imposed_for(mt, np.arange(0, 21 * 21, 21), range(6)))
 
