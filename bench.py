@@ -385,6 +385,53 @@ def run_loads(args):
     print(json.dumps(line), flush=True)
 
 
+def run_pcg(args):
+    """PCG (node-block Jacobi) on the separated 1000 x 1000 plate stiffness, all four edges restrained and a
+    surface load on every plate: a fixed number of iterations, timed per iteration."""
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    mesh = meshes.plate_mesh(args.nx, args.nx)
+    g = FEM(meshes.REL_TOL, meshes.ABS_TOL, mesh.nodes_number)
+    meshes.load(g, mesh)
+    g.assemble()
+    g.add_uniformly_distributed_surface_loads(mesh.plates["numbers"], np.full(len(mesh.plates["numbers"]), 2, np.uint8),
+                                              -1e3)
+    x, y = mesh.xyz[:, 0], mesh.xyz[:, 1]
+    edge = np.flatnonzero((x == 0.0) | (y == 0.0) | (x == x.max()) | (y == y.max()))
+    imp = np.zeros(6 * mesh.nodes_number, np.uint8)
+    for d in range(6):
+        imp[6 * edge + d] = 1
+    sep = g.separate_stiffness_matrix_sparse_iterative(imp)
+    r_a = g.compose_r_a_vector(sep.k_aa_indexes)
+    iters = args.pcg_iters
+    ms = []
+    for it in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        try:
+            g.find_ua_vector_iterative_pcg_block_jacobi_sparse(sep, r_a, None, iters)
+        except Exception as e:  # a fixed iteration count: the no-convergence status is expected
+            assert "no convergence" in str(e), e
+        if it >= args.warmup:
+            ms.append((time.perf_counter() - t0) * 1e3)
+    t = float(np.median(ms)) / iters
+    nnz = int(sep.blocks["k_aa"][0][-1])
+    n = sep.n_aa
+    traffic = nnz * 12 + (n + 1) * 8 + n * 8 * 9  # K_aa (values + columns + row starts) + the vector sweeps
+    gbs = traffic / (t * 1e-3) / 1e9
+    line = {"metric": "PCG iterations/s (block Jacobi, K_aa of the plate mesh)", "value": 1e3 / t, "unit": "iterations/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"plate_mesh_{args.nx}x{args.nx}, edges restrained: K_aa {n:,} DOFs, "
+                                   f"{nnz:,} entries; {iters} iterations per call",
+                       "timing": "host wall time of the call / iterations (one host synchronisation per iteration; set-up of the preconditioner included)"},
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": measured_peaks()[0], "unit": "GB/s",
+                         "frac": gbs / measured_peaks()[0], "traffic": None,
+                         "algorithmic": f"{traffic / 1e9:.2f} GB per iteration (SpMV + vector sweeps)"}}
+    print(json.dumps(line), flush=True)
+
+
 def ptr_u8(a):
     import ctypes
 
@@ -397,11 +444,12 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="plate", choices=["plate", "beam", "truss", "batch", "adjoint", "separate", "loads"])
+    ap.add_argument("--workload", default="plate", choices=["plate", "beam", "truss", "batch", "adjoint", "separate", "loads", "pcg"])
     ap.add_argument("--pairs", type=int, default=64, help="(u, lambda) pairs of the adjoint workload")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--nx", type=int, default=1000, help="plate mesh size (nx x nx); 1000 is the full workload")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--pcg-iters", type=int, default=200, help="PCG iterations per step of the pcg workload")
     ap.add_argument("--small", action="store_true",
                     help="profiling-sized batch (64 structures) and adjoint (21x21x5 frame + 200x200 slab) cases")
     args = ap.parse_args()
@@ -420,6 +468,9 @@ def main():
         return
     if args.workload == "loads":
         run_loads(args)
+        return
+    if args.workload == "pcg":
+        run_pcg(args)
         return
 
     import torch

@@ -65,6 +65,8 @@ SIGNATURES = {
     "fem_gpu_add_surface_loads": (c_int, [hp, u32p, u8p, dp, c_size_t, szp]),
     "fem_gpu_get_forces": (c_int, [hp, dp]),
     "fem_gpu_get_forces_device": (c_int, [hp, POINTER(c_void_p)]),
+    "fem_gpu_solve_pcg": (c_int, [hp, dp, dp, c_int, c_int, dp, POINTER(c_int)]),
+    "fem_gpu_reactions": (c_int, [hp, dp, dp, dp, dp]),
     "fem_gpu_separate_sparse": (c_int, [hp, u8p]),
     "fem_gpu_get_separation_sizes": (c_int, [hp, i64p, i64p, i64p]),
     "fem_gpu_get_separation_indexes": (c_int, [hp, i64p, i64p]),

@@ -1258,6 +1258,9 @@ struct fem_gpu {
   DevBuf<int32_t> sep_ci[4];
   DevBuf<double> sep_v[4];
   int64_t sep_n[2] = {0, 0}, sep_nnz[4] = {0, 0, 0, 0};
+  // PCG on K_aa: vectors, dot-product partials, preconditioner blocks and their inverses
+  DevBuf<double> pcg_vec, pcg_part, pcg_scal, pcg_inv;
+  DevBuf<uint32_t> pcg_blk;
   // validation scratch
   DevBuf<int> vstatus;
   DevBuf<unsigned long long> vfirst;
@@ -1446,6 +1449,8 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   h->ld_key.release();
   h->ld_val.release();
   h->forces.release();
+  for (DevBuf<double>* v : {&h->pcg_vec, &h->pcg_part, &h->pcg_scal, &h->pcg_inv}) v->release();
+  h->pcg_blk.release();
   h->sep_imposed.release();
   h->sep_cls.release();
   h->sep_u32.release();
@@ -2678,3 +2683,5 @@ extern "C" int fem_gpu_last_numeric_timing(fem_gpu_t* h, float* element_ms, floa
 #include "fem_separate.cuh"
 // concentrated, line and surface loads and the forces vector
 #include "fem_loads.cuh"
+// PCG solution of the separated system and the reactions
+#include "fem_solve.cuh"

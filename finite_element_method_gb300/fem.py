@@ -372,6 +372,35 @@ class FEM:
             blocks[name] = (rp, ci, va)
         return SeparatedStiffnessSparse(aa, bb, blocks)
 
+    def _pcg(self, sep, r_a_vector, u_b_vector, max_iter, block):
+        r_a = np.ascontiguousarray(r_a_vector, dtype=np.float64)
+        u_b = None if u_b_vector is None else np.ascontiguousarray(u_b_vector, dtype=np.float64)
+        assert r_a.shape == (sep.n_aa,) and (u_b is None or u_b.shape == (sep.n_bb,))
+        u_a = np.zeros(sep.n_aa)
+        it = c_int(0)
+        self._check(self._L.fem_gpu_solve_pcg(self._h, ptr(r_a, c_double), None if u_b is None else ptr(u_b, c_double),
+                                              int(block), int(max_iter), ptr(u_a, c_double), ctypes.byref(it)))
+        return u_a, it.value
+
+    def find_ua_vector_iterative_pcg_jacobi_sparse(self, sep, r_a_vector, u_b_vector, max_iter):
+        """find_ua_vector_iterative_pcg_jacobi_sparse (methods_for_global_analysis.rs:189-233) on the GPU, for the
+        separation `sep` of this model's last separate_stiffness_matrix_sparse_iterative: (u_a, iterations)"""
+        return self._pcg(sep, r_a_vector, u_b_vector, max_iter, False)
+
+    def find_ua_vector_iterative_pcg_block_jacobi_sparse(self, sep, r_a_vector, u_b_vector, max_iter):
+        """find_ua_vector_iterative_pcg_block_jacobi_sparse (methods_for_global_analysis.rs:235-275): node blocks"""
+        return self._pcg(sep, r_a_vector, u_b_vector, max_iter, True)
+
+    def find_r_r_vector_sparse(self, sep, u_a_vector, u_b_vector):
+        """find_r_r_vector_sparse (methods_for_global_analysis.rs:293-330): reactions K_ba u_a + K_bb u_b - r_b"""
+        u_a = np.ascontiguousarray(u_a_vector, dtype=np.float64)
+        u_b = np.ascontiguousarray(u_b_vector, dtype=np.float64)
+        r_b = np.ascontiguousarray(self.forces_vector()[np.asarray(sep.k_bb_indexes, np.int64)])
+        r_r = np.zeros(sep.n_bb)
+        self._check(self._L.fem_gpu_reactions(self._h, ptr(u_a, c_double), ptr(u_b, c_double), ptr(r_b, c_double),
+                                              ptr(r_r, c_double)))
+        return r_r
+
     def vjp_last_ms(self) -> float:
         x = c_float(0)
         self._check(self._L.fem_gpu_vjp_last_ms(self._h, ctypes.byref(x)))

@@ -66,6 +66,7 @@ enum {
   FEM_GPU_ERR_SEP_NO_RESTRAINTS = 23, /* "No restraints" */
   FEM_GPU_ERR_SEP_EMPTY_KAA = 24,  /* "Sparse separation: K_aa is empty (structure has no free stiffness?)" */
   FEM_GPU_ERR_ELEM_NOT_EXIST = 25, /* "<Kind> element with number N does not exist!" */
+  FEM_GPU_ERR_NOT_CONVERGED = 26,  /* fem_gpu_solve_pcg: "find_ua_vector_iterative: PCG failed: ..." */
   FEM_GPU_ERR_ARGUMENT = 30,       /* null pointer / size out of range */
   FEM_GPU_ERR_STATE = 31,          /* e.g. CSR requested before fem_gpu_assemble */
   FEM_GPU_ERR_CUDA = 40,           /* CUDA runtime failure or no device */
@@ -245,6 +246,22 @@ int fem_gpu_get_separation_indexes(fem_gpu_t* h, int64_t* aa_indexes, int64_t* b
 int fem_gpu_get_separation_block(fem_gpu_t* h, int which, int64_t* row_ptr, int32_t* col_idx, double* values);
 int fem_gpu_get_separation_block_device(fem_gpu_t* h, int which, const int64_t** row_ptr, const int32_t** col_idx,
                                         const double** values);
+
+/* ---- solution -------------------------------------------------------------
+ * find_ua_vector_iterative_pcg_jacobi_sparse / ..._block_jacobi_sparse
+ * (methods_for_global_analysis.rs:189-275) on the separation of the last
+ * fem_gpu_separate_sparse: b = r_a - K_ab u_b, then K_aa u_a = b by
+ * preconditioned conjugate gradients from u_a = 0 with the diagonal of K_aa
+ * (block_jacobi = 0) or its node blocks (1) as preconditioner, stopping when
+ * ||r||_2 <= max(rel_tol ||b||_2, abs_tol) (the handle's tolerances) or after
+ * max_iter iterations (FEM_GPU_ERR_NOT_CONVERGED).  r_a: n_aa host doubles (the
+ * forces at the free DOFs), u_b: n_bb (imposed displacements; NULL = 0), u_a:
+ * n_aa out; *iterations: the iterations run. */
+int fem_gpu_solve_pcg(fem_gpu_t* h, const double* r_a, const double* u_b, int block_jacobi, int max_iter,
+                      double* u_a, int* iterations);
+/* find_r_r_vector_sparse (methods_for_global_analysis.rs:100-133, :293-330): the reactions at the restrained
+ * DOFs, r_r = K_ba u_a + K_bb u_b - r_b (host arrays; u_b, r_b NULL = 0) */
+int fem_gpu_reactions(fem_gpu_t* h, const double* u_a, const double* u_b, const double* r_b, double* r_r);
 
 /* Dense assembly of one small structure without any device allocation.
  * No counterpart in the reference: it serves callers that cannot call
