@@ -432,6 +432,94 @@ def run_pcg(args):
     print(json.dumps(line), flush=True)
 
 
+# Algorithmic FP64 work per plate of the element-results kernel (k_plate_results, flat mesh: R = I), counted
+# from its formulation (FMA = 2 flops, add / mul / div / sqrt = 1): normal 15, local coordinates 39, local
+# fields 100, edge vectors, lengths, differences and tying values 72, corner determinants 12 and their shared
+# reciprocal 12, edge weights 24, strain sums 58, shear sums 18, material constants 20, results 18.
+RESULTS_FLOPS_PER_PLATE = 15 + 39 + 100 + 72 + 12 + 12 + 24 + 58 + 18 + 20 + 18
+# bytes per plate the kernel must move: connectivity 16 + properties 32 + results 64, and per node (about one
+# per plate in the 1000 x 1000 mesh) coordinates 24 + displacements 48
+RESULTS_BYTES = dict(per_plate=16 + 32 + 64, per_node=24 + 48)
+
+
+def run_results(args):
+    """Element results (membrane forces, bending moments, shear forces) of every plate of the 1000 x 1000 mesh
+    from a displacements vector: device-resident kernel time (`value`), the host API end to end (`e2e`), and
+    the CPU restatement on all host threads."""
+    import torch
+
+    from oracle import fem_oracle as fo
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    mesh = meshes.plate_mesh(args.nx, args.nx)
+    n_pl, n_nd = len(mesh.plates["numbers"]), mesh.nodes_number
+    g = FEM(meshes.REL_TOL, meshes.ABS_TOL, n_nd)
+    meshes.load(g, mesh)
+    disp = np.random.default_rng(17).standard_normal(6 * n_nd) * 1e-3
+    d_disp = torch.from_numpy(disp).cuda()
+    d_out = torch.empty((n_pl, 8), dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # larger than the 129 MB L2
+    ms = []
+    with ClockSampler(dev) as clocks:
+        for it in range(args.warmup + args.steps):
+            flush.fill_(it & 0xFF)
+            torch.cuda.synchronize()
+            g.element_results_device(d_disp.data_ptr(), 0, 0, d_out.data_ptr())
+            torch.cuda.synchronize()
+            if it >= args.warmup:
+                ms.append(g.results_last_ms())
+    t = float(np.mean(ms))
+    # end to end through the host API: pinned displacements in, pinned results out
+    h_disp = torch.empty(6 * n_nd, dtype=torch.float64, pin_memory=True).numpy()
+    h_disp[:] = disp
+    h_out = {"truss": torch.empty((0, 1), dtype=torch.float64, pin_memory=True).numpy(),
+             "beam": torch.empty((0, 10), dtype=torch.float64, pin_memory=True).numpy(),
+             "plate": torch.empty((n_pl, 8), dtype=torch.float64, pin_memory=True).numpy()}
+    e2e_ms = []
+    for it in range(max(args.warmup, 3) + args.steps):
+        flush.fill_(it & 0xFF)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.element_results(h_disp, out=h_out)
+        if it >= max(args.warmup, 3):
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    t_e2e = float(np.median(e2e_ms))
+    ok = bool(np.array_equal(h_out["plate"], d_out.cpu().numpy()))
+    line = {"metric": "plate element results per second", "value": n_pl / (t * 1e-3), "unit": "elements/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"plate_mesh_{args.nx}x{args.nx}: {n_pl:,} plates, {n_nd:,} nodes, random "
+                                   "displacements (N(0, 1e-3), seed 17)",
+                       "timing": "CUDA events around the result kernel on the model's stream; L2 flushed (256 MB "
+                                 "write) before every step", "host_and_device_agree": ok},
+            "e2e": {"value": n_pl / (t_e2e * 1e-3), "unit": "elements/s", "ms_per_step": t_e2e,
+                    "h2d_bytes_per_step": 8 * 6 * n_nd, "d2h_bytes_per_step": 8 * 8 * n_pl,
+                    "api": "FEM.element_results (fem_gpu_element_results), pinned host buffers"},
+            "gpu_launches": args.steps}
+    fl = RESULTS_FLOPS_PER_PLATE * n_pl / (t * 1e-3)
+    by = (RESULTS_BYTES["per_plate"] * n_pl + RESULTS_BYTES["per_node"] * n_nd) / (t * 1e-3) / 1e9
+    hbm = measured_peaks()[0]
+    line["roofline"] = {"bound": "fp64", "achieved": fl / 1e12, "peak": FP64_PEAK_FLOPS / 1e12, "unit": "TFLOP/s",
+                        "frac": fl / FP64_PEAK_FLOPS, "traffic": None,
+                        "algorithmic": f"{RESULTS_FLOPS_PER_PLATE} flops per plate (FMA = 2); "
+                                       f"{by:.0f} GB/s of algorithmic bytes = {by / hbm:.3f} of measured HBM",
+                        "peak_source": "2 DFMA/clk/SM x 152 SMs x 2070 MHz"}
+    line["clocks"] = clocks.summary()
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        secs = []
+        for _ in range(3):
+            out, sec = fo.element_results(mesh, disp, n_threads=threads)
+            secs.append(sec)
+        line["cpu_baseline"] = {"value": n_pl / min(secs), "unit": "elements/s", "cores": threads, "kind": "port",
+                                "sample": f"all {n_pl:,} plates, C restatement (oracle) on {threads} threads, "
+                                          "best of 3",
+                                "matches_gpu": bool(np.array_equal(out["plate"], h_out["plate"]))}
+    print(json.dumps(line), flush=True)
+    g.close()
+
+
 def ptr_u8(a):
     import ctypes
 
@@ -444,7 +532,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="plate", choices=["plate", "beam", "truss", "batch", "adjoint", "separate", "loads", "pcg"])
+    ap.add_argument("--workload", default="plate", choices=["plate", "beam", "truss", "batch", "adjoint", "separate", "loads", "pcg",
+                                                         "results"])
     ap.add_argument("--pairs", type=int, default=64, help="(u, lambda) pairs of the adjoint workload")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--nx", type=int, default=1000, help="plate mesh size (nx x nx); 1000 is the full workload")
@@ -468,6 +557,9 @@ def main():
         return
     if args.workload == "loads":
         run_loads(args)
+        return
+    if args.workload == "results":
+        run_results(args)
         return
     if args.workload == "pcg":
         run_pcg(args)

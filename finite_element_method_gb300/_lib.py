@@ -67,6 +67,10 @@ SIGNATURES = {
     "fem_gpu_get_forces_device": (c_int, [hp, POINTER(c_void_p)]),
     "fem_gpu_solve_pcg": (c_int, [hp, dp, dp, c_int, c_int, dp, POINTER(c_int)]),
     "fem_gpu_reactions": (c_int, [hp, dp, dp, dp, dp]),
+    "fem_gpu_element_results": (c_int, [hp, dp, c_size_t, dp, dp, dp]),
+    "fem_gpu_element_results_device": (c_int, [hp, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fem_gpu_results_last_ms": (c_int, [hp, POINTER(c_float)]),
+    "fem_gpu_get_element_numbers": (c_int, [hp, c_int, u32p]),
     "fem_gpu_separate_sparse": (c_int, [hp, u8p]),
     "fem_gpu_get_separation_sizes": (c_int, [hp, i64p, i64p, i64p]),
     "fem_gpu_get_separation_indexes": (c_int, [hp, i64p, i64p]),

@@ -1301,6 +1301,10 @@ struct fem_gpu {
   DevBuf<double> vjp_in, vjp_uT, vjp_lT, vjp_Ws, vjp_gc, vjp_gp, vjp_gxyz;
   DevBuf<uint32_t> vjp_pblk;  // stiffness block of every element node pair
   float t_vjp_ms = 0;
+  // element results: staged displacements and results, and the events around the result kernels
+  DevBuf<double> res_buf;
+  cudaEvent_t res_ev[2] = {nullptr, nullptr};
+  bool res_timed = false;
 
   int fail(int code, const char* fmt, ...) {
     char b[1024];
@@ -1462,7 +1466,10 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
     h->sep_ci[b].release();
     h->sep_v[b].release();
   }
+  h->res_buf.release();
   for (auto& ev : h->ev)
+    if (ev) cudaEventDestroy(ev);
+  for (auto& ev : h->res_ev)
     if (ev) cudaEventDestroy(ev);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -2685,3 +2692,4 @@ extern "C" int fem_gpu_last_numeric_timing(fem_gpu_t* h, float* element_ms, floa
 #include "fem_loads.cuh"
 // PCG solution of the separated system and the reactions
 #include "fem_solve.cuh"
+#include "fem_results.cuh"

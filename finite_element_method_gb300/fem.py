@@ -401,6 +401,89 @@ class FEM:
                                               ptr(r_r, c_double)))
         return r_r
 
+    # -- global and element results ------------------------------------------------
+    TRUSS_COMPONENTS = ("ForceR",)
+    BEAM_COMPONENTS = ("ForceR", "ForceS", "ForceT", "MomentR", "MomentS", "MomentS", "MomentS", "MomentT", "MomentT",
+                       "MomentT")
+    PLATE_COMPONENTS = ("MembraneForceR", "MembraneForceS", "MembraneForceRS", "BendingMomentR", "BendingMomentS",
+                        "BendingMomentRS", "ShearForceRT", "ShearForceST")
+
+    def compose_global_analysis_result(self, k_aa_indexes, k_bb_indexes, u_a_vector, r_r_vector) -> None:
+        """compose_global_analysis_result (methods_for_global_analysis.rs:334-359): the free DOFs' displacements
+        into the displacements vector, the reactions into the forces vector at the restrained DOFs"""
+        self._imposed()
+        forces = self.forces_vector()
+        self._displacements[np.asarray(k_aa_indexes, np.int64)] = np.asarray(u_a_vector, dtype=np.float64)
+        forces[np.asarray(k_bb_indexes, np.int64)] = np.asarray(r_r_vector, dtype=np.float64)
+        self._result_forces = forces
+
+    def displacements_vector(self):
+        """the displacements vector (6 * nodes_number): imposed values, then the solution once composed"""
+        self._imposed()
+        return self._displacements.copy()
+
+    def extract_global_analysis_result(self):
+        """extract_global_analysis_result (methods_for_global_analysis.rs:361-387): (node number, DOF, displacement,
+        load) for every DOF of every node, in node index order"""
+        self._imposed()
+        forces = getattr(self, "_result_forces", None)
+        if forces is None:
+            forces = self.forces_vector()
+        out = []
+        for i, number in enumerate(self.index_node_numbers()):
+            for d in range(6):
+                out.append((int(number), self.DOF_PARAMETERS[d], float(self._displacements[6 * i + d]),
+                            float(forces[6 * i + d])))
+        return out
+
+    def element_results(self, displacements=None, out=None):
+        """Every element's results on the GPU (fem_gpu_element_results) from `displacements` (default: this
+        model's displacements vector): {"truss": (n, 1), "beam": (n, 10), "plate": (n, 8)} in call order, the
+        components in the order of TRUSS_COMPONENTS, BEAM_COMPONENTS (MomentS and MomentT at node 1, average, node
+        2) and PLATE_COMPONENTS.  `out` may supply the three C-contiguous float64 arrays (e.g. in pinned memory)."""
+        if displacements is None:
+            self._imposed()
+            displacements = self._displacements
+        disp = np.ascontiguousarray(displacements, dtype=np.float64).ravel()
+        nt, nb, np_ = self.element_counts()
+        if out is None:
+            out = {"truss": np.zeros((nt, 1)), "beam": np.zeros((nb, 10)), "plate": np.zeros((np_, 8))}
+        for k, shape in (("truss", (nt, 1)), ("beam", (nb, 10)), ("plate", (np_, 8))):
+            a = out[k]
+            if a.shape != shape or a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError(f"out[{k!r}] must be a C-contiguous float64 array of shape {shape}")
+        self._check(self._L.fem_gpu_element_results(self._h, ptr(disp, c_double), disp.size,
+                                                    ptr(out["truss"], c_double), ptr(out["beam"], c_double),
+                                                    ptr(out["plate"], c_double)))
+        return out
+
+    def element_results_device(self, displacements, truss_out, beam_out, plate_out) -> None:
+        """fem_gpu_element_results_device on device pointers (ints), asynchronous on the model's stream"""
+        self._check(self._L.fem_gpu_element_results_device(self._h, displacements, truss_out, beam_out, plate_out))
+
+    def results_last_ms(self) -> float:
+        x = c_float(0)
+        self._check(self._L.fem_gpu_results_last_ms(self._h, ctypes.byref(x)))
+        return x.value
+
+    def element_numbers(self, kind: str):
+        """element numbers of one kind ("truss", "beam", "plate") in call order"""
+        k = ("truss", "beam", "plate").index(kind)
+        out = np.zeros(self.element_counts()[k], np.uint32)
+        self._check(self._L.fem_gpu_get_element_numbers(self._h, k, ptr(out, c_uint32)))
+        return out
+
+    def extract_elements_analysis_result(self):
+        """extract_elements_analysis_result (methods_for_element_analysis.rs:27-58): (element number,
+        [(component, value), ...]) for the trusses, then the beams, then the plates, each in call order"""
+        res = self.element_results()
+        out = []
+        for kind, names in (("truss", self.TRUSS_COMPONENTS), ("beam", self.BEAM_COMPONENTS),
+                            ("plate", self.PLATE_COMPONENTS)):
+            for number, row in zip(self.element_numbers(kind), res[kind]):
+                out.append((int(number), [(c, float(v)) for c, v in zip(names, row)]))
+        return out
+
     def vjp_last_ms(self) -> float:
         x = c_float(0)
         self._check(self._L.fem_gpu_vjp_last_ms(self._h, ctypes.byref(x)))

@@ -263,6 +263,34 @@ int fem_gpu_solve_pcg(fem_gpu_t* h, const double* r_a, const double* u_b, int bl
  * DOFs, r_r = K_ba u_a + K_bb u_b - r_b (host arrays; u_b, r_b NULL = 0) */
 int fem_gpu_reactions(fem_gpu_t* h, const double* u_a, const double* u_b, const double* r_b, double* r_r);
 
+/* ---- element results ------------------------------------------------------
+ * extract_elements_analysis_result (methods_for_element_analysis.rs:27-58;
+ * truss.rs:281-333, beam.rs:803-993, plate.rs:1196-1409): every element's
+ * forces and moments from the displacements vector (6 per node in node index
+ * order, DOF order X, Y, Z, ThX, ThY, ThZ -- the reference's
+ * displacements_vector after compose_global_analysis_result).  Elements in
+ * call order per kind; components in the reference's order:
+ *   truss_out  n_truss x 1   ForceR
+ *   beam_out   n_beam x 10   ForceR, ForceS, ForceT, MomentR, MomentS at node 1,
+ *                            MomentS average, MomentS at node 2, MomentT at node 1,
+ *                            MomentT average, MomentT at node 2
+ *   plate_out  n_plate x 8   MembraneForceR, MembraneForceS, MembraneForceRS,
+ *                            BendingMomentR, BendingMomentS, BendingMomentRS,
+ *                            ShearForceRT, ShearForceST
+ * A NULL output skips that kind.  Host arrays; n_displacements >= 6 * nodes
+ * added.  Values are those of the reference's formulas within 1e-12 of each
+ * value's magnitude scale (the sum of the absolute terms). */
+int fem_gpu_element_results(fem_gpu_t* h, const double* displacements, size_t n_displacements, double* truss_out,
+                            double* beam_out, double* plate_out);
+/* the same on DEVICE arrays (displacements, beam_out and plate_out 16-byte aligned), launched on the handle's
+ * stream without synchronising */
+int fem_gpu_element_results_device(fem_gpu_t* h, const double* displacements, double* truss_out, double* beam_out,
+                                   double* plate_out);
+/* device time (CUDA events on the handle's stream) of the last element-results launch */
+int fem_gpu_results_last_ms(fem_gpu_t* h, float* ms);
+/* element numbers of one kind (0 truss, 1 beam, 2 plate) in call order (n of that kind, host array) */
+int fem_gpu_get_element_numbers(fem_gpu_t* h, int kind, uint32_t* numbers);
+
 /* Dense assembly of one small structure without any device allocation.
  * No counterpart in the reference: it serves callers that cannot call
  * cudaMalloc -- hosts that own all device memory through their own pool or

@@ -1713,3 +1713,291 @@ int orc_assemble_parallel(const orc_mesh_t* mesh, double rel_tol, double abs_tol
   free(jobs);
   return st;
 }
+
+/* ------------------------------------------------------------------------ */
+/* element results (methods_for_element_analysis.rs:27-58)                   */
+/* ------------------------------------------------------------------------ */
+
+/* row i of R times a 3-vector as a left-to-right fma chain */
+static inline double rrow(const double R[9], int i, const double* u) {
+  return fma(R[3 * i + 2], u[2], fma(R[3 * i + 1], u[1], R[3 * i] * u[0]));
+}
+
+/* truss.rs:281-333.  One integration point r = 0, B = [dh1, 0, 0, dh2, 0, 0] / (L/2)
+ * with dh1 = -1/2, dh2 = 1/2 on the local displacements (R u per node), so the
+ * strain is (u2 - u1) / L with u_i the local axial displacement of node i;
+ * area = area_at_r(0) = A (+ (A2 - A)/2 when tapered, truss.rs:120-130);
+ * ForceR = strain (E area). */
+int orc_truss_results(const double x1[3], const double x2[3], double young, double area, int has_area2,
+                      double area2, double rel_tol, double abs_tol, const double* u6, double* out1) {
+  double R[9];
+  int st = orc_truss_rotation(x1, x2, rel_tol, abs_tol, R);
+  if (st) return st;
+  double d[3];
+  sub3(x2, x1, d);
+  const double L = norm3(d);
+  double a_r = area;
+  if (has_area2) a_r = area + (area2 - area) * 0.5;
+  const double u1 = rrow(R, 0, u6), u2 = rrow(R, 0, u6 + 3);
+  out1[0] = ((u2 - u1) * (1.0 / L)) * (young * a_r);
+  return ORC_OK;
+}
+
+/* beam.rs:803-993.  One integration point r = 0 (h1 = h2 = 1/2, dh1 = -1/2,
+ * dh2 = 1/2, 1/J = 2/L) on the local displacements ul = (R u) per 3-block
+ * (u1, th1, u2, th2); with s = 1/L the six strains of beam.rs:260-493 are
+ *   e_u   = (ul6 - ul0) s
+ *   e_v   = (ul7 - ul1) s - (ul5 + ul11)/2      (dv/dx - th_w)
+ *   e_w   = (ul8 - ul2) s - (ul4 + ul10)/2      (dw/dx - th_v)
+ *   e_thu = (ul9 - ul3) s, e_thv = (ul10 - ul4) s, e_thw = (ul11 - ul5) s
+ * and the results, G = E / (2 (1 + nu)):
+ *   ForceR = e_u (E A), ForceS = e_v ((G A) k), ForceT = e_w ((G A) k),
+ *   MomentR = e_thu (G It), MomentS = e_thv (E I22p) at mid-length and
+ *   +- (L ForceT)/2 at the nodes, MomentT = e_thw (E I11p), +- (L ForceS)/2.
+ * out10: ForceR, ForceS, ForceT, MomentR, MomentS (node 1, average, node 2),
+ * MomentT (node 1, average, node 2) -- the reference's component order. */
+int orc_beam_results(const double x1[3], const double x2[3], double young, double poisson, double area, double i11,
+                     double i22, double i12, double it, double shear_factor, const double axis[3], double rel_tol,
+                     double abs_tol, const double* u12, double* out10) {
+  double R[9], i11p, i22p;
+  int st = orc_beam_rotation(x1, x2, i11, i22, i12, axis, rel_tol, abs_tol, R, &i11p, &i22p);
+  if (st) return st;
+  double d[3];
+  sub3(x2, x1, d);
+  const double L = norm3(d);
+  const double s = 1.0 / L;
+  double ul[12];
+  for (int b = 0; b < 4; ++b)
+    for (int i = 0; i < 3; ++i) ul[3 * b + i] = rrow(R, i, u12 + 3 * b);
+  const double G = young / (2.0 * (1.0 + poisson));
+  const double gak = (G * area) * shear_factor;
+  const double eu = (ul[6] - ul[0]) * s;
+  const double ev = fma(ul[7] - ul[1], s, (ul[5] + ul[11]) * -0.5);
+  const double ew = fma(ul[8] - ul[2], s, (ul[4] + ul[10]) * -0.5);
+  const double fr = eu * (young * area);
+  const double fs = ev * gak;
+  const double ft = ew * gak;
+  const double mr = ((ul[9] - ul[3]) * s) * (G * it);
+  const double ms = ((ul[10] - ul[4]) * s) * (young * i22p);
+  const double mt = ((ul[11] - ul[5]) * s) * (young * i11p);
+  const double hs = (L * ft) * 0.5, ht = (L * fs) * 0.5;
+  out10[0] = fr;
+  out10[1] = fs;
+  out10[2] = ft;
+  out10[3] = mr;
+  out10[4] = ms + hs;
+  out10[5] = ms;
+  out10[6] = ms - hs;
+  out10[7] = mt + ht;
+  out10[8] = mt;
+  out10[9] = mt - ht;
+  return ORC_OK;
+}
+
+/* plate.rs:1196-1409.  The reference sums the strain-displacement matrices
+ * (membrane plate.rs:160-274, bending :276-390, assumed-strain shear
+ * :392-511) over the four corner points (r, s) = (1,1), (-1,1), (-1,-1),
+ * (1,-1) and multiplies the sum by the local displacements (R u per node).
+ *
+ * At a corner only the corner node and its two edge neighbours have nonzero
+ * shape-function derivatives and the Jacobian rows are half the two edge
+ * vectors, so dh/dx, dh/dy there is the gradient of the nodal field from its
+ * differences along those edges.  With the four edges (local coordinates,
+ * node 3 at the origin; head minus tail)
+ *   E0 = X1 - X2, E1 = X4 - X3 (the r direction), E2 = X1 - X4, E3 = X2 - X3 (s),
+ * corner k has (a, b) = (E0, E2), (E0, E3), (E1, E3), (E1, E2),
+ * d_k = a x b = 4 det J, q_k = 1 / d_k, and for a nodal field f with edge
+ * differences F:  df/dx|k = q_k (b_y F_a - a_y F_b),  df/dy|k = q_k (a_x F_b - b_x F_a).
+ * Each edge belongs to two corners, so the corner sums are edge sums with
+ * geometric weights (corner order inside each weight):
+ *   Wx0 = y2 q0 + y3 q1    Wy0 = -(x2 q0 + x3 q1)     (xi, yi: components of Ei)
+ *   Wx1 = y3 q2 + y2 q3    Wy1 = -(x3 q2 + x2 q3)
+ *   Wx2 = -(y0 q0 + y1 q3) Wy2 = x0 q0 + x1 q3
+ *   Wx3 = -(y0 q1 + y1 q2) Wy3 = x0 q1 + x1 q2
+ * sum_k df/dx = sum_e Wx_e F_e, sum_k df/dy = sum_e Wy_e F_e.  The shear
+ * multipliers of plate.rs:443-447 are |b| q_k (gamma_rz) and |a| q_k
+ * (gamma_sz), and the tying value of an edge row (plate.rs:452-508) is
+ *   Gam_e = (w_h - w_t) + (x_e (thy_h + thy_t) - y_e (thx_h + thx_t)) / 2,
+ * so sum_k gamma_rz = Gam0 (l2 q0 + l3 q1) + Gam1 (l3 q2 + l2 q3) and
+ * sum_k gamma_sz = Gam2 (l0 q0 + l1 q3) + Gam3 (l0 q1 + l1 q2), l_e = |E_e|.
+ * The four q_k share one reciprocal.  Forces: membrane C_m e (t/4) with
+ * C_m = E/(1-nu^2) [[1,nu,0],[nu,1,0],[0,0,(1-nu)/2]]; bending C_b k (t^2/24),
+ * C_b = E t/(2(1-nu^2)) [same]; shear E/(2(1+nu)) g (t k_s / 4), where
+ * e = (du/dx, dv/dy, du/dy + dv/dx), k = (-dthy/dx, dthx/dy, dthx/dx - dthy/dy)
+ * and g = (gamma_rz, gamma_sz) are the corner sums.
+ * out8: MembraneForceR, MembraneForceS, MembraneForceRS, BendingMomentR (the
+ * second bending row), BendingMomentS (the first), BendingMomentRS,
+ * ShearForceRT, ShearForceST. */
+int orc_plate_results(const double x1[3], const double x2[3], const double x3[3], const double x4[3], double young,
+                      double poisson, double thickness, double shear_factor, double rel_tol, double abs_tol,
+                      const double* u24, double* out8) {
+  double R[9];
+  int st = orc_plate_rotation(x2, x3, x4, rel_tol, abs_tol, R);
+  if (st) return st;
+  const double* X[4] = {x1, x2, x3, x4};
+  double xl[4] = {0, 0, 0, 0}, yl[4] = {0, 0, 0, 0};
+  for (int i = 0; i < 4; ++i) {
+    if (i == 2) continue;
+    double dd[3];
+    sub3(X[i], x3, dd);
+    xl[i] = (R[0] * dd[0] + R[1] * dd[1]) + R[2] * dd[2];
+    yl[i] = (R[3] * dd[0] + R[4] * dd[1]) + R[5] * dd[2];
+  }
+  /* local nodal fields u, v, w, thx, thy */
+  double fu[4], fv[4], fw[4], ftx[4], fty[4];
+  for (int i = 0; i < 4; ++i) {
+    const double* ui = u24 + 6 * i;
+    fu[i] = rrow(R, 0, ui);
+    fv[i] = rrow(R, 1, ui);
+    fw[i] = rrow(R, 2, ui);
+    ftx[i] = rrow(R, 0, ui + 3);
+    fty[i] = rrow(R, 1, ui + 3);
+  }
+  static const int eh[4] = {0, 3, 0, 1}, et[4] = {1, 2, 3, 2};
+  double ex[4], ey[4], el[4], Fu[4], Fv[4], Ftx[4], Fty[4], Gm[4];
+  for (int e = 0; e < 4; ++e) {
+    const int p = eh[e], q = et[e];
+    ex[e] = xl[p] - xl[q];
+    ey[e] = yl[p] - yl[q];
+    el[e] = sqrt(fma(ex[e], ex[e], ey[e] * ey[e]));
+    Fu[e] = fu[p] - fu[q];
+    Fv[e] = fv[p] - fv[q];
+    Ftx[e] = ftx[p] - ftx[q];
+    Fty[e] = fty[p] - fty[q];
+    Gm[e] = fma(fma(ex[e], fty[p] + fty[q], -(ey[e] * (ftx[p] + ftx[q]))), 0.5, fw[p] - fw[q]);
+  }
+  double dk[4];
+  dk[0] = fma(ex[0], ey[2], -(ey[0] * ex[2]));
+  dk[1] = fma(ex[0], ey[3], -(ey[0] * ex[3]));
+  dk[2] = fma(ex[1], ey[3], -(ey[1] * ex[3]));
+  dk[3] = fma(ex[1], ey[2], -(ey[1] * ex[2]));
+  double q[4];
+  {
+    const double d01 = dk[0] * dk[1], d23 = dk[2] * dk[3];
+    const double inv = 1.0 / (d01 * d23);
+    q[0] = (dk[1] * d23) * inv;
+    q[1] = (dk[0] * d23) * inv;
+    q[2] = (dk[3] * d01) * inv;
+    q[3] = (dk[2] * d01) * inv;
+  }
+  const double Wx[4] = {fma(ey[2], q[0], ey[3] * q[1]), fma(ey[3], q[2], ey[2] * q[3]),
+                        -fma(ey[0], q[0], ey[1] * q[3]), -fma(ey[0], q[1], ey[1] * q[2])};
+  const double Wy[4] = {-fma(ex[2], q[0], ex[3] * q[1]), -fma(ex[3], q[2], ex[2] * q[3]),
+                        fma(ex[0], q[0], ex[1] * q[3]), fma(ex[0], q[1], ex[1] * q[2])};
+  double e0 = Wx[0] * Fu[0], e1 = Wy[0] * Fv[0], k0 = Wx[0] * Fty[0], k1 = Wy[0] * Ftx[0];
+  double e2 = fma(Wx[0], Fv[0], Wy[0] * Fu[0]), k2 = fma(Wx[0], Ftx[0], -(Wy[0] * Fty[0]));
+  for (int e = 1; e < 4; ++e) {
+    e0 = fma(Wx[e], Fu[e], e0);
+    e1 = fma(Wy[e], Fv[e], e1);
+    e2 = fma(Wx[e], Fv[e], fma(Wy[e], Fu[e], e2));
+    k0 = fma(Wx[e], Fty[e], k0);
+    k1 = fma(Wy[e], Ftx[e], k1);
+    k2 = fma(-Wy[e], Fty[e], fma(Wx[e], Ftx[e], k2));
+  }
+  k0 = -k0;
+  const double g0 = fma(Gm[1], fma(el[3], q[2], el[2] * q[3]), Gm[0] * fma(el[2], q[0], el[3] * q[1]));
+  const double g1 = fma(Gm[3], fma(el[0], q[1], el[1] * q[2]), Gm[2] * fma(el[0], q[0], el[1] * q[3]));
+  const double nu = poisson, t = thickness;
+  const double dinv = 1.0 / (1.0 - nu * nu);
+  const double cm = (young * dinv) * (t * 0.25);
+  const double cbm = ((young * t) * (0.5 * dinv)) * ((t * t) / 24.0);
+  const double cs = (young / (2.0 * (1.0 + nu))) * ((t * shear_factor) * 0.25);
+  const double hn = (1.0 - nu) * 0.5;
+  out8[0] = cm * fma(nu, e1, e0);
+  out8[1] = cm * fma(nu, e0, e1);
+  out8[2] = cm * (hn * e2);
+  out8[3] = cbm * fma(nu, k0, k1);
+  out8[4] = cbm * fma(nu, k1, k0);
+  out8[5] = cbm * (hn * k2);
+  out8[6] = cs * g0;
+  out8[7] = cs * g1;
+  return ORC_OK;
+}
+
+/* A mesh's element results from a displacements vector (6 per node, node
+ * index order), n_threads threads over contiguous element ranges; outputs in
+ * element call order (NULL skips a kind); *seconds: wall time. */
+typedef struct {
+  const orc_mesh_t* m;
+  const double* disp;
+  double rel_tol, abs_tol;
+  double *t_out, *b_out, *p_out;
+  size_t t0, t1, b0, b1, p0, p1;
+  int status;
+} res_job;
+
+static void gather_u(const double* disp, const int32_t* nd, int nn, int per, double* u) {
+  for (int i = 0; i < nn; ++i)
+    for (int c = 0; c < per; ++c) u[per * i + c] = disp[6 * (size_t)nd[i] + (size_t)c];
+}
+
+static void* res_worker(void* arg) {
+  res_job* j = (res_job*)arg;
+  const orc_mesh_t* m = j->m;
+  const double* X = m->xyz;
+  double u[24];
+  if (j->t_out)
+    for (size_t e = j->t0; e < j->t1; ++e) {
+      const int32_t* nd = m->t_nodes + 2 * e;
+      double a2 = m->t_area2 ? m->t_area2[e] : NAN;
+      gather_u(j->disp, nd, 2, 3, u);
+      int st = orc_truss_results(X + 3 * (size_t)nd[0], X + 3 * (size_t)nd[1], m->t_young[e], m->t_area[e],
+                                 a2 == a2, a2, j->rel_tol, j->abs_tol, u, j->t_out + e);
+      if (st) j->status = st;
+    }
+  if (j->b_out)
+    for (size_t e = j->b0; e < j->b1; ++e) {
+      const int32_t* nd = m->b_nodes + 2 * e;
+      gather_u(j->disp, nd, 2, 6, u);
+      int st = orc_beam_results(X + 3 * (size_t)nd[0], X + 3 * (size_t)nd[1], m->b_young[e], m->b_poisson[e],
+                                m->b_area[e], m->b_i11[e], m->b_i22[e], m->b_i12[e], m->b_it[e], m->b_shear[e],
+                                m->b_axis + 3 * e, j->rel_tol, j->abs_tol, u, j->b_out + 10 * e);
+      if (st) j->status = st;
+    }
+  if (j->p_out)
+    for (size_t e = j->p0; e < j->p1; ++e) {
+      const int32_t* nd = m->p_nodes + 4 * e;
+      gather_u(j->disp, nd, 4, 6, u);
+      int st = orc_plate_results(X + 3 * (size_t)nd[0], X + 3 * (size_t)nd[1], X + 3 * (size_t)nd[2],
+                                 X + 3 * (size_t)nd[3], m->p_young[e], m->p_poisson[e], m->p_thickness[e],
+                                 m->p_shear[e], j->rel_tol, j->abs_tol, u, j->p_out + 8 * e);
+      if (st) j->status = st;
+    }
+  return NULL;
+}
+
+int orc_element_results(const orc_mesh_t* mesh, const double* displacements, double rel_tol, double abs_tol,
+                        int n_threads, double* truss_out, double* beam_out, double* plate_out, double* seconds) {
+  if (n_threads < 1) n_threads = 1;
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)n_threads);
+  res_job* jobs = (res_job*)calloc((size_t)n_threads, sizeof(res_job));
+  struct timespec t0, t1;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
+  for (int t = 0; t < n_threads; ++t) {
+    res_job* j = &jobs[t];
+    j->m = mesh;
+    j->disp = displacements;
+    j->rel_tol = rel_tol;
+    j->abs_tol = abs_tol;
+    j->t_out = truss_out;
+    j->b_out = beam_out;
+    j->p_out = plate_out;
+    j->t0 = mesh->n_truss * (size_t)t / (size_t)n_threads;
+    j->t1 = mesh->n_truss * (size_t)(t + 1) / (size_t)n_threads;
+    j->b0 = mesh->n_beam * (size_t)t / (size_t)n_threads;
+    j->b1 = mesh->n_beam * (size_t)(t + 1) / (size_t)n_threads;
+    j->p0 = mesh->n_plate * (size_t)t / (size_t)n_threads;
+    j->p1 = mesh->n_plate * (size_t)(t + 1) / (size_t)n_threads;
+    pthread_create(&th[t], NULL, res_worker, j);
+  }
+  int st = ORC_OK;
+  for (int t = 0; t < n_threads; ++t) {
+    pthread_join(th[t], NULL);
+    if (jobs[t].status) st = jobs[t].status;
+  }
+  clock_gettime(CLOCK_MONOTONIC, &t1);
+  if (seconds) *seconds = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+  free(th);
+  free(jobs);
+  return st;
+}

@@ -126,6 +126,22 @@ int orc_beam_rotation(const double x1[3], const double x2[3], double i11, double
 int orc_plate_rotation(const double x2[3], const double x3[3], const double x4[3], double rel_tol,
                        double abs_tol, double* r9);
 
+/* element results from local displacements of the element's nodes in global
+ * axes (truss: 3 per node, beam and plate: 6 per node), in the reference's
+ * component order: truss [ForceR]; beam [ForceR, ForceS, ForceT, MomentR,
+ * MomentS x3 (node 1, average, node 2), MomentT x3]; plate [MembraneForceR,
+ * MembraneForceS, MembraneForceRS, BendingMomentR, BendingMomentS,
+ * BendingMomentRS, ShearForceRT, ShearForceST] (truss.rs:281-333,
+ * beam.rs:803-993, plate.rs:1196-1409) */
+int orc_truss_results(const double x1[3], const double x2[3], double young, double area, int has_area2,
+                      double area2, double rel_tol, double abs_tol, const double* u6, double* out1);
+int orc_beam_results(const double x1[3], const double x2[3], double young, double poisson, double area, double i11,
+                     double i22, double i12, double it, double shear_factor, const double axis[3], double rel_tol,
+                     double abs_tol, const double* u12, double* out10);
+int orc_plate_results(const double x1[3], const double x2[3], const double x3[3], const double x4[3], double young,
+                      double poisson, double thickness, double shear_factor, double rel_tol, double abs_tol,
+                      const double* u24, double* out8);
+
 /* the transcendental kernels shared (by algorithm, not by code) with the GPU */
 double orc_sin(double x);
 double orc_cos(double x);
@@ -155,6 +171,12 @@ typedef struct {
  * nnz, *seconds the wall time of assembly + CSR conversion. */
 int orc_assemble_parallel(const orc_mesh_t* mesh, double rel_tol, double abs_tol, int n_threads, int64_t* row_ptr,
                           int32_t* col_idx, double* values, int64_t values_cap, int64_t* nnz_out, double* seconds);
+
+/* Every element's results of a mesh from the displacements vector (6 per
+ * node, node index order), n_threads threads over contiguous element ranges;
+ * outputs in element call order (NULL skips a kind), *seconds: wall time. */
+int orc_element_results(const orc_mesh_t* mesh, const double* displacements, double rel_tol, double abs_tol,
+                        int n_threads, double* truss_out, double* beam_out, double* plate_out, double* seconds);
 
 #ifdef __cplusplus
 }

@@ -69,6 +69,10 @@ def lib():
             getattr(L, f).argtypes = [c_double]
         L.orc_assemble_parallel.argtypes = [ctypes.POINTER(OrcMesh), c_double, c_double, c_int, i64p, ip32, dp,
                                             c_int64, i64p, dp]
+        L.orc_truss_results.argtypes = [dp, dp, c_double, c_double, c_int, c_double, c_double, c_double, dp, dp]
+        L.orc_beam_results.argtypes = [dp, dp] + [c_double] * 8 + [dp, c_double, c_double, dp, dp]
+        L.orc_plate_results.argtypes = [dp, dp, dp, dp] + [c_double] * 6 + [dp, dp]
+        L.orc_element_results.argtypes = [ctypes.POINTER(OrcMesh), dp, c_double, c_double, c_int, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -340,6 +344,59 @@ def assemble_parallel(mesh, n_threads, rel_tol=1e-12, abs_tol=1e-12, want_csr=Tr
         raise OracleError(st, "parallel assembly failed")
     n = nnz.value
     return sec.value, n, (rp, ci[:n], va[:n])
+
+
+def truss_results(x1, x2, young, area, area2, u6, rel_tol=1e-12, abs_tol=1e-12):
+    """[ForceR] of one truss from its nodes' global displacements (3 per node), truss.rs:281-333"""
+    out = np.zeros(1)
+    a, b = _v3(x1), _v3(x2)
+    u = np.ascontiguousarray(u6, dtype=np.float64).reshape(6)
+    st = lib().orc_truss_results(_p(a, c_double), _p(b, c_double), young, area, int(area2 is not None),
+                                 0.0 if area2 is None else area2, rel_tol, abs_tol, _p(u, c_double), _p(out, c_double))
+    if st:
+        raise OracleError(st, "truss results failed")
+    return out
+
+
+def beam_results(x1, x2, young, poisson, area, i11, i22, i12, it, shear_factor, axis, u12, rel_tol=1e-12,
+                 abs_tol=1e-12):
+    """the 10 beam results (beam.rs:803-993) from its nodes' global displacements (6 per node)"""
+    out = np.zeros(10)
+    a, b, ax = _v3(x1), _v3(x2), _v3(axis)
+    u = np.ascontiguousarray(u12, dtype=np.float64).reshape(12)
+    st = lib().orc_beam_results(_p(a, c_double), _p(b, c_double), young, poisson, area, i11, i22, i12, it,
+                                shear_factor, _p(ax, c_double), rel_tol, abs_tol, _p(u, c_double), _p(out, c_double))
+    if st:
+        raise OracleError(st, "beam results failed")
+    return out
+
+
+def plate_results(x1, x2, x3, x4, young, poisson, thickness, shear_factor, u24, rel_tol=1e-12, abs_tol=1e-12):
+    """the 8 plate results (plate.rs:1196-1409) from its nodes' global displacements (6 per node)"""
+    out = np.zeros(8)
+    p = [_v3(x) for x in (x1, x2, x3, x4)]
+    u = np.ascontiguousarray(u24, dtype=np.float64).reshape(24)
+    st = lib().orc_plate_results(*[_p(x, c_double) for x in p], young, poisson, thickness, shear_factor, rel_tol,
+                                 abs_tol, _p(u, c_double), _p(out, c_double))
+    if st:
+        raise OracleError(st, "plate results failed")
+    return out
+
+
+def element_results(mesh, displacements, n_threads=1, rel_tol=1e-12, abs_tol=1e-12):
+    """Every element's results of a meshes.Mesh from its displacements vector (6 per node, index order):
+    ({"truss": (n, 1), "beam": (n, 10), "plate": (n, 8)}, seconds)."""
+    s = mesh_struct(mesh)
+    disp = np.ascontiguousarray(displacements, dtype=np.float64)
+    assert disp.shape == (6 * mesh.nodes_number,)
+    out = {"truss": np.zeros((s.n_truss, 1)), "beam": np.zeros((s.n_beam, 10)), "plate": np.zeros((s.n_plate, 8))}
+    sec = c_double(0)
+    st = lib().orc_element_results(ctypes.byref(s), _p(disp, c_double), rel_tol, abs_tol, n_threads,
+                                   _p(out["truss"], c_double), _p(out["beam"], c_double), _p(out["plate"], c_double),
+                                   ctypes.byref(sec))
+    if st:
+        raise OracleError(st, "element results failed")
+    return out, sec.value
 
 
 def sin(x):

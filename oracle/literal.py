@@ -281,3 +281,133 @@ def plate_global_matrix(x1, x2, x3, x4, E, nu, t, k_s, rel_tol=1e-12, abs_tol=1e
         K[6 * i + 5, 6 * i + 5] = K[6 * i + 5, 6 * i + 5] + 1  # KROT6 (plate.rs:25, :716-721)
     T = _blockdiag(R, 8, bk)
     return _out(T.T.dot(K).dot(T), bk)
+
+
+# --------------------------------------------------------------------------
+# element results (methods_for_element_analysis.rs:27-58)
+#
+# Each function returns (values, scale): the results as the reference writes
+# them (dense B matrices summed over the integration / corner points, times
+# the rotated displacements, times C) and the same expression with every
+# factor replaced by its absolute value -- the magnitude a rounding error is
+# measured against.
+# --------------------------------------------------------------------------
+
+def _both(M, bk):
+    return M, np.array([abs(v) for v in np.asarray(M, dtype=object).ravel()], dtype=object).reshape(np.shape(M))
+
+
+def truss_results(x1, x2, E, A, A2, u6, rel_tol=1e-12, abs_tol=1e-12, bk=FLOAT):
+    """truss.rs:281-333"""
+    x1, x2 = bk.vec(x1), bk.vec(x2)
+    d = x2 - x1
+    L = bk.norm(d)
+    R = align_rotation(d, [L, 0, 0], abs_tol, bk)
+    T, Ta = _both(_blockdiag(R, 2, bk), bk)
+    u, ua = _both(bk.vec(u6), bk)
+    r = bk.num(0)
+    B, Ba = _both(bk.vec([-0.5, 0, 0, 0.5, 0, 0]) * (1 / (L / 2)), bk)  # truss.rs:95-118
+    E, A = bk.num(E), bk.num(A)
+    area = bk.num(0) + (A if A2 is None else (bk.num(A2) - A) / 2 * r + A - (bk.num(A2) - A) / 2 * -1)
+    f = E * area / 1
+    return [B.dot(T.dot(u)) * f], [Ba.dot(Ta.dot(ua)) * abs(f)]
+
+
+def beam_results(x1, x2, E, nu, A, i11, i22, i12, it, k_s, axis, u12, rel_tol=1e-12, abs_tol=1e-12, bk=FLOAT):
+    """beam.rs:803-993"""
+    R, i11p, i22p = beam_rotation(x1, x2, i11, i22, i12, axis, rel_tol, abs_tol, bk)
+    d = bk.vec(x2) - bk.vec(x1)
+    L = bk.norm(d)
+    r = bk.num(0)
+    inv = 1 / (L / 2)
+    dh1, dh2, h1, h2 = bk.num(-0.5), bk.num(0.5), (1 - r) / 2, (1 + r) / 2
+
+    def row(entries):
+        v = bk.zeros(1, 12)
+        for idx, val in entries:
+            v[0, idx] = val
+        return v[0]
+
+    T, Ta = _both(_blockdiag(R, 4, bk), bk)
+    u, ua = _both(bk.vec(u12), bk)
+    ul, ula = T.dot(u), Ta.dot(ua)
+    E, nu, A, it, k_s = (bk.num(v) for v in (E, nu, A, it, k_s))
+    G = E / (2 * (1 + nu))
+    rows = [  # beam.rs:260-493
+        (row([(0, dh1 * inv), (6, dh2 * inv)]), E * A / 1),
+        (row([(1, dh1 * inv), (7, dh2 * inv)]) - row([(5, h1), (11, h2)]), G * A * k_s / 1),
+        (row([(2, dh1 * inv), (8, dh2 * inv)]) - row([(4, h1), (10, h2)]), G * A * k_s / 1),
+        (row([(3, dh1 * inv), (9, dh2 * inv)]), G * it / 1),
+        (row([(4, dh1 * inv), (10, dh2 * inv)]), E * i22p / 1),
+        (row([(5, dh1 * inv), (11, dh2 * inv)]), E * i11p / 1),
+    ]
+    v = [B.dot(ul) * c for B, c in rows]
+    s = [np.array([abs(x) for x in B], dtype=object).dot(ula) * abs(c) for B, c in rows]
+    fr, fs, ft, mr, ms, mt = v
+    sr, ss, st, smr, sms, smt = s
+    vals = [fr, fs, ft, mr, ms + L * ft / 2, ms, ms - L * ft / 2, mt + L * fs / 2, mt, mt - L * fs / 2]
+    scale = [sr, ss, st, smr, sms + L * st / 2, sms, sms + L * st / 2, smt + L * ss / 2, smt, smt + L * ss / 2]
+    return vals, scale
+
+
+def plate_results(x1, x2, x3, x4, E, nu, t, k_s, u24, rel_tol=1e-12, abs_tol=1e-12, bk=FLOAT):
+    """plate.rs:1196-1409: B matrices (plate.rs:160-511) summed over the corner points"""
+    X = [bk.vec(v) for v in (x1, x2, x3, x4)]
+    R = plate_rotation(X[1], X[2], X[3], abs_tol, bk)
+    loc = {i: R.dot(X[i] - X[2]) for i in (0, 1, 3)}
+    z = bk.num(0)
+    xs = [loc[0][0], loc[1][0], z, loc[3][0]]
+    ys = [loc[0][1], loc[1][1], z, loc[3][1]]
+    x1l, x2l, x3l, x4l = xs
+    y1l, y2l, y3l, y4l = ys
+    a_x, b_x, c_x = x1l - x2l - x3l + x4l, x1l - x2l + x3l - x4l, x1l + x2l - x3l - x4l
+    a_y, b_y, c_y = y1l - y2l - y3l + y4l, y1l - y2l + y3l - y4l, y1l + y2l - y3l - y4l
+    q = bk.num(0.25)
+    Bm, Bb, Bs = bk.zeros(3, 24), bk.zeros(3, 24), bk.zeros(2, 24)
+    one = bk.num(1)
+    for r, s in [(one, one), (-one, one), (-one, -one), (one, -one)]:  # plate.rs:1248-1253
+        dhr = [q * (1 + s), -q * (1 + s), -q * (1 - s), q * (1 - s)]
+        dhs = [q * (1 + r), q * (1 - r), -q * (1 - r), -q * (1 + r)]
+        J = [[_dot(dhr, xs), _dot(dhr, ys)], [_dot(dhs, xs), _dot(dhs, ys)]]
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0]
+        Ji = [[J[1][1] / det, -J[0][1] / det], [-J[1][0] / det, J[0][0] / det]]
+        dxy = [[Ji[a][0] * dhr[i] + Ji[a][1] * dhs[i] for i in range(4)] for a in range(2)]
+        for i in range(4):
+            Bm[0, 6 * i] += dxy[0][i]
+            Bm[1, 6 * i + 1] += dxy[1][i]
+            Bm[2, 6 * i] += dxy[1][i]
+            Bm[2, 6 * i + 1] += dxy[0][i]
+            Bb[0, 6 * i + 4] += -dxy[0][i]
+            Bb[1, 6 * i + 3] += dxy[1][i]
+            Bb[2, 6 * i + 3] += dxy[0][i]
+            Bb[2, 6 * i + 4] += -dxy[1][i]
+        mr = bk.sqrt((c_x + r * b_x) ** 2 + (c_y + r * b_y) ** 2) / (8 * det)
+        ms = bk.sqrt((a_x + s * b_x) ** 2 + (a_y + s * b_y) ** 2) / (8 * det)
+        for (c, w, sg, ex, ey) in ((0, 1 + s, 1, x1l - x2l, y1l - y2l), (1, 1 + s, -1, x1l - x2l, y1l - y2l),
+                                   (2, 1 - s, -1, x4l - x3l, y4l - y3l), (3, 1 - s, 1, x4l - x3l, y4l - y3l)):
+            Bs[0, 6 * c + 2] += sg * w / 2 * mr
+            Bs[0, 6 * c + 3] += -w * ey / 4 * mr
+            Bs[0, 6 * c + 4] += w * ex / 4 * mr
+        for (c, w, sg, ex, ey) in ((0, 1 + r, 1, x1l - x4l, y1l - y4l), (1, 1 - r, 1, x2l - x3l, y2l - y3l),
+                                   (2, 1 - r, -1, x2l - x3l, y2l - y3l), (3, 1 + r, -1, x1l - x4l, y1l - y4l)):
+            Bs[1, 6 * c + 2] += sg * w / 2 * ms
+            Bs[1, 6 * c + 3] += -w * ey / 4 * ms
+            Bs[1, 6 * c + 4] += w * ex / 4 * ms
+    T, Ta = _both(_blockdiag(R, 8, bk), bk)
+    u, ua = _both(bk.vec(u24), bk)
+    ul, ula = T.dot(u), Ta.dot(ua)
+    E, nu, t, k_s = (bk.num(v) for v in (E, nu, t, k_s))
+    cmat = np.array([[1, nu, 0], [nu, 1, 0], [0, 0, (1 - nu) / 2]], dtype=object)
+    Cm = cmat * (E / (1 - nu ** 2))
+    Cb = cmat * (E * t / (2 * (1 - nu ** 2)))
+    Cs = bk.eye(2) * (E / (2 * (1 + nu)))
+    fm = Cm.dot(Bm.dot(ul)) * (t / 4)
+    fb = Cb.dot(Bb.dot(ul)) * (t ** 2 / 24)
+    fs = Cs.dot(Bs.dot(ul)) * (t * k_s / 4)
+    ab = lambda M: np.array([abs(x) for x in np.asarray(M, dtype=object).ravel()], dtype=object).reshape(np.shape(M))
+    sm = ab(Cm).dot(ab(Bm).dot(ula)) * (t / 4)
+    sb = ab(Cb).dot(ab(Bb).dot(ula)) * (t ** 2 / 24)
+    ss = ab(Cs).dot(ab(Bs).dot(ula)) * abs(t * k_s / 4)
+    vals = [fm[0], fm[1], fm[2], fb[1], fb[0], fb[2], fs[0], fs[1]]
+    scale = [sm[0], sm[1], sm[2], sb[1], sb[0], sb[2], ss[0], ss[1]]
+    return vals, scale
