@@ -56,6 +56,10 @@ template <class T>
 struct DevBuf {
   T* p = nullptr;
   size_t cap = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
   cudaError_t reserve(size_t n, cudaStream_t s, size_t keep = 0) {
     if (n <= cap) return cudaSuccess;
     size_t nc = std::max<size_t>(n, cap ? cap + cap / 2 : 256);
@@ -459,8 +463,16 @@ __device__ __forceinline__ void plate_element(size_t e, NodesView nd, const Plat
   plate_pair<3, 3>(C, R, ident, nidx, ep + 9, sink);
 }
 
-__global__ void __launch_bounds__(256) k_plate(NodesView nd, PlateView pl, double abs_tol, size_t count,
-                                               BlockSink sink) {
+// block size and minimum resident blocks per SM of the plate element kernel (its register budget)
+#ifndef FEM_PLATE_THREADS
+#define FEM_PLATE_THREADS 128
+#endif
+#ifndef FEM_PLATE_MIN_BLOCKS
+#define FEM_PLATE_MIN_BLOCKS 1
+#endif
+
+__global__ void __launch_bounds__(FEM_PLATE_THREADS, FEM_PLATE_MIN_BLOCKS)
+    k_plate(NodesView nd, PlateView pl, double abs_tol, size_t count, BlockSink sink) {
   size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (e >= count) return;
   plate_element(e, nd, pl, abs_tol, sink);
@@ -1260,7 +1272,16 @@ struct fem_gpu {
   int64_t sep_n[2] = {0, 0}, sep_nnz[4] = {0, 0, 0, 0};
   // PCG on K_aa: vectors, dot-product partials, preconditioner blocks and their inverses
   DevBuf<double> pcg_vec, pcg_part, pcg_scal, pcg_inv;
-  DevBuf<uint32_t> pcg_blk;
+  DevBuf<uint32_t> pcg_blk, pcg_info;
+  DevBuf<int> pcg_state;
+  // sliced ELLPACK copy of K_aa for the PCG's products (valid with the separation it was built from)
+  bool sell_valid = false;
+  size_t sell_windows = 0;
+  int64_t sell_entries = 0;
+  DevBuf<int64_t> sell_off;
+  DevBuf<uint32_t> sell_perm;
+  DevBuf<int32_t> sell_col;
+  DevBuf<double> sell_val;
   // validation scratch
   DevBuf<int> vstatus;
   DevBuf<unsigned long long> vfirst;
@@ -1455,6 +1476,12 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   h->forces.release();
   for (DevBuf<double>* v : {&h->pcg_vec, &h->pcg_part, &h->pcg_scal, &h->pcg_inv}) v->release();
   h->pcg_blk.release();
+  h->pcg_info.release();
+  h->pcg_state.release();
+  h->sell_off.release();
+  h->sell_perm.release();
+  h->sell_col.release();
+  h->sell_val.release();
   h->sep_imposed.release();
   h->sep_cls.release();
   h->sep_u32.release();
@@ -2188,13 +2215,16 @@ int launch_elements(fem_gpu* h, BlockSink sink_t, BlockSink sink_b, BlockSink si
     k_truss<<<grid_for(h->nt, 128), 128, 0, h->stream>>>(nd, h->trusses(), h->abs_tol, h->nt, sink_t);
   if (h->nbm)
     k_beam<<<grid_for(h->nbm, 128), 128, 0, h->stream>>>(nd, h->beams(), h->rel_tol, h->abs_tol, h->nbm, sink_b);
-  if (h->np) k_plate<<<grid_for(h->np, 128), 128, 0, h->stream>>>(nd, h->plates(), h->abs_tol, h->np, sink_p);
+  if (h->np)
+    k_plate<<<grid_for(h->np, FEM_PLATE_THREADS), FEM_PLATE_THREADS, 0, h->stream>>>(nd, h->plates(), h->abs_tol,
+                                                                                   h->np, sink_p);
   CK(cudaGetLastError());
   return FEM_GPU_OK;
 }
 
 int numeric_launch(fem_gpu* h) {
   h->sep_valid = false;  // a separation describes the stiffness it was taken from
+  h->sell_valid = false;
   CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->stream));
   CK(cudaEventRecord(h->ev[0], h->stream));
   BlockSink st{nullptr, h->V.p, h->off_t.p, h->flag.p};

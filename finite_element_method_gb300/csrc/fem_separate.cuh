@@ -151,6 +151,7 @@ const char* const kDofNames[6] = {"X", "Y", "Z", "ThX", "ThY", "ThZ"};
 extern "C" int fem_gpu_separate_sparse(fem_gpu_t* h, const uint8_t* imposed) {
   if (!h || !imposed) return FEM_GPU_ERR_ARGUMENT;
   h->sep_valid = false;
+  h->sell_valid = false;
   if (!h->pattern_valid || !h->numeric_done) return h->fail(FEM_GPU_ERR_STATE, "call fem_gpu_assemble first");
   cudaStream_t s = h->stream;
   const size_t n = (size_t)h->nodes_number * 6;
