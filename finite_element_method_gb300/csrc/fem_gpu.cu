@@ -463,16 +463,8 @@ __device__ __forceinline__ void plate_element(size_t e, NodesView nd, const Plat
   plate_pair<3, 3>(C, R, ident, nidx, ep + 9, sink);
 }
 
-// block size and minimum resident blocks per SM of the plate element kernel (its register budget)
-#ifndef FEM_PLATE_THREADS
-#define FEM_PLATE_THREADS 128
-#endif
-#ifndef FEM_PLATE_MIN_BLOCKS
-#define FEM_PLATE_MIN_BLOCKS 1
-#endif
-
-__global__ void __launch_bounds__(FEM_PLATE_THREADS, FEM_PLATE_MIN_BLOCKS)
-    k_plate(NodesView nd, PlateView pl, double abs_tol, size_t count, BlockSink sink) {
+__global__ void __launch_bounds__(256) k_plate(NodesView nd, PlateView pl, double abs_tol, size_t count,
+                                               BlockSink sink) {
   size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (e >= count) return;
   plate_element(e, nd, pl, abs_tol, sink);
@@ -2215,9 +2207,7 @@ int launch_elements(fem_gpu* h, BlockSink sink_t, BlockSink sink_b, BlockSink si
     k_truss<<<grid_for(h->nt, 128), 128, 0, h->stream>>>(nd, h->trusses(), h->abs_tol, h->nt, sink_t);
   if (h->nbm)
     k_beam<<<grid_for(h->nbm, 128), 128, 0, h->stream>>>(nd, h->beams(), h->rel_tol, h->abs_tol, h->nbm, sink_b);
-  if (h->np)
-    k_plate<<<grid_for(h->np, FEM_PLATE_THREADS), FEM_PLATE_THREADS, 0, h->stream>>>(nd, h->plates(), h->abs_tol,
-                                                                                   h->np, sink_p);
+  if (h->np) k_plate<<<grid_for(h->np, 128), 128, 0, h->stream>>>(nd, h->plates(), h->abs_tol, h->np, sink_p);
   CK(cudaGetLastError());
   return FEM_GPU_OK;
 }
