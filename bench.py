@@ -1,6 +1,7 @@
 """Benchmark of the FP64 element-stiffness-and-assembly path on one GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload plate|beam|truss]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload plate|beam|truss|batch|adjoint|separate|loads|pcg|results]
 
 A step is one numeric assembly pass over the whole mesh into the FP64 CSR
 global stiffness (element kernels + deterministic block reduction), with the
@@ -22,7 +23,6 @@ import json
 import os
 import subprocess
 import sys
-import threading
 import time
 
 import numpy as np
@@ -65,40 +65,46 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """SM clocks and throttle reasons sampled by one `nvidia-smi -lms` process that runs exactly while the timed
+    region runs (started on entry, terminated on exit; every line it printed is a sample from inside)."""
 
-    def __init__(self, gpu_index=0, period_ms=100):
-        self.samples, self.max_mhz, self.reasons = [], None, set()
-        self._stop = threading.Event()
-        self._idx, self._period = gpu_index, period_ms
-        self._t = threading.Thread(target=self._run, daemon=True)
-
-    def _run(self):
-        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+    QUERY = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self._idx), f"--query-gpu={q}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                f = [x.strip() for x in out.stdout.strip().split(",")]
-                if len(f) >= 6:
-                    self.samples.append(float(f[0]))
-                    self.max_mhz = float(f[1])
-                    for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
-                                        "sw_power_cap"), f[2:6]):
-                        if v.lower().startswith("active"):
-                            self.reasons.add(name)
-            except Exception:
-                pass
-            self._stop.wait(self._period / 1000.0)
+
+    def __init__(self, gpu_index=0, period_ms=20):
+        self.samples, self.max_mhz, self.reasons = [], None, set()
+        self._idx, self._period, self._p = gpu_index, period_ms, None
 
     def __enter__(self):
-        self._t.start()
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", "-i", str(self._idx), f"--query-gpu={self.QUERY}",
+                                        "--format=csv,noheader,nounits", "-lms", str(self._period)],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self._p = None
         return self
 
     def __exit__(self, *exc):
-        self._stop.set()
-        self._t.join(timeout=10)
+        if self._p is None:
+            return
+        self._p.terminate()
+        try:
+            out, _ = self._p.communicate(timeout=10)
+        except subprocess.TimeoutExpired:
+            self._p.kill()
+            out, _ = self._p.communicate()
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 6:
+                continue
+            try:
+                self.samples.append(float(f[0]))
+                self.max_mhz = float(f[1])
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), f[2:6]):
+                if v.lower().startswith("active"):
+                    self.reasons.add(name)
 
     def summary(self):
         return {"sm_mhz": float(np.median(self.samples)) if self.samples else None, "sm_max_mhz": self.max_mhz,
@@ -535,7 +541,7 @@ def ptr_u8(a):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="plate", choices=["plate", "beam", "truss", "batch", "adjoint", "separate", "loads", "pcg",
