@@ -399,7 +399,7 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
 
 extern "C" int fem_gpu_batch_destroy(fem_gpu_batch_t* b) {
   if (!b) return FEM_GPU_OK;
-  if (b->stream) cudaStreamSynchronize(b->stream);
+  cudaDeviceSynchronize();  // device pointers were handed out: all work must be done before the pool reuses them
   if (b->graph) cudaGraphExecDestroy(b->graph);
   DevBuf<double>* d[] = {&b->dx, &b->dy, &b->dz, &b->t_E, &b->t_A, &b->t_A2, &b->b_E, &b->b_nu, &b->b_A, &b->b_i11,
                          &b->b_i22, &b->b_i12, &b->b_it, &b->b_ks, &b->b_ax, &b->b_ay, &b->b_az, &b->p_E, &b->p_nu,
@@ -417,8 +417,9 @@ extern "C" int fem_gpu_batch_destroy(fem_gpu_batch_t* b) {
   b->counter.release();
   for (auto& e : b->ev)
     if (e) cudaEventDestroy(e);
-  if (b->stream) cudaStreamDestroy(b->stream);
-  delete b;
+  cudaStream_t s = b->stream;
+  delete b;  // the remaining device arrays are freed in the stream's order: the stream goes last
+  if (s) cudaStreamDestroy(s);
   return FEM_GPU_OK;
 }
 

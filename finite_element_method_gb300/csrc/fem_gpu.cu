@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstring>
 #include <cub/cub.cuh>
+#include <mutex>
 #include <string>
 #include <unordered_map>
 #include <unordered_set>
@@ -52,10 +53,42 @@ __host__ __device__ __forceinline__ void pair_nodes2(int p, int& i, int& j) {
 // ---------------------------------------------------------------------------
 // device buffers
 // ---------------------------------------------------------------------------
+// Device memory comes from one stream-ordered pool per device that keeps what is freed (release threshold
+// at its maximum): a model's buffers and an assembly's temporaries are served again without cudaMalloc /
+// cudaFree, which cost milliseconds at these sizes and synchronise the device.
+// fem_gpu_release_cached_memory hands the cached memory back.
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pools[64] = {};
+
+cudaError_t device_pool(cudaMemPool_t* out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_pool_mutex);
+  if (!g_pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    e = cudaMemPoolCreate(&pool, &props);
+    if (e != cudaSuccess) return e;
+    uint64_t keep_all = ~0ull;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep_all);
+    if (e != cudaSuccess) return e;
+    g_pools[dev] = pool;
+  }
+  *out = g_pools[dev];
+  return cudaSuccess;
+}
+
+// A device array owned by one object and used on one stream: allocated and freed in that stream's order.
 template <class T>
 struct DevBuf {
   T* p = nullptr;
   size_t cap = 0;
+  cudaStream_t st = nullptr;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
@@ -63,22 +96,30 @@ struct DevBuf {
   cudaError_t reserve(size_t n, cudaStream_t s, size_t keep = 0) {
     if (n <= cap) return cudaSuccess;
     size_t nc = std::max<size_t>(n, cap ? cap + cap / 2 : 256);
-    T* q = nullptr;
-    cudaError_t e = cudaMalloc((void**)&q, nc * sizeof(T));
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = device_pool(&pool);
     if (e != cudaSuccess) return e;
-    if (p && keep) {
-      e = cudaMemcpyAsync(q, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, s);
-      if (e != cudaSuccess) return e;
-      e = cudaStreamSynchronize(s);
-      if (e != cudaSuccess) return e;
+    T* q = nullptr;
+    e = cudaMallocFromPoolAsync((void**)&q, nc * sizeof(T), pool, s);
+    if (e != cudaSuccess) return e;
+    if (p) {
+      if (st != s && st) {  // the old array's last uses were ordered on another stream
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return e;
+      }
+      if (keep) {
+        e = cudaMemcpyAsync(q, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return e;
+      }
+      cudaFreeAsync(p, s);
     }
-    if (p) cudaFree(p);
     p = q;
     cap = nc;
+    st = s;
     return cudaSuccess;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, st);
     p = nullptr;
     cap = 0;
   }
@@ -1423,9 +1464,20 @@ extern "C" int fem_gpu_create(double rel_tol, double abs_tol, uint32_t nodes_num
   return FEM_GPU_OK;
 }
 
+extern "C" int fem_gpu_release_cached_memory(void) {
+  cudaMemPool_t pool = nullptr;
+  cudaError_t e = device_pool(&pool);
+  if (e != cudaSuccess) return FEM_GPU_ERR_CUDA;
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return FEM_GPU_ERR_CUDA;
+  return cudaMemPoolTrimTo(pool, 0) == cudaSuccess ? FEM_GPU_OK : FEM_GPU_ERR_CUDA;
+}
+
 extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   if (!h) return FEM_GPU_OK;
-  if (h->stream) cudaStreamSynchronize(h->stream);
+  // work of any stream may still read the model's arrays (device pointers handed out): wait for all of it
+  // before the arrays go back to the pool
+  cudaDeviceSynchronize();
   DevBuf<double>* d[] = {&h->dx, &h->dy, &h->dz, &h->stage, &h->t_E, &h->t_A, &h->t_A2, &h->b_E, &h->b_nu, &h->b_A,
                          &h->b_i11, &h->b_i22, &h->b_i12, &h->b_it, &h->b_ks, &h->b_ax, &h->b_ay, &h->b_az,
                          &h->p_E, &h->p_nu, &h->p_t, &h->p_ks, &h->V, &h->values};
@@ -1490,8 +1542,10 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
     if (ev) cudaEventDestroy(ev);
   for (auto& ev : h->res_ev)
     if (ev) cudaEventDestroy(ev);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  // the remaining device arrays are freed by their destructors, in the stream's order: the stream goes last
+  cudaStream_t s = h->stream;
   delete h;
+  if (s) cudaStreamDestroy(s);
   return FEM_GPU_OK;
 }
 

@@ -291,6 +291,11 @@ int fem_gpu_results_last_ms(fem_gpu_t* h, float* ms);
 /* element numbers of one kind (0 truss, 1 beam, 2 plate) in call order (n of that kind, host array) */
 int fem_gpu_get_element_numbers(fem_gpu_t* h, int kind, uint32_t* numbers);
 
+/* Device arrays of every model and batch come from one stream-ordered memory pool per device that keeps
+ * freed memory for reuse (no cudaMalloc / cudaFree on the assembly path after the first model).  This hands
+ * the cached memory of the current device back to the driver (after a device synchronisation). */
+int fem_gpu_release_cached_memory(void);
+
 /* Dense assembly of one small structure without any device allocation.
  * No counterpart in the reference: it serves callers that cannot call
  * cudaMalloc -- hosts that own all device memory through their own pool or
