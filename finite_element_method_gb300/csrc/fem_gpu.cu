@@ -1259,6 +1259,9 @@ struct fem_gpu {
   size_t n_nodes = 0;
   HostVec<uint32_t> idx_number;
   HostVec<CoordKey> node_ck;  // normalised coordinate bits by index
+  // node_coords holds the nodes [0, coords_built): bulk calls check coordinates on the GPU and leave the
+  // host registry behind; a single-node call brings it up to date first
+  size_t coords_built = 0;
   NumberMap node_idx;             // number -> index
   PartTable node_coords;          // coordinate hash -> index
   DevBuf<double> dx, dy, dz;
@@ -1285,6 +1288,7 @@ struct fem_gpu {
   std::vector<uint32_t> p_num, p_nodes;
   NumberMap p_by_num;
   PartTable p_sets;  // sorted node-number set hash -> element index
+  size_t sets_built = 0;  // p_sets holds the plates [0, sets_built) (bulk calls check node sets on the GPU)
   DevBuf<int32_t> p_n1, p_n2, p_n3, p_n4;
   DevBuf<double> p_E, p_nu, p_t, p_ks;
   // loads: nodal contributions (DOF, value) in call order and the forces vector they sum to
@@ -1409,6 +1413,160 @@ cudaError_t upload(DevBuf<T>& buf, size_t at, const T* src, size_t n, cudaStream
 
 // runs the validation kernel over [begin, begin+count) and returns the first
 // failing offset (or count) and its status code
+// ---- duplicate checks of bulk calls on the GPU ------------------------------------------------------------
+// Items are grouped by a 63-bit hash of their key (radix sort of (hash, item), stable, so a group lists its
+// items in call order); inside a group an item is compared exactly with the earlier ones.  The result is the
+// smallest item equal to an earlier item -- the first failure a sequential pass over the registry would meet.
+__device__ __forceinline__ unsigned long long dev_mix64(unsigned long long x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return x;
+}
+constexpr unsigned long long kNoKey = ~0ull;  // items that equal nothing sort last
+
+// node coordinates: the model's nodes [0, start) on the device (SoA), then the call's nodes (interleaved)
+struct CoordSource {
+  const double *x, *y, *z, *xyz;
+  size_t start;
+  __device__ __forceinline__ void get(size_t i, double& a, double& b, double& c) const {
+    if (i < start) {
+      a = x[i];
+      b = y[i];
+      c = z[i];
+    } else {
+      const double* p = xyz + 3 * (i - start);
+      a = p[0];
+      b = p[1];
+      c = p[2];
+    }
+  }
+};
+
+__global__ void k_coord_keys(size_t n, CoordSource src, unsigned long long* __restrict__ key, uint32_t* __restrict__ idx) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double a, b, c;
+  src.get(i, a, b, c);
+  idx[i] = (uint32_t)i;
+  if (a != a || b != b || c != c) {  // NaN coordinates equal no other (the reference compares with ==)
+    key[i] = kNoKey;
+    return;
+  }
+  if (a == 0.0) a = 0.0;  // -0.0 == 0.0
+  if (b == 0.0) b = 0.0;
+  if (c == 0.0) c = 0.0;
+  const unsigned long long ha = (unsigned long long)__double_as_longlong(a),
+                           hb = (unsigned long long)__double_as_longlong(b),
+                           hc = (unsigned long long)__double_as_longlong(c);
+  key[i] = dev_mix64(ha ^ dev_mix64(hb ^ dev_mix64(hc))) >> 1;
+}
+
+__global__ void k_coord_dups(size_t n, const unsigned long long* __restrict__ skey, const uint32_t* __restrict__ sidx,
+                             CoordSource src, unsigned long long* first) {
+  const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k == 0 || k >= n || skey[k] == kNoKey || skey[k - 1] != skey[k]) return;
+  const uint32_t j = sidx[k];
+  double a, b, c;
+  src.get(j, a, b, c);
+  for (size_t p = k; p-- > 0 && skey[p] == skey[k];) {
+    double a2, b2, c2;
+    src.get(sidx[p], a2, b2, c2);
+    if (a2 == a && b2 == b && c2 == c) {
+      atomicMin(first, (unsigned long long)j);
+      return;
+    }
+  }
+}
+
+// plate node sets (node indexes, which map one to one to node numbers), sorted by a comparator network
+__device__ __forceinline__ uint4 dev_sorted4(int32_t p, int32_t q, int32_t r, int32_t s) {
+  uint32_t a = (uint32_t)p, b = (uint32_t)q, c = (uint32_t)r, d = (uint32_t)s, t;
+#define FEM_DSWAP(x, y) \
+  if (y < x) {          \
+    t = x;              \
+    x = y;              \
+    y = t;              \
+  }
+  FEM_DSWAP(a, b)
+  FEM_DSWAP(c, d)
+  FEM_DSWAP(a, c)
+  FEM_DSWAP(b, d)
+  FEM_DSWAP(b, c)
+#undef FEM_DSWAP
+  return make_uint4(a, b, c, d);
+}
+
+__global__ void k_set4_keys(size_t n, const int32_t* __restrict__ n1, const int32_t* __restrict__ n2,
+                            const int32_t* __restrict__ n3, const int32_t* __restrict__ n4,
+                            unsigned long long* __restrict__ key, uint32_t* __restrict__ idx) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint4 v = dev_sorted4(n1[i], n2[i], n3[i], n4[i]);
+  idx[i] = (uint32_t)i;
+  key[i] = dev_mix64(((unsigned long long)v.x << 32 | v.y) ^ dev_mix64((unsigned long long)v.z << 32 | v.w)) >> 1;
+}
+
+__global__ void k_set4_dups(size_t n, const unsigned long long* __restrict__ skey, const uint32_t* __restrict__ sidx,
+                            const int32_t* __restrict__ n1, const int32_t* __restrict__ n2,
+                            const int32_t* __restrict__ n3, const int32_t* __restrict__ n4, unsigned long long* first) {
+  const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k == 0 || k >= n || skey[k - 1] != skey[k]) return;
+  const uint32_t j = sidx[k];
+  const uint4 v = dev_sorted4(n1[j], n2[j], n3[j], n4[j]);
+  for (size_t p = k; p-- > 0 && skey[p] == skey[k];) {
+    const uint32_t i = sidx[p];
+    const uint4 w = dev_sorted4(n1[i], n2[i], n3[i], n4[i]);
+    if (w.x == v.x && w.y == v.y && w.z == v.z && w.w == v.w) {
+      atomicMin(first, (unsigned long long)j);
+      return;
+    }
+  }
+}
+
+// a cub device-wide call: size query, temporary storage from the handle, the call
+template <class F>
+int cub_call(fem_gpu* h, F f) {
+  size_t bytes = 0;
+  CK(f((void*)nullptr, bytes));
+  CK(h->cub_tmp.reserve(bytes ? bytes : 1, h->stream));
+  CK(f((void*)h->cub_tmp.p, bytes));
+  return FEM_GPU_OK;
+}
+
+// The smallest of the items [0, total) that equals an earlier item (total when none): keys(key, idx) launches
+// the key kernel over [0, total), dups(skey, sidx, first) the comparison over the sorted items.
+template <class Keys, class Dups>
+int first_duplicate(fem_gpu* h, size_t total, Keys keys, Dups dups, size_t* first) {
+  *first = total;
+  if (total < 2) return FEM_GPU_OK;
+  cudaStream_t s = h->stream;
+  DevBuf<unsigned long long> key, skey, out;
+  DevBuf<uint32_t> idx, sidx;
+  CK(key.reserve(total, s));
+  CK(skey.reserve(total, s));
+  CK(idx.reserve(total, s));
+  CK(sidx.reserve(total, s));
+  CK(out.reserve(1, s));
+  const unsigned long long none = total;
+  CK(cudaMemcpyAsync(out.p, &none, sizeof none, cudaMemcpyHostToDevice, s));
+  keys(key.p, idx.p);
+  CK(cudaGetLastError());
+  int st = cub_call(h, [&](void* tmp, size_t& bytes) {
+    return cub::DeviceRadixSort::SortPairs(tmp, bytes, key.p, skey.p, idx.p, sidx.p, (int64_t)total, 0, 64, s);
+  });
+  if (st) return st;
+  dups(skey.p, sidx.p, out.p);
+  CK(cudaGetLastError());
+  unsigned long long f = 0;
+  CK(cudaMemcpyAsync(&f, out.p, sizeof f, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  *first = (size_t)f;
+  return FEM_GPU_OK;
+}
+
 template <class Launch>
 int first_failure(fem_gpu* h, size_t count, Launch launch, size_t* first_bad, int* code) {
   *first_bad = count;
@@ -1628,6 +1786,59 @@ size_t registry_pass(unsigned T, size_t limit, const uint8_t* own_a, const uint8
 }
 }  // namespace
 
+namespace {
+// Registry entries of items that bulk calls checked on the GPU go in when a call first needs the host
+// registry: keys in parallel, then each thread inserts its partitions' keys in item order.
+template <class Key>
+void registry_catch_up(PartTable& reg, size_t b0, size_t n, Key key) {
+  if (!n) return;
+  const unsigned T = n >= kParallelAdd ? add_threads() : 1u;
+  const PartOwner owner(T);
+  HostVec<uint64_t> hs(n);
+  HostVec<uint8_t> own(n);
+  parallel_chunks(T, n, [&](unsigned, size_t b, size_t e) {
+    for (size_t q = b; q < e; ++q) {
+      uint64_t k = 0;
+      own[q] = key(b0 + q, &k) ? owner(k) : (uint8_t)0xff;
+      hs[q] = k;
+    }
+  });
+  run_threads(T, [&](unsigned t) {
+    const size_t ahead = 8 * (size_t)T;
+    for (size_t q = 0; q < n; ++q) {
+      if (q + ahead < n && own[q + ahead] == t) reg.prefetch(hs[q + ahead]);
+      if (own[q] == t) reg.insert(hs[q], (int64_t)(b0 + q));
+    }
+  });
+}
+
+void ensure_coords(fem_gpu* h) {
+  if (h->coords_built >= h->n_nodes) return;
+  h->node_coords.reserve(h->n_nodes);
+  registry_catch_up(h->node_coords, h->coords_built, h->n_nodes - h->coords_built, [&](size_t i, uint64_t* k) {
+    const CoordKey& ck = h->node_ck[i];
+    double x, y, z;
+    memcpy(&x, &ck.a, 8);
+    memcpy(&y, &ck.b, 8);
+    memcpy(&z, &ck.c, 8);
+    if (!(x == x && y == y && z == z)) return false;  // NaN coordinates are never equal to any
+    *k = coord_hash(ck);
+    return true;
+  });
+  h->coords_built = h->n_nodes;
+}
+
+void ensure_sets(fem_gpu* h) {
+  if (h->sets_built >= h->np) return;
+  h->p_sets.reserve(h->np);
+  registry_catch_up(h->p_sets, h->sets_built, h->np - h->sets_built, [&](size_t e, uint64_t* k) {
+    *k = set4_hash(sorted4(&h->p_nodes[4 * e]));
+    return true;
+  });
+  h->sets_built = h->np;
+}
+}  // namespace
+
 // add_node, methods_for_node_data_handle.rs:39-79
 extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const double* xyz, size_t n,
                                  size_t* n_added) {
@@ -1638,7 +1849,6 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
   size_t start = h->n_nodes, k = 0;
   int code = FEM_GPU_OK;
   h->node_idx.reserve(h->n_nodes + n);
-  h->node_coords.reserve(h->n_nodes + n);
   h->node_ck.reserve(h->n_nodes + n);
   h->idx_number.reserve(h->n_nodes + n);
   if (n >= kParallelAdd) {
@@ -1647,24 +1857,17 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
     const size_t room = h->nodes_number > start ? (size_t)h->nodes_number - start : 0;
     const size_t limit = std::min(n, room);
     const PartOwner owner(T);
-    HostVec<uint64_t> chash(n);
-    HostVec<uint8_t> pa(n), pb(n);
+    HostVec<uint8_t> pa(n), pb(n, 0xff);  // role B (coordinates) is checked on the GPU
     std::vector<uint32_t> tmax(T, 0);
     h->node_ck.resize(start + n);
     h->idx_number.resize(start + n);
+    // the call's coordinates go up first: the GPU checks them against every node while the host checks numbers
+    CK(upload(h->stage, 0, xyz, 3 * n, h->stream));
     parallel_chunks(T, n, [&](unsigned t, size_t b, size_t e) {
       uint32_t mx = 0;
       for (size_t q = b; q < e; ++q) {
-        const double x = xyz[3 * q], y = xyz[3 * q + 1], z = xyz[3 * q + 2];
-        const CoordKey ck = coord_key(x, y, z);
-        h->node_ck[start + q] = ck;
+        h->node_ck[start + q] = coord_key(xyz[3 * q], xyz[3 * q + 1], xyz[3 * q + 2]);
         h->idx_number[start + q] = numbers[q];
-        if (x == x && y == y && z == z) {
-          chash[q] = coord_hash(ck);
-          pb[q] = owner(chash[q]);
-        } else {
-          pb[q] = 0xff;  // NaN coordinates are never equal to any
-        }
         mx = std::max(mx, numbers[q]);
       }
       tmax[t] = mx;
@@ -1673,27 +1876,35 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
     parallel_chunks(T, n, [&](unsigned, size_t b, size_t e) {
       for (size_t q = b; q < e; ++q) pa[q] = owner.of_part(h->node_idx.part(numbers[q]));
     });
-    const HostVec<CoordKey>& known = h->node_ck;
     int role = 0;
-    const size_t f = registry_pass(
+    size_t f = registry_pass(
         T, limit, pa.data(), pb.data(),
         [&](size_t q) {
           if (h->node_idx.find(numbers[q]) >= 0) return false;
           h->node_idx.insert(numbers[q], (int64_t)(start + q));
           return true;
         },
-        [&](size_t q) {
-          const CoordKey& ck = known[start + q];
-          if (h->node_coords.find(chash[q], [&](int64_t i) { return known[(size_t)i] == ck; }) >= 0) return false;
-          h->node_coords.insert(chash[q], (int64_t)(start + q));
-          return true;
+        [&](size_t) { return true; }, [&](size_t q) { h->node_idx.prefetch(numbers[q]); }, [&](size_t) {}, &role);
+    // exact coordinates: the smallest new node equal to an earlier node (of the model or of the call)
+    const CoordSource src{h->dx.p, h->dy.p, h->dz.p, h->stage.p, start};
+    const size_t total = start + n;
+    size_t fc = total;
+    st = first_duplicate(
+        h, total,
+        [&](unsigned long long* key, uint32_t* idx) {
+          k_coord_keys<<<grid_for(total, 256), 256, 0, h->stream>>>(total, src, key, idx);
         },
-        [&](size_t q) { h->node_idx.prefetch(numbers[q]); }, [&](size_t q) { h->node_coords.prefetch(chash[q]); },
-        &role);
-    for (size_t q = f; q < limit; ++q) {  // entries of items at or after the first failure go again
-      h->node_idx.erase(numbers[q], (int64_t)(start + q));
-      if (pb[q] != 0xff) h->node_coords.erase(chash[q], (int64_t)(start + q));
+        [&](const unsigned long long* skey, const uint32_t* sidx, unsigned long long* out) {
+          k_coord_dups<<<grid_for(total, 256), 256, 0, h->stream>>>(total, skey, sidx, src, out);
+        },
+        &fc);
+    if (st) return st;
+    if (fc >= start && fc - start < f) {  // (nodes of the model are distinct: fc < start cannot happen)
+      f = fc - start;
+      role = 2;
     }
+    for (size_t q = f; q < limit; ++q)  // entries of items at or after the first failure go again
+      h->node_idx.erase(numbers[q], (int64_t)(start + q));
     h->node_ck.resize(start + f);
     h->idx_number.resize(start + f);
     h->n_nodes = start + f;
@@ -1711,6 +1922,10 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
     }
   }
   constexpr size_t kAhead = 8;  // prefetch distance (entries) into the coordinate registry
+  if (n < kParallelAdd) {
+    ensure_coords(h);
+    h->node_coords.reserve(h->n_nodes + n);
+  }
   if (n < kParallelAdd)
     for (size_t q = 0; q < std::min(n, kAhead); ++q)
       h->node_coords.prefetch(coord_hash(coord_key(xyz[3 * q], xyz[3 * q + 1], xyz[3 * q + 2])));
@@ -1747,11 +1962,13 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
     h->idx_number.push_back(num);
     h->n_nodes++;
   }
+  if (n < kParallelAdd) h->coords_built = h->n_nodes;
   if (n_added) *n_added = k;
   size_t m = h->n_nodes - start;
   if (m) {
-    // the accepted prefix of the caller's interleaved xyz goes up as is and is split on the device
-    CK(upload(h->stage, 0, xyz, 3 * m, h->stream));
+    // the accepted prefix of the caller's interleaved xyz goes up as is (bulk calls sent it already) and is
+    // split on the device
+    if (n < kParallelAdd) CK(upload(h->stage, 0, xyz, 3 * m, h->stream));
     k_split_xyz<<<grid_for(m, 256), 256, 0, h->stream>>>(m, h->stage.p, h->dx.p + start, h->dy.p + start,
                                                          h->dz.p + start);
     CK(cudaGetLastError());
@@ -1846,8 +2063,7 @@ int plate_checks(fem_gpu* h, const uint32_t* numbers, const uint32_t* nodes, siz
   const size_t base = h->np;
   for (int q = 0; q < 4; ++q) id[q].resize(n);
   const PartOwner owner(T);
-  HostVec<uint64_t> hs(n);
-  HostVec<uint8_t> pa(n), pb(n);
+  HostVec<uint8_t> pa(n), pb(n, 0xff);  // role B (node sets) is checked on the GPU
   std::vector<size_t> tmiss(T, n), trep(T, n);
   std::vector<uint32_t> tmax(T, 0);
   parallel_chunks(T, n, [&](unsigned t, size_t b, size_t e) {
@@ -1863,42 +2079,49 @@ int plate_checks(fem_gpu* h, const uint32_t* numbers, const uint32_t* nodes, siz
       if (miss && tmiss[t] == n) tmiss[t] = q;
       const Set4 key = sorted4(nn);
       if ((key.s[0] == key.s[1] || key.s[1] == key.s[2] || key.s[2] == key.s[3]) && trep[t] == n) trep[t] = q;
-      hs[q] = set4_hash(key);
-      pb[q] = owner(hs[q]);
       mx = std::max(mx, numbers[q]);
     }
     tmax[t] = mx;
   });
   const size_t limit = *std::min_element(tmiss.begin(), tmiss.end());
   if (*std::min_element(trep.begin(), trep.end()) < limit) return -1;
+  // the node indexes of the items before the first missing node go up now: the GPU checks their node sets
+  // against every plate's while the host checks the numbers
+  for (int c = 0; c < 4; ++c) {
+    DevBuf<int32_t>& dst = c == 0 ? h->p_n1 : c == 1 ? h->p_n2 : c == 2 ? h->p_n3 : h->p_n4;
+    CK(upload(dst, base, id[c].data(), limit, h->stream));
+  }
   h->p_by_num.fit(*std::max_element(tmax.begin(), tmax.end()));
   parallel_chunks(T, n, [&](unsigned, size_t b, size_t e) {
     for (size_t q = b; q < e; ++q) pa[q] = owner.of_part(h->p_by_num.part(numbers[q]));
   });
-  const size_t np0 = h->np;
   int role = 0;
-  const size_t f = registry_pass(
+  size_t f = registry_pass(
       T, limit, pa.data(), pb.data(),
       [&](size_t q) {
         if (h->p_by_num.find(numbers[q]) >= 0) return false;
         h->p_by_num.insert(numbers[q], (int64_t)(base + q));
         return true;
       },
-      [&](size_t q) {
-        const Set4 key = sorted4(nodes + 4 * q);
-        const bool same = h->p_sets.find(hs[q], [&](int64_t e) {
-          const uint32_t* mm = (size_t)e < np0 ? &h->p_nodes[4 * (size_t)e] : nodes + 4 * ((size_t)e - np0);
-          return sorted4(mm) == key;
-        }) >= 0;
-        if (same) return false;
-        h->p_sets.insert(hs[q], (int64_t)(base + q));
-        return true;
+      [&](size_t) { return true; }, [&](size_t q) { h->p_by_num.prefetch(numbers[q]); }, [&](size_t) {}, &role);
+  const size_t total = base + limit;
+  size_t fs = total;
+  const int32_t *n1 = h->p_n1.p, *n2 = h->p_n2.p, *n3 = h->p_n3.p, *n4 = h->p_n4.p;
+  const int st = first_duplicate(
+      h, total,
+      [&](unsigned long long* key, uint32_t* idx) {
+        k_set4_keys<<<grid_for(total, 256), 256, 0, h->stream>>>(total, n1, n2, n3, n4, key, idx);
       },
-      [&](size_t q) { h->p_by_num.prefetch(numbers[q]); }, [&](size_t q) { h->p_sets.prefetch(hs[q]); }, &role);
-  for (size_t q = f; q < limit; ++q) {
-    h->p_by_num.erase(numbers[q], (int64_t)(base + q));
-    h->p_sets.erase(hs[q], (int64_t)(base + q));
+      [&](const unsigned long long* skey, const uint32_t* sidx, unsigned long long* out) {
+        k_set4_dups<<<grid_for(total, 256), 256, 0, h->stream>>>(total, skey, sidx, n1, n2, n3, n4, out);
+      },
+      &fs);
+  if (st) return st;
+  if (fs >= base && fs - base < f) {  // (the model's plates have distinct node sets: fs < base cannot happen)
+    f = fs - base;
+    role = 2;
   }
+  for (size_t q = f; q < limit; ++q) h->p_by_num.erase(numbers[q], (int64_t)(base + q));
   for (int c = 0; c < 4; ++c) id[c].resize(f);
   *passed = f;
   if (f == n) return FEM_GPU_OK;
@@ -2144,7 +2367,6 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
   std::string host_err;
   size_t k = 0;
   h->p_by_num.reserve(h->np + n);
-  h->p_sets.reserve(h->np + n);
   h->p_nodes.reserve(4 * (h->np + n));
   h->p_num.reserve(h->np + n);
   bool sequential = n < kParallelAdd;
@@ -2155,7 +2377,13 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
       sequential = true;
       k = 0;
       for (auto& v : id) v.clear();
+    } else if (host_code >= FEM_GPU_ERR_CUDA) {
+      return host_code;
     }
+  }
+  if (sequential) {
+    ensure_sets(h);
+    h->p_sets.reserve(h->np + n);
   }
   for (; k < n && sequential; ++k) {
     if (k + kRegAhead < n) {
@@ -2204,10 +2432,12 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
   }
   if (host_code) host_err = h->err;
   size_t m = k, base = h->np;
-  CK(upload(h->p_n1, base, id[0].data(), m, h->stream));
-  CK(upload(h->p_n2, base, id[1].data(), m, h->stream));
-  CK(upload(h->p_n3, base, id[2].data(), m, h->stream));
-  CK(upload(h->p_n4, base, id[3].data(), m, h->stream));
+  if (sequential) {  // (the bulk checks sent the node indexes up already)
+    CK(upload(h->p_n1, base, id[0].data(), m, h->stream));
+    CK(upload(h->p_n2, base, id[1].data(), m, h->stream));
+    CK(upload(h->p_n3, base, id[2].data(), m, h->stream));
+    CK(upload(h->p_n4, base, id[3].data(), m, h->stream));
+  }
   CK(upload(h->p_E, base, young, m, h->stream));
   CK(upload(h->p_nu, base, poisson, m, h->stream));
   CK(upload(h->p_t, base, thickness, m, h->stream));
@@ -2224,11 +2454,12 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
   size_t accepted = std::min(m, bad);
   for (size_t j = accepted; j < m; ++j) {
     h->p_by_num.erase(numbers[j], (int64_t)(base + j));
-    h->p_sets.erase(set4_hash(sorted4(nodes + 4 * j)), (int64_t)(base + j));
+    if (sequential) h->p_sets.erase(set4_hash(sorted4(nodes + 4 * j)), (int64_t)(base + j));
   }
   h->p_num.insert(h->p_num.end(), numbers, numbers + accepted);
   h->p_nodes.insert(h->p_nodes.end(), nodes, nodes + 4 * accepted);
   h->np += accepted;
+  if (sequential) h->sets_built = h->np;
   h->append_run(kPlate, base, accepted);
   if (n_added) *n_added = accepted;
   if (bad < m) {
@@ -2290,14 +2521,6 @@ int numeric_launch(fem_gpu* h) {
   return FEM_GPU_OK;
 }
 
-template <class F>
-int cub_call(fem_gpu* h, F f) {
-  size_t bytes = 0;
-  CK(f((void*)nullptr, bytes));
-  CK(h->cub_tmp.reserve(bytes ? bytes : 1, h->stream));
-  CK(f((void*)h->cub_tmp.p, bytes));
-  return FEM_GPU_OK;
-}
 
 int symbolic(fem_gpu* h) {
   cudaStream_t s = h->stream;
@@ -2595,6 +2818,10 @@ extern "C" int fem_gpu_set_node_coordinates(fem_gpu_t* h, const double* xyz, siz
   CK(cudaMemcpyAsync(h->dy.p, b.data(), n_nodes * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(h->dz.p, c.data(), n_nodes * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  // later duplicate checks compare against the nodes' new coordinates
+  for (size_t i = 0; i < n_nodes; ++i) h->node_ck[i] = coord_key(a[i], b[i], c[i]);
+  h->node_coords = PartTable();
+  h->coords_built = 0;
   h->numeric_done = false;
   return FEM_GPU_OK;
 }

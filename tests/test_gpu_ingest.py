@@ -141,3 +141,77 @@ def test_bulk_plates(case):
     g.assemble()
     for a, b in zip(g.stiffness_csr(), o.csr()):
         np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+# -- the registries of bulk calls are checked on the GPU and built on the host only when a later call needs
+#    them: every mix of bulk and single calls must still see every earlier node and plate
+
+def two_layers():
+    """the grid twice, the second layer at z = 1 (node numbers continue), each with its quads"""
+    numbers, xyz, quads, _ = grid()
+    n = len(numbers)
+    xyz2 = xyz.copy()
+    xyz2[:, 2] = 1.0
+    return numbers, xyz, quads, numbers + n, xyz2, quads + n
+
+
+def test_bulk_then_single_and_second_bulk_nodes():
+    n1, x1, _, n2, x2, _ = two_layers()
+    g, o = both(len(n1) + len(n2) + 50000)
+    for m in (g, o):
+        m.add_nodes(n1, x1)
+    # a single node at the coordinates of a bulk-added node, then a fresh one
+    expect_same_failure(lambda: g.add_node(10 ** 6, *x1[1234]), lambda: o.add_node(10 ** 6, *x1[1234]))
+    for m in (g, o):
+        m.add_node(10 ** 6, 1e3, 1e3, 0.0)
+    # a second bulk call whose item 30000 repeats the coordinates of a first-call node
+    bad = x2.copy()
+    bad[30000] = x1[77]
+    expect_same_failure(lambda: g.add_nodes(n2, bad), lambda: o.add_nodes(n2, bad))
+    np.testing.assert_array_equal(g.index_node_numbers(), o.index_node_numbers())
+    assert g.node_count() == len(n1) + 1 + 30000
+    # and a duplicate of the single node inside a bulk call
+    more_n = np.arange(2 * 10 ** 6, 2 * 10 ** 6 + 40000, dtype=np.uint32)
+    more_x = np.stack([np.arange(40000) * 0.25 + 5e3, np.zeros(40000), np.zeros(40000)], -1)
+    more_x[35000] = [1e3, 1e3, -0.0]  # -0.0 == 0.0
+    expect_same_failure(lambda: g.add_nodes(more_n, more_x), lambda: o.add_nodes(more_n, more_x))
+    np.testing.assert_array_equal(g.index_node_numbers(), o.index_node_numbers())
+
+
+def test_bulk_then_single_and_second_bulk_plates():
+    n1, x1, q1, n2, x2, q2 = two_layers()
+    m = len(q1)
+    E, nu, t, ks = 70e9, 0.3, 0.02, 5 / 6
+    g, o = both(len(n1) + len(n2))
+    for x in (g, o):
+        x.add_nodes(n1, x1)
+        x.add_nodes(n2, x2)
+        x.add_plates(np.arange(1, m + 1), q1, E, nu, t, ks)
+    # a single plate on the node set of a bulk-added plate (other order)
+    q = q1[321][[1, 2, 3, 0]]
+    expect_same_failure(lambda: g.add_plate(10 ** 6, *q, E, nu, t, ks), lambda: o.add_plate(10 ** 6, *q, E, nu, t, ks))
+    # a second bulk call whose item 17000 repeats a first-call plate's node set
+    bad = q2.copy()
+    bad[17000] = q1[4321][[3, 2, 1, 0]]
+    expect_same_failure(lambda: g.add_plates(np.arange(m + 1, 2 * m + 1), bad, E, nu, t, ks),
+                        lambda: o.add_plates(np.arange(m + 1, 2 * m + 1), bad, E, nu, t, ks))
+    assert g.element_counts()[2] == m + 17000
+    # the single path sees the second bulk call's plates too
+    q = q2[5][[2, 3, 0, 1]]
+    expect_same_failure(lambda: g.add_plate(10 ** 6 + 1, *q, E, nu, t, ks),
+                        lambda: o.add_plate(10 ** 6 + 1, *q, E, nu, t, ks))
+    g.assemble()
+    for a, b in zip(g.stiffness_csr(), o.csr()):
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def test_moved_nodes_are_checked_at_their_new_coordinates():
+    numbers, xyz, _, _ = grid()
+    g = FEM(1e-12, 1e-12, len(numbers) + 2)
+    g.add_nodes(numbers, xyz)
+    moved = xyz.copy()
+    moved[500] = [7e3, 7e3, 7e3]
+    g.set_node_coordinates(moved)
+    g.add_node(10 ** 6, *xyz[500])  # the old place is free now
+    with pytest.raises(FEMError, match="already exists"):
+        g.add_node(10 ** 6 + 1, 7e3, 7e3, 7e3)
