@@ -1274,6 +1274,8 @@ struct fem_gpu {
   std::vector<uint32_t> t_num;
   NumberMap t_by_num;  // number -> element index
   PartTable t_pairs;   // node pair -> element index
+  std::vector<uint32_t> t_nodes;  // node numbers per truss (2 each)
+  size_t t_pairs_built = 0;       // t_pairs holds the trusses [0, t_pairs_built) (bulk calls check on the GPU)
   DevBuf<int32_t> t_n1, t_n2;
   DevBuf<double> t_E, t_A, t_A2;
   // beam
@@ -1281,6 +1283,8 @@ struct fem_gpu {
   std::vector<uint32_t> b_num;
   NumberMap b_by_num;
   PartTable b_pairs;
+  std::vector<uint32_t> b_nodes;
+  size_t b_pairs_built = 0;
   DevBuf<int32_t> b_n1, b_n2;
   DevBuf<double> b_E, b_nu, b_A, b_i11, b_i22, b_i12, b_it, b_ks, b_ax, b_ay, b_az;
   // plate
@@ -1567,6 +1571,23 @@ int first_duplicate(fem_gpu* h, size_t total, Keys keys, Dups dups, size_t* firs
   return FEM_GPU_OK;
 }
 
+// two-node elements: the node pair itself (smaller index high) is the key, so equal keys are equal pairs
+__global__ void k_pair_keys(size_t n, const int32_t* __restrict__ n1, const int32_t* __restrict__ n2,
+                            unsigned long long* __restrict__ key, uint32_t* __restrict__ idx) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t a = (uint32_t)n1[i], b = (uint32_t)n2[i];
+  key[i] = a < b ? ((unsigned long long)a << 32 | b) : ((unsigned long long)b << 32 | a);
+  idx[i] = (uint32_t)i;
+}
+
+__global__ void k_pair_dups(size_t n, const unsigned long long* __restrict__ skey, const uint32_t* __restrict__ sidx,
+                            unsigned long long* first) {
+  const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k == 0 || k >= n || skey[k - 1] != skey[k]) return;
+  atomicMin(first, (unsigned long long)sidx[k]);
+}
+
 template <class Launch>
 int first_failure(fem_gpu* h, size_t count, Launch launch, size_t* first_bad, int* code) {
   *first_bad = count;
@@ -1828,6 +1849,16 @@ void ensure_coords(fem_gpu* h) {
   h->coords_built = h->n_nodes;
 }
 
+void ensure_pairs(PartTable& reg, size_t* built, size_t count, const std::vector<uint32_t>& nodes) {
+  if (*built >= count) return;
+  reg.reserve(count);
+  registry_catch_up(reg, *built, count - *built, [&](size_t e, uint64_t* k) {
+    *k = pair_key(nodes[2 * e], nodes[2 * e + 1]);
+    return true;
+  });
+  *built = count;
+}
+
 void ensure_sets(fem_gpu* h) {
   if (h->sets_built >= h->np) return;
   h->p_sets.reserve(h->np);
@@ -1994,15 +2025,14 @@ int lookup_node(fem_gpu* h, uint32_t num, int32_t* idx) {
 // sequential loop's order: both nodes exist, the number is new, the node pair is new.  Returns the
 // status of the first failing item (message set as the sequential loop would set it); *passed is
 // the number of items before it, whose node indices are in i1, i2.
-int two_node_checks(fem_gpu* h, const char* kind, NumberMap& by_num, PartTable& pairs, size_t base,
-                    const uint32_t* numbers, const uint32_t* nodes, size_t n, HostVec<int32_t>& i1,
+int two_node_checks(fem_gpu* h, const char* kind, NumberMap& by_num, DevBuf<int32_t>& dn1, DevBuf<int32_t>& dn2,
+                    size_t base, const uint32_t* numbers, const uint32_t* nodes, size_t n, HostVec<int32_t>& i1,
                     HostVec<int32_t>& i2, size_t* passed) {
   const unsigned T = add_threads();
   i1.resize(n);
   i2.resize(n);
   const PartOwner owner(T);
-  HostVec<uint64_t> pk(n);
-  HostVec<uint8_t> pa(n), pb(n);
+  HostVec<uint8_t> pa(n), pb(n, 0xff);  // role B (node pairs) is checked on the GPU
   std::vector<size_t> tmiss(T, n);
   std::vector<uint32_t> tmax(T, 0);
   parallel_chunks(T, n, [&](unsigned t, size_t b, size_t e) {
@@ -2012,35 +2042,46 @@ int two_node_checks(fem_gpu* h, const char* kind, NumberMap& by_num, PartTable& 
       if ((a < 0 || c < 0) && tmiss[t] == n) tmiss[t] = q;
       i1[q] = (int32_t)a;
       i2[q] = (int32_t)c;
-      pk[q] = pair_key(nodes[2 * q], nodes[2 * q + 1]);
-      pb[q] = owner(pk[q]);
       mx = std::max(mx, numbers[q]);
     }
     tmax[t] = mx;
   });
   const size_t limit = *std::min_element(tmiss.begin(), tmiss.end());
+  // the node indexes of the items before the first missing node go up now: the GPU checks their pairs
+  // against every element's of the kind while the host checks the numbers
+  CK(upload(dn1, base, i1.data(), limit, h->stream));
+  CK(upload(dn2, base, i2.data(), limit, h->stream));
   by_num.fit(*std::max_element(tmax.begin(), tmax.end()));
   parallel_chunks(T, n, [&](unsigned, size_t b, size_t e) {
     for (size_t q = b; q < e; ++q) pa[q] = owner.of_part(by_num.part(numbers[q]));
   });
   int role = 0;
-  const size_t f = registry_pass(
+  size_t f = registry_pass(
       T, limit, pa.data(), pb.data(),
       [&](size_t q) {
         if (by_num.find(numbers[q]) >= 0) return false;
         by_num.insert(numbers[q], (int64_t)(base + q));
         return true;
       },
-      [&](size_t q) {
-        if (pairs.find(pk[q]) >= 0) return false;
-        pairs.insert(pk[q], (int64_t)(base + q));
-        return true;
+      [&](size_t) { return true; }, [&](size_t q) { by_num.prefetch(numbers[q]); }, [&](size_t) {}, &role);
+  const size_t total = base + limit;
+  size_t fp = total;
+  const int32_t *d1 = dn1.p, *d2 = dn2.p;
+  const int st = first_duplicate(
+      h, total,
+      [&](unsigned long long* key, uint32_t* idx) {
+        k_pair_keys<<<grid_for(total, 256), 256, 0, h->stream>>>(total, d1, d2, key, idx);
       },
-      [&](size_t q) { by_num.prefetch(numbers[q]); }, [&](size_t q) { pairs.prefetch(pk[q]); }, &role);
-  for (size_t q = f; q < limit; ++q) {
-    by_num.erase(numbers[q], (int64_t)(base + q));
-    pairs.erase(pk[q], (int64_t)(base + q));
+      [&](const unsigned long long* skey, const uint32_t* sidx, unsigned long long* out) {
+        k_pair_dups<<<grid_for(total, 256), 256, 0, h->stream>>>(total, skey, sidx, out);
+      },
+      &fp);
+  if (st) return st;
+  if (fp >= base && fp - base < f) {  // (the model's elements have distinct pairs: fp < base cannot happen)
+    f = fp - base;
+    role = 2;
   }
+  for (size_t q = f; q < limit; ++q) by_num.erase(numbers[q], (int64_t)(base + q));
   i1.resize(f);
   i2.resize(f);
   *passed = f;
@@ -2155,13 +2196,18 @@ extern "C" int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const 
   std::string host_err;
   size_t k = 0;
   h->t_by_num.reserve(h->nt + n);
-  h->t_pairs.reserve(h->nt + n);
-  if (n >= kParallelAdd) {
-    host_code = two_node_checks(h, "Truss", h->t_by_num, h->t_pairs, h->nt, numbers, nodes, n, i1, i2, &k);
+  const bool bulk = n >= kParallelAdd;
+  if (bulk) {
+    host_code = two_node_checks(h, "Truss", h->t_by_num, h->t_n1, h->t_n2, h->nt, numbers, nodes, n, i1, i2, &k);
+    if (host_code >= FEM_GPU_ERR_CUDA) return host_code;
     a2v.resize(k);
     for (size_t q = 0; q < k; ++q) a2v[q] = area2 ? area2[q] : NAN;
   }
-  for (; k < n && n < kParallelAdd; ++k) {
+  if (!bulk) {
+    ensure_pairs(h->t_pairs, &h->t_pairs_built, h->nt, h->t_nodes);
+    h->t_pairs.reserve(h->nt + n);
+  }
+  for (; k < n && !bulk; ++k) {
     if (k + kRegAhead < n) {
       const uint32_t* f = nodes + 2 * (k + kRegAhead);
       h->t_pairs.prefetch(pair_key(f[0], f[1]));
@@ -2187,8 +2233,10 @@ extern "C" int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const 
   }
   if (host_code) host_err = h->err;
   size_t m = k, base = h->nt;
-  CK(upload(h->t_n1, base, i1.data(), m, h->stream));
-  CK(upload(h->t_n2, base, i2.data(), m, h->stream));
+  if (!bulk) {  // (the bulk checks sent the node indexes up already)
+    CK(upload(h->t_n1, base, i1.data(), m, h->stream));
+    CK(upload(h->t_n2, base, i2.data(), m, h->stream));
+  }
   CK(upload(h->t_E, base, young, m, h->stream));
   CK(upload(h->t_A, base, area, m, h->stream));
   CK(upload(h->t_A2, base, a2v.data(), m, h->stream));
@@ -2204,10 +2252,12 @@ extern "C" int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const 
   size_t accepted = std::min(m, bad);
   for (size_t j = accepted; j < m; ++j) {  // roll back registry entries past the failure
     h->t_by_num.erase(numbers[j], (int64_t)(base + j));
-    h->t_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]), (int64_t)(base + j));
+    if (!bulk) h->t_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]), (int64_t)(base + j));
   }
   h->t_num.insert(h->t_num.end(), numbers, numbers + accepted);
+  h->t_nodes.insert(h->t_nodes.end(), nodes, nodes + 2 * accepted);
   h->nt += accepted;
+  if (!bulk) h->t_pairs_built = h->nt;
   h->append_run(kTruss, base, accepted);
   if (n_added) *n_added = accepted;
   if (bad < m) {
@@ -2247,14 +2297,15 @@ extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const ui
   std::string host_err;
   size_t k = 0;
   h->b_by_num.reserve(h->nbm + n);
-  h->b_pairs.reserve(h->nbm + n);
+  const bool bulk = n >= kParallelAdd;
   i1.reserve(n);
   i2.reserve(n);
   ax.reserve(n);
   ay.reserve(n);
   az.reserve(n);
-  if (n >= kParallelAdd) {
-    host_code = two_node_checks(h, "Beam", h->b_by_num, h->b_pairs, h->nbm, numbers, nodes, n, i1, i2, &k);
+  if (bulk) {
+    host_code = two_node_checks(h, "Beam", h->b_by_num, h->b_n1, h->b_n2, h->nbm, numbers, nodes, n, i1, i2, &k);
+    if (host_code >= FEM_GPU_ERR_CUDA) return host_code;
     ax.resize(k);
     ay.resize(k);
     az.resize(k);
@@ -2266,7 +2317,11 @@ extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const ui
       }
     });
   }
-  for (; k < n && n < kParallelAdd; ++k) {
+  if (!bulk) {
+    ensure_pairs(h->b_pairs, &h->b_pairs_built, h->nbm, h->b_nodes);
+    h->b_pairs.reserve(h->nbm + n);
+  }
+  for (; k < n && !bulk; ++k) {
     if (k + kRegAhead < n) {
       const uint32_t* f = nodes + 2 * (k + kRegAhead);
       h->b_pairs.prefetch(pair_key(f[0], f[1]));
@@ -2294,8 +2349,10 @@ extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const ui
   }
   if (host_code) host_err = h->err;
   size_t m = k, base = h->nbm;
-  CK(upload(h->b_n1, base, i1.data(), m, h->stream));
-  CK(upload(h->b_n2, base, i2.data(), m, h->stream));
+  if (!bulk) {  // (the bulk checks sent the node indexes up already)
+    CK(upload(h->b_n1, base, i1.data(), m, h->stream));
+    CK(upload(h->b_n2, base, i2.data(), m, h->stream));
+  }
   CK(upload(h->b_E, base, young, m, h->stream));
   CK(upload(h->b_nu, base, poisson, m, h->stream));
   CK(upload(h->b_A, base, area, m, h->stream));
@@ -2318,10 +2375,12 @@ extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const ui
   size_t accepted = std::min(m, bad);
   for (size_t j = accepted; j < m; ++j) {
     h->b_by_num.erase(numbers[j], (int64_t)(base + j));
-    h->b_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]), (int64_t)(base + j));
+    if (!bulk) h->b_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]), (int64_t)(base + j));
   }
   h->b_num.insert(h->b_num.end(), numbers, numbers + accepted);
+  h->b_nodes.insert(h->b_nodes.end(), nodes, nodes + 2 * accepted);
   h->nbm += accepted;
+  if (!bulk) h->b_pairs_built = h->nbm;
   h->append_run(kBeam, base, accepted);
   if (n_added) *n_added = accepted;
   if (bad < m) {

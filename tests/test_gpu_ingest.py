@@ -215,3 +215,35 @@ def test_moved_nodes_are_checked_at_their_new_coordinates():
     g.add_node(10 ** 6, *xyz[500])  # the old place is free now
     with pytest.raises(FEMError, match="already exists"):
         g.add_node(10 ** 6 + 1, 7e3, 7e3, 7e3)
+
+
+@pytest.mark.parametrize("kind", ["truss", "beam"])
+def test_bulk_then_single_and_second_bulk_two_node_elements(kind):
+    numbers, xyz, _, bars = grid()
+    m = len(bars)
+    half = m // 2  # 40,200 per call: both calls take the bulk path
+    enums = np.arange(1, m + 1, dtype=np.uint32)
+    g, o = both(len(numbers))
+    for x in (g, o):
+        x.add_nodes(numbers, xyz)
+    if kind == "truss":
+        add = lambda x, nums, prs: x.add_trusses(nums, prs, 200e9, 3e-4)
+        one = lambda x, num, u, v: x.add_truss(num, u, v, 200e9, 3e-4)
+    else:
+        args = (210e9, 0.3, 1e-2, 3e-5, 8e-5, 0.0, 2e-5, 5 / 6, [0.0, 0.0, 1.0])
+        add = lambda x, nums, prs: x.add_beams(nums, prs, *args)
+        one = lambda x, num, u, v: x.add_beam(num, u, v, *args)
+    for x in (g, o):
+        add(x, enums[:half], bars[:half])
+    # a single element on a bulk-added pair (reversed), then a second bulk call repeating a first-call pair
+    u, v = bars[999]
+    expect_same_failure(lambda: one(g, 10 ** 6, v, u), lambda: one(o, 10 ** 6, v, u))
+    rest = bars[half:].copy()
+    rest[33000] = bars[5][::-1]
+    expect_same_failure(lambda: add(g, enums[half:], rest), lambda: add(o, enums[half:], rest))
+    assert g.element_counts()[0 if kind == "truss" else 1] == half + 33000
+    u, v = rest[7]
+    expect_same_failure(lambda: one(g, 10 ** 6 + 1, u, v), lambda: one(o, 10 ** 6 + 1, u, v))
+    g.assemble()
+    for a, b in zip(g.stiffness_csr(), o.csr()):
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
