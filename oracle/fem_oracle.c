@@ -1898,11 +1898,12 @@ int orc_plate_results(const double x1[3], const double x2[3], const double x3[3]
   const double g0 = fma(Gm[1], fma(el[3], q[2], el[2] * q[3]), Gm[0] * fma(el[2], q[0], el[3] * q[1]));
   const double g1 = fma(Gm[3], fma(el[0], q[1], el[1] * q[2]), Gm[2] * fma(el[0], q[0], el[1] * q[3]));
   const double nu = poisson, t = thickness;
+  // one division: E / (2 (1 + nu)) = E ((1 - nu) / 2) / (1 - nu^2), and t^2 / 24 by the constant 1/24
   const double dinv = 1.0 / (1.0 - nu * nu);
-  const double cm = (young * dinv) * (t * 0.25);
-  const double cbm = ((young * t) * (0.5 * dinv)) * ((t * t) / 24.0);
-  const double cs = (young / (2.0 * (1.0 + nu))) * ((t * shear_factor) * 0.25);
   const double hn = (1.0 - nu) * 0.5;
+  const double cm = (young * dinv) * (t * 0.25);
+  const double cbm = ((young * t) * (0.5 * dinv)) * ((t * t) * (1.0 / 24.0));
+  const double cs = ((young * hn) * dinv) * ((t * shear_factor) * 0.25);
   out8[0] = cm * fma(nu, e1, e0);
   out8[1] = cm * fma(nu, e0, e1);
   out8[2] = cm * (hn * e2);
