@@ -1357,6 +1357,12 @@ struct fem_gpu {
   bool numeric_done = false;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   float t_elem_ms = 0, t_reduce_ms = 0;
+  // the numeric pass as a CUDA graph (captured at its first launch after each symbolic phase)
+  cudaGraphExec_t num_graph = nullptr;
+  void drop_numeric_graph() {
+    if (num_graph) cudaGraphExecDestroy(num_graph);
+    num_graph = nullptr;
+  }
   // vector-Jacobian product
   bool vjp_inc_valid = false;
   DevBuf<int64_t> vjp_inc_off, vjp_inc;
@@ -1396,6 +1402,7 @@ struct fem_gpu {
     pattern_valid = false;
     vjp_inc_valid = false;
     numeric_done = false;
+    drop_numeric_graph();
   }
 };
 
@@ -1717,6 +1724,7 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
     h->sep_v[b].release();
   }
   h->res_buf.release();
+  h->drop_numeric_graph();
   for (auto& ev : h->ev)
     if (ev) cudaEventDestroy(ev);
   for (auto& ev : h->res_ev)
@@ -1877,6 +1885,7 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
   if (!h || (n && (!numbers || !xyz))) return FEM_GPU_ERR_ARGUMENT;
   int st = ensure_ready(h);
   if (st) return st;
+  h->drop_numeric_graph();  // the element and node arrays may move
   size_t start = h->n_nodes, k = 0;
   int code = FEM_GPU_OK;
   h->node_idx.reserve(h->n_nodes + n);
@@ -2187,6 +2196,7 @@ extern "C" int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const 
   if (!h || (n && (!numbers || !nodes || !young || !area))) return FEM_GPU_ERR_ARGUMENT;
   int st = ensure_ready(h);
   if (st) return st;
+  h->drop_numeric_graph();  // the element and node arrays may move
   HostVec<int32_t> i1, i2;
   HostVec<double> a2v;
   i1.reserve(n);
@@ -2291,6 +2301,7 @@ extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const ui
     return FEM_GPU_ERR_ARGUMENT;
   int st = ensure_ready(h);
   if (st) return st;
+  h->drop_numeric_graph();  // the element and node arrays may move
   HostVec<int32_t> i1, i2;
   HostVec<double> ax, ay, az;
   int host_code = FEM_GPU_OK;
@@ -2420,6 +2431,7 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
     return FEM_GPU_ERR_ARGUMENT;
   int st = ensure_ready(h);
   if (st) return st;
+  h->drop_numeric_graph();  // the element and node arrays may move
   HostVec<int32_t> id[4];
   for (auto& v : id) v.reserve(n);
   int host_code = FEM_GPU_OK;
@@ -2556,17 +2568,16 @@ int launch_elements(fem_gpu* h, BlockSink sink_t, BlockSink sink_b, BlockSink si
   return FEM_GPU_OK;
 }
 
-int numeric_launch(fem_gpu* h) {
-  h->sep_valid = false;  // a separation describes the stiffness it was taken from
-  h->sell_valid = false;
+// the numeric pass's operations (captured into the handle's graph); the phase events are graph nodes
+int numeric_enqueue(fem_gpu* h) {
   CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->stream));
-  CK(cudaEventRecord(h->ev[0], h->stream));
+  CK(cudaEventRecordWithFlags(h->ev[0], h->stream, cudaEventRecordExternal));
   BlockSink st{nullptr, h->V.p, h->off_t.p, h->flag.p};
   BlockSink sb{nullptr, h->V.p, h->off_b.p, h->flag.p};
   BlockSink sp{nullptr, h->V.p, h->off_p.p, h->flag.p};
   int r = launch_elements(h, st, sb, sp);
   if (r) return r;
-  CK(cudaEventRecord(h->ev[1], h->stream));
+  CK(cudaEventRecordWithFlags(h->ev[1], h->stream, cudaEventRecordExternal));
   if (h->n_blocks) {
     if (h->n_desc)
       k_block_sums<<<grid_for(h->n_desc, 256), 256, 0, h->stream>>>(h->n_desc, h->s_words, h->slot_desc.p, h->V.p,
@@ -2575,13 +2586,40 @@ int numeric_launch(fem_gpu* h) {
                       h->stream>>>((size_t)h->nnz, h->src_map.p, h->V.p, h->vs_off, h->values.p, h->flag.p);
   }
   CK(cudaGetLastError());
-  CK(cudaEventRecord(h->ev[2], h->stream));
+  CK(cudaEventRecordWithFlags(h->ev[2], h->stream, cudaEventRecordExternal));
+  return FEM_GPU_OK;
+}
+
+// One numeric pass: a single graph launch (the pass's arrays keep their addresses until the next
+// symbolic phase, which drops the graph)
+int numeric_launch(fem_gpu* h) {
+  h->sep_valid = false;  // a separation describes the stiffness it was taken from
+  h->sell_valid = false;
+  if (!h->num_graph) {
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const int r = numeric_enqueue(h);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (r) {
+      if (g) cudaGraphDestroy(g);
+      return r;
+    }
+    if (e != cudaSuccess) return h->cuda_fail(e, "cudaStreamEndCapture");
+    const cudaError_t ei = cudaGraphInstantiate(&h->num_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+      h->num_graph = nullptr;
+      return h->cuda_fail(ei, "cudaGraphInstantiate");
+    }
+  }
+  CK(cudaGraphLaunch(h->num_graph, h->stream));
   h->numeric_done = true;
   return FEM_GPU_OK;
 }
 
 
 int symbolic(fem_gpu* h) {
+  h->drop_numeric_graph();
   cudaStream_t s = h->stream;
   size_t np = h->n_pairs;
   const size_t nrows = (size_t)h->nodes_number * 6;

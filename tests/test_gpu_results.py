@@ -154,3 +154,48 @@ def test_full_plate_mesh_sample_and_identities():
     rb = g.element_results(u.ravel())["plate"]
     assert np.max(np.abs(rb)) < 1e-6 * np.max(np.abs(r1))
     g.close()
+
+
+def test_tapered_trusses_and_skew_beams_with_product_of_inertia():
+    """element kinds and options the generated meshes do not exercise: tapered trusses (area_2), beams
+    with I12 != 0 and equal I11 = I22, local axes along x, y and skew, vertical members"""
+    rng = np.random.default_rng(21)
+    n = 40
+    xyz = rng.uniform(-3.0, 3.0, (n, 3))
+    xyz[n - 2] = xyz[0] + [0.0, 0.0, 2.0]  # vertical members 0 -> n-2 and n-1 -> 1
+    xyz[n - 1] = xyz[1] + [0.0, 0.0, -1.5]
+    g = FEM(1e-12, 1e-12, n)
+    g.add_nodes(np.arange(1, n + 1), xyz)
+    trusses, beams = [], []
+    pairs = [(a, b) for a in range(n - 2) for b in range(a + 1, n - 2)]
+    order = rng.permutation(len(pairs))[:55]
+    for e in range(25):
+        a, b = pairs[order[e]]
+        a2 = None if e % 3 == 0 else float(rng.uniform(1e-4, 5e-4))
+        g.add_truss(e + 1, a + 1, b + 1, 200e9, 3e-4, a2)
+        trusses.append((a, b, a2))
+    for e in range(30):
+        a, b = pairs[order[25 + e]]
+        if e % 2:
+            a, b = b, a
+        d = xyz[b] - xyz[a]
+        axis = [[0.0, 0.0, 1.0], [1.0, 0.0, 0.0], [0.3, -0.4, 0.5]][e % 3]
+        if abs(np.dot(d, axis)) > 0.99 * np.linalg.norm(d) * np.linalg.norm(axis):
+            axis = [0.0, 1.0, 0.0]
+        i11, i22 = (5e-5, 5e-5) if e % 4 == 0 else (8e-5, 3e-5)
+        i12 = 0.0 if e % 2 else 1e-5
+        g.add_beam(100 + e, a + 1, b + 1, 210e9, 0.3, 1.2e-2, i11, i22, i12, 2e-5, 5 / 6, axis)
+        beams.append((a, b, i11, i22, i12, axis))
+    for e, (a, b) in enumerate(((0, n - 2), (n - 1, 1))):
+        g.add_beam(200 + e, a + 1, b + 1, 210e9, 0.3, 1.2e-2, 8e-5, 3e-5, 1e-5 * e, 2e-5, 5 / 6, [1.0, 0.0, 0.0])
+        beams.append((a, b, 8e-5, 3e-5, 1e-5 * e, [1.0, 0.0, 0.0]))
+    disp = rng.standard_normal(6 * n) * 1e-3
+    got = g.element_results(disp)
+    for e, (a, b, a2) in enumerate(trusses):
+        want = fo.truss_results(xyz[a], xyz[b], 200e9, 3e-4, a2, np.r_[disp[6 * a:6 * a + 3], disp[6 * b:6 * b + 3]])
+        assert got["truss"][e, 0] == want[0]
+    for e, (a, b, i11, i22, i12, axis) in enumerate(beams):
+        want = fo.beam_results(xyz[a], xyz[b], 210e9, 0.3, 1.2e-2, i11, i22, i12, 2e-5, 5 / 6, axis,
+                               np.r_[disp[6 * a:6 * a + 6], disp[6 * b:6 * b + 6]])
+        assert np.array_equal(got["beam"][e], want), (e, got["beam"][e] - want)
+    g.close()
