@@ -12,9 +12,9 @@
 //     K_ba or K_bb with local indices (positions in the a and b lists);
 //   * an empty K_aa -> the reference's "K_aa is empty" error.
 // The reference collects the triplets in hash-map order; here every block is
-// a CSR matrix sorted by (row, column) -- the same set of triplets.  One warp
-// per stiffness row: coalesced reads of the row, ballots for the counts, and
-// the ballot prefix for each entry's position, so the result is
+// a CSR matrix sorted by (row, column) -- the same set of triplets.  Four
+// lanes per stiffness row read it in order; each entry's position is the row's
+// start plus the kept entries before it (ballot prefixes), so the result is
 // deterministic.
 
 enum : uint8_t { kSepExcluded = 0, kSepA = 1, kSepB = 2 };
@@ -48,28 +48,37 @@ __global__ void k_sep_classify(size_t n, const int64_t* __restrict__ row_ptr, co
   isB[i] = c == kSepB;
 }
 
-// one warp per row: how many kept entries go to each block; cnt is kSepBlocks x n, by global row
+// Four lanes per stiffness row, eight rows per warp: a row of ~20 entries would leave most of a whole
+// warp idle and make every warp a chain of dependent loads; with four lanes each load instruction reads
+// four consecutive entries of eight rows.
+constexpr int kSepLanes = 4;
+
+// how many kept entries each row sends to each block; cnt is kSepBlocks x n, by global row
 __global__ void k_sep_count(size_t n, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col_idx,
                             const double* __restrict__ val, const uint8_t* __restrict__ cls, uint32_t* __restrict__ cnt) {
-  const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) / 32;
-  const int lane = threadIdx.x & 31;
-  if (w >= n) return;
-  const uint8_t ci = cls[w];
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t row = t / kSepLanes;
+  const int sub = (int)(t % kSepLanes);
+  const uint8_t ci = row < n ? cls[row] : kSepExcluded;
+  const int64_t b = row < n ? row_ptr[row] : 0;
+  const int64_t e = ci != kSepExcluded ? row_ptr[row + 1] : b;
   uint32_t na = 0, nb = 0;
-  if (ci != kSepExcluded) {
-    for (int64_t k0 = row_ptr[w]; k0 < row_ptr[w + 1]; k0 += 32) {
-      const int64_t k = k0 + lane;
-      uint8_t cj = kSepExcluded;
-      if (k < row_ptr[w + 1] && nonzero(val[k])) cj = cls[col_idx[k]];
-      na += __popc(__ballot_sync(0xffffffffu, cj == kSepA));
-      nb += __popc(__ballot_sync(0xffffffffu, cj == kSepB));
-    }
+  for (int64_t k = b + sub; __any_sync(0xffffffffu, k < e); k += kSepLanes) {
+    uint8_t cj = kSepExcluded;
+    if (k < e && nonzero(val[k])) cj = cls[col_idx[k]];
+    na += cj == kSepA;
+    nb += cj == kSepB;
   }
-  if (lane == 0) {
-    cnt[0 * n + w] = ci == kSepA ? na : 0;  // K_aa
-    cnt[1 * n + w] = ci == kSepA ? nb : 0;  // K_ab
-    cnt[2 * n + w] = ci == kSepB ? na : 0;  // K_ba
-    cnt[3 * n + w] = ci == kSepB ? nb : 0;  // K_bb
+#pragma unroll
+  for (int o = 1; o < kSepLanes; o <<= 1) {
+    na += __shfl_xor_sync(0xffffffffu, na, o);
+    nb += __shfl_xor_sync(0xffffffffu, nb, o);
+  }
+  if (row < n && sub == 0) {
+    cnt[0 * n + row] = ci == kSepA ? na : 0;  // K_aa
+    cnt[1 * n + row] = ci == kSepA ? nb : 0;  // K_ab
+    cnt[2 * n + row] = ci == kSepB ? na : 0;  // K_ba
+    cnt[3 * n + row] = ci == kSepB ? nb : 0;  // K_bb
   }
 }
 
@@ -104,38 +113,45 @@ struct SepOut {
   double* v[kSepBlocks];
 };
 
-// one warp per row: every kept entry at its position (row start + ballot prefix), local column index
+// every kept entry at its position (row start + the count of kept entries before it in the row, from the
+// ballots of the row's four lanes), local column index
 __global__ void k_sep_fill(size_t n, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col_idx,
                            const double* __restrict__ val, const uint8_t* __restrict__ cls,
                            const uint32_t* __restrict__ posA, const uint32_t* __restrict__ posB,
                            const unsigned long long* __restrict__ scan, SepOut out) {
-  const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) / 32;
-  const int lane = threadIdx.x & 31;
-  if (w >= n) return;
-  const uint8_t ci = cls[w];
-  if (ci == kSepExcluded) return;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t row = t / kSepLanes;
+  const int sub = (int)(t % kSepLanes);
+  const int shift = (int)(threadIdx.x & 31) & ~(kSepLanes - 1);
+  const uint8_t ci = row < n ? cls[row] : kSepExcluded;
+  const int64_t b = row < n ? row_ptr[row] : 0;
+  const int64_t e = ci != kSepExcluded ? row_ptr[row + 1] : b;
   const size_t stride = n + 1;
   const int ba = ci == kSepA ? 0 : 2;  // block of (row class, column a); +1 for column b
-  unsigned long long pa = scan[(size_t)ba * stride + w], pb = scan[(size_t)(ba + 1) * stride + w];
-  const unsigned lt = (1u << lane) - 1u;
-  for (int64_t k0 = row_ptr[w]; k0 < row_ptr[w + 1]; k0 += 32) {
-    const int64_t k = k0 + lane;
+  unsigned long long pa = 0, pb = 0;
+  if (ci != kSepExcluded) {
+    pa = scan[(size_t)ba * stride + row];
+    pb = scan[(size_t)(ba + 1) * stride + row];
+  }
+  const unsigned below = (1u << sub) - 1u, group = (1u << kSepLanes) - 1u;
+  for (int64_t k0 = b; __any_sync(0xffffffffu, k0 < e); k0 += kSepLanes) {
+    const int64_t k = k0 + sub;
     uint8_t cj = kSepExcluded;
     int32_t c = 0;
     double v = 0.0;
-    if (k < row_ptr[w + 1]) {
+    if (k < e) {
       v = val[k];
       c = col_idx[k];
       if (nonzero(v)) cj = cls[c];
     }
-    const unsigned ma = __ballot_sync(0xffffffffu, cj == kSepA);
-    const unsigned mb = __ballot_sync(0xffffffffu, cj == kSepB);
+    const unsigned ma = (__ballot_sync(0xffffffffu, cj == kSepA) >> shift) & group;
+    const unsigned mb = (__ballot_sync(0xffffffffu, cj == kSepB) >> shift) & group;
     if (cj == kSepA) {
-      const unsigned long long at = pa + __popc(ma & lt);
+      const unsigned long long at = pa + __popc(ma & below);
       out.ci[ba][at] = (int32_t)posA[c];
       out.v[ba][at] = v;
     } else if (cj == kSepB) {
-      const unsigned long long at = pb + __popc(mb & lt);
+      const unsigned long long at = pb + __popc(mb & below);
       out.ci[ba + 1][at] = (int32_t)posB[c];
       out.v[ba + 1][at] = v;
     }
@@ -202,7 +218,8 @@ extern "C" int fem_gpu_separate_sparse(fem_gpu_t* h, const uint8_t* imposed) {
   if (nab[1] == 0) return h->fail(FEM_GPU_ERR_SEP_NO_RESTRAINTS, "No restraints");
   // per-row counts of each block, their scans (n + 1 each: the last entry is the block's size)
   if (n) {
-    k_sep_count<<<grid_for(n * 32, 256), 256, 0, s>>>(n, h->row_ptr.p, h->col_idx.p, h->values.p, h->sep_cls.p, cnt);
+    k_sep_count<<<grid_for(n * kSepLanes, 256), 256, 0, s>>>(n, h->row_ptr.p, h->col_idx.p, h->values.p,
+                                                              h->sep_cls.p, cnt);
     CK(cudaGetLastError());
   }
   for (int b = 0; b < kSepBlocks; ++b) {
@@ -242,8 +259,8 @@ extern "C" int fem_gpu_separate_sparse(fem_gpu_t* h, const uint8_t* imposed) {
     o.v[b] = h->sep_v[b].p;
   }
   if (n)
-    k_sep_fill<<<grid_for(n * 32, 256), 256, 0, s>>>(n, h->row_ptr.p, h->col_idx.p, h->values.p, h->sep_cls.p, posA,
-                                                      posB, h->sep_scan.p, o);
+    k_sep_fill<<<grid_for(n * kSepLanes, 256), 256, 0, s>>>(n, h->row_ptr.p, h->col_idx.p, h->values.p,
+                                                             h->sep_cls.p, posA, posB, h->sep_scan.p, o);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(s));
   h->sep_valid = true;
