@@ -263,9 +263,11 @@ __global__ void k_rotation(int kind, NodesView nd, const int32_t* n1, const int3
 // ---------------------------------------------------------------------------
 // kernels: symbolic
 // ---------------------------------------------------------------------------
+// node-pair keys are (lower << kb) | higher with kb the bits of the largest node index, so the radix sort
+// runs over 2 kb bits only
 __global__ void k_gen_pairs(int kind, const int32_t* __restrict__ n1, const int32_t* __restrict__ n2,
                             const int32_t* __restrict__ n3, const int32_t* __restrict__ n4, size_t begin,
-                            size_t count, size_t pair_base, uint64_t* keys, uint32_t* vals) {
+                            size_t count, size_t pair_base, int kb, uint64_t* keys, uint32_t* vals) {
   size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (k >= count) return;
   size_t e = begin + k;
@@ -284,7 +286,7 @@ __global__ void k_gen_pairs(int kind, const int32_t* __restrict__ n1, const int3
     uint32_t I = (uint32_t)nodes[i], J = (uint32_t)nodes[j];
     uint32_t lo = I < J ? I : J, hi = I < J ? J : I;
     size_t pid = pair_base + k * ppe + p;
-    keys[pid] = ((uint64_t)lo << 32) | hi;
+    keys[pid] = ((uint64_t)lo << kb) | hi;
     vals[pid] = ((uint32_t)kind << 30) | (uint32_t)(e * ppe + p);
   }
 }
@@ -547,7 +549,7 @@ __device__ __forceinline__ uint64_t transpose36(uint64_t m) {
 }
 
 __global__ void k_block_meta(const uint32_t* __restrict__ blk_start, size_t nb, size_t n_pairs,
-                             const uint64_t* __restrict__ keys, const uint64_t* __restrict__ sorted_mask,
+                             const uint64_t* __restrict__ keys, int kb, const uint64_t* __restrict__ sorted_mask,
                              uint32_t* blk_count, uint64_t* blk_mask, uint64_t* blk_maskT, int32_t* blk_I,
                              int32_t* blk_J, uint32_t* adj_n) {
   size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -560,32 +562,33 @@ __global__ void k_block_meta(const uint32_t* __restrict__ blk_start, size_t nb, 
   blk_mask[b] = m;
   blk_maskT[b] = transpose36(m);
   uint64_t key = keys[s];
-  int32_t I = (int32_t)(key >> 32), J = (int32_t)(key & 0xffffffffu);
+  int32_t I = (int32_t)(key >> kb), J = (int32_t)(key & ((1ull << kb) - 1ull));
   blk_I[b] = I;
   blk_J[b] = J;
   adj_n[b] = I == J ? 1u : 2u;
 }
 
 __global__ void k_adjacency(const uint32_t* __restrict__ adj_off, size_t nb, const int32_t* __restrict__ blk_I,
-                            const int32_t* __restrict__ blk_J, uint64_t* akeys, uint32_t* avals) {
+                            const int32_t* __restrict__ blk_J, int kb, uint64_t* akeys, uint32_t* avals) {
   size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (b >= nb) return;
   uint32_t o = adj_off[b];
   uint32_t I = (uint32_t)blk_I[b], J = (uint32_t)blk_J[b];
-  akeys[o] = ((uint64_t)I << 32) | J;
+  akeys[o] = ((uint64_t)I << kb) | J;
   avals[o] = (uint32_t)(b << 1);
   if (I != J) {
-    akeys[o + 1] = ((uint64_t)J << 32) | I;
+    akeys[o + 1] = ((uint64_t)J << kb) | I;
     avals[o + 1] = (uint32_t)((b << 1) | 1u);
   }
 }
 
-__global__ void k_row_segments(const uint64_t* __restrict__ akeys, size_t na, int32_t* seg_begin, int32_t* seg_end) {
+__global__ void k_row_segments(const uint64_t* __restrict__ akeys, size_t na, int kb, int32_t* seg_begin,
+                               int32_t* seg_end) {
   size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (k >= na) return;
-  uint32_t r = (uint32_t)(akeys[k] >> 32);
-  if (k == 0 || (uint32_t)(akeys[k - 1] >> 32) != r) seg_begin[r] = (int32_t)k;
-  if (k + 1 == na || (uint32_t)(akeys[k + 1] >> 32) != r) seg_end[r] = (int32_t)(k + 1);
+  uint32_t r = (uint32_t)(akeys[k] >> kb);
+  if (k == 0 || (uint32_t)(akeys[k - 1] >> kb) != r) seg_begin[r] = (int32_t)k;
+  if (k + 1 == na || (uint32_t)(akeys[k + 1] >> kb) != r) seg_end[r] = (int32_t)(k + 1);
 }
 
 __device__ __forceinline__ uint32_t kinds_of(uint64_t m) {
@@ -725,7 +728,7 @@ __device__ __forceinline__ int warp_inclusive_sum(int v) {
 // stored with the row node second (t = 1) is read transposed.  The node's
 // groups are placed the same way.
 __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin, const int32_t* __restrict__ seg_end,
-                           const uint64_t* __restrict__ akeys, const uint32_t* __restrict__ avals,
+                           const uint64_t* __restrict__ akeys, int kb, const uint32_t* __restrict__ avals,
                            const uint64_t* __restrict__ blk_mask, const uint64_t* __restrict__ blk_maskT,
                            const uint8_t* __restrict__ blk_lay, const uint32_t* __restrict__ blk_count,
                            const unsigned long long* __restrict__ blk_voff, SlotLayout L,
@@ -751,7 +754,7 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
       const uint32_t v = avals[k];
       const uint32_t b = v >> 1;
       t = v & 1u;
-      J = (uint32_t)(akeys[k] & 0xffffffffu);
+      J = (uint32_t)(akeys[k] & ((1ull << kb) - 1ull));
       m = t ? blk_maskT[b] : blk_mask[b];
       lay = blk_lay[b];
       const int cat = slot_cat(blk_count[b]);
@@ -2633,6 +2636,9 @@ int symbolic(fem_gpu* h) {
     h->pattern_valid = true;
     return FEM_GPU_OK;
   }
+  // bits of the largest node index (keys pack two indices in 2 kb bits)
+  int kb = 1;
+  while (kb < 32 && (((uint64_t)h->nodes_number - 1) >> kb) != 0) ++kb;
   // 1. pair keys in call order
   DevBuf<uint64_t> keys, skeys;
   DevBuf<uint32_t> vals, svals;
@@ -2643,13 +2649,13 @@ int symbolic(fem_gpu* h) {
   for (const Run& r : h->runs) {
     if (r.kind == kTruss)
       k_gen_pairs<<<grid_for(r.count, 256), 256, 0, s>>>(kTruss, h->t_n1.p, h->t_n2.p, nullptr, nullptr, r.begin,
-                                                         r.count, r.pair_base, keys.p, vals.p);
+                                                         r.count, r.pair_base, kb, keys.p, vals.p);
     else if (r.kind == kBeam)
       k_gen_pairs<<<grid_for(r.count, 256), 256, 0, s>>>(kBeam, h->b_n1.p, h->b_n2.p, nullptr, nullptr, r.begin,
-                                                         r.count, r.pair_base, keys.p, vals.p);
+                                                         r.count, r.pair_base, kb, keys.p, vals.p);
     else
       k_gen_pairs<<<grid_for(r.count, 256), 256, 0, s>>>(kPlate, h->p_n1.p, h->p_n2.p, h->p_n3.p, h->p_n4.p,
-                                                         r.begin, r.count, r.pair_base, keys.p, vals.p);
+                                                         r.begin, r.count, r.pair_base, kb, keys.p, vals.p);
   }
   CK(cudaGetLastError());
   // 2. per-pair non-zero masks from the element arithmetic
@@ -2665,7 +2671,7 @@ int symbolic(fem_gpu* h) {
   }
   // 3. stable sort by node-pair key (call order preserved within a block)
   int st = cub_call(h, [&](void* tmp, size_t& bytes) {
-    return cub::DeviceRadixSort::SortPairs(tmp, bytes, keys.p, skeys.p, vals.p, svals.p, (int64_t)np, 0, 64, s);
+    return cub::DeviceRadixSort::SortPairs(tmp, bytes, keys.p, skeys.p, vals.p, svals.p, (int64_t)np, 0, 2 * kb, s);
   });
   if (st) return st;
   // 4. slots and sorted masks
@@ -2700,7 +2706,7 @@ int symbolic(fem_gpu* h) {
   DevBuf<uint32_t> adj_n, adj_off;
   CK(adj_n.reserve(nb, s));
   CK(adj_off.reserve(nb, s));
-  k_block_meta<<<grid_for(nb, 256), 256, 0, s>>>(h->blk_start.p, nb, np, skeys.p, smask.p, h->blk_count.p,
+  k_block_meta<<<grid_for(nb, 256), 256, 0, s>>>(h->blk_start.p, nb, np, skeys.p, kb, smask.p, h->blk_count.p,
                                                  h->blk_mask.p, h->blk_maskT.p, h->blk_I.p, h->blk_J.p, adj_n.p);
   st = cub_call(h, [&](void* tmp, size_t& bytes) {
     return cub::DeviceScan::ExclusiveSum(tmp, bytes, adj_n.p, adj_off.p, (int64_t)nb, s);
@@ -2743,9 +2749,10 @@ int symbolic(fem_gpu* h) {
   CK(sakeys.reserve(na, s));
   CK(avals.reserve(na, s));
   CK(savals.reserve(na, s));
-  k_adjacency<<<grid_for(nb, 256), 256, 0, s>>>(adj_off.p, nb, h->blk_I.p, h->blk_J.p, akeys.p, avals.p);
+  k_adjacency<<<grid_for(nb, 256), 256, 0, s>>>(adj_off.p, nb, h->blk_I.p, h->blk_J.p, kb, akeys.p, avals.p);
   st = cub_call(h, [&](void* tmp, size_t& bytes) {
-    return cub::DeviceRadixSort::SortPairs(tmp, bytes, akeys.p, sakeys.p, avals.p, savals.p, (int64_t)na, 0, 64, s);
+    return cub::DeviceRadixSort::SortPairs(tmp, bytes, akeys.p, sakeys.p, avals.p, savals.p, (int64_t)na, 0, 2 * kb,
+                                           s);
   });
   if (st) return st;
   size_t nn = h->nodes_number;
@@ -2760,7 +2767,7 @@ int symbolic(fem_gpu* h) {
   CK(cudaMemsetAsync(seg_e.p, 0xff, nn * sizeof(int32_t), s));
   CK(cudaMemsetAsync(row_nnz.p, 0, (nrows + 1) * sizeof(int64_t), s));
   CK(cudaMemsetAsync(gcount.p, 0, (nn + 1) * sizeof(int64_t), s));
-  k_row_segments<<<grid_for(na, 256), 256, 0, s>>>(sakeys.p, na, seg_b.p, seg_e.p);
+  k_row_segments<<<grid_for(na, 256), 256, 0, s>>>(sakeys.p, na, kb, seg_b.p, seg_e.p);
   k_row_counts<<<grid_for(nn, 128), 128, 0, s>>>(nn, seg_b.p, seg_e.p, savals.p, h->blk_mask.p, h->blk_maskT.p,
                                                  row_nnz.p, gcount.p);
   st = cub_call(h, [&](void* tmp, size_t& bytes) {
@@ -2825,7 +2832,7 @@ int symbolic(fem_gpu* h) {
     CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), s));
     k_slot_desc<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_pmask.p, h->blk_lay.p, h->blk_voff.p, L,
                                                   h->slot_desc.p, h->flag.p);
-    k_row_fill<<<grid_for(nn * 32, 256), 256, 0, s>>>(nn, seg_b.p, seg_e.p, sakeys.p, savals.p, h->blk_mask.p,
+    k_row_fill<<<grid_for(nn * 32, 256), 256, 0, s>>>(nn, seg_b.p, seg_e.p, sakeys.p, kb, savals.p, h->blk_mask.p,
                                                     h->blk_maskT.p, h->blk_lay.p, h->blk_count.p, h->blk_voff.p, L,
                                                     h->row_ptr.p, gbase.p, h->col_idx.p, h->nnz_group.p,
                                                     h->src_map.p, h->g_row.p, h->g_col.p, h->g_kind.p);

@@ -123,6 +123,36 @@ def test_determinism_and_reassembly():
     np.testing.assert_array_equal(v1.view(np.uint64), v2.view(np.uint64))
 
 
+def test_additions_after_assembly():
+    """assemble, add more elements (a bulk call, a rejected call, single calls), assemble again: the numeric
+    pass (replayed as a graph between symbolic phases) sees the new and moved arrays"""
+    m = meshes.plate_mesh(40, 40, size=4.0)
+    half = len(m.plates["numbers"]) // 2
+    g = FEM(1e-12, 1e-12, m.nodes_number)
+    o = OracleFEM(1e-12, 1e-12, m.nodes_number)
+    p = m.plates
+    for x in (g, o):
+        x.add_nodes(m.node_numbers, m.xyz)
+        x.add_plates(p["numbers"][:half], p["nodes"][:half], p["young"][:half], p["poisson"][:half],
+                     p["thickness"][:half], p["shear_factor"][:half])
+    g.assemble()
+    for _ in range(2):
+        g.assemble_numeric_async()
+    g.check_pattern()
+    for x in (g, o):
+        x.add_plates(p["numbers"][half:], p["nodes"][half:], p["young"][half:], p["poisson"][half:],
+                     p["thickness"][half:], p["shear_factor"][half:])
+        with pytest.raises((FEMError, OracleError)):  # every plate rejected (numbers taken)
+            x.add_plates(p["numbers"][:3], p["nodes"][:3], p["young"][:3], p["poisson"][:3], p["thickness"][:3],
+                         p["shear_factor"][:3])
+        x.add_truss(10 ** 6, 1, 41 * 41, 200e9, 3e-4)
+    g.assemble()
+    compare(g, o)
+    g.assemble_numeric_async()
+    g.check_pattern()
+    compare(g, o)
+
+
 def test_coordinate_update_reuses_or_rebuilds_pattern():
     """new coordinates (same topology): the next assemble equals a fresh oracle build on them."""
     m = meshes.beam_frame(6, 6, 4, seed=31)
