@@ -708,19 +708,22 @@ __device__ __forceinline__ int packed_pos(uint32_t lay, int en) {
 }
 
 // inclusive prefix sum over the lanes of a warp
-__device__ __forceinline__ int warp_inclusive_sum(int v) {
-  const int lane = threadIdx.x & 31;
+constexpr int kRowLanes = 16;  // lanes per node in the row fill (a plate-mesh node has 9 blocks, a frame node 7)
+
+// inclusive prefix sum over the kRowLanes lanes of a node
+__device__ __forceinline__ int seg_inclusive_sum(int v) {
+  const int sl = threadIdx.x & (kRowLanes - 1);
 #pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const int u = __shfl_up_sync(0xffffffffu, v, d);
-    if (lane >= d) v += u;
+  for (int d = 1; d < kRowLanes; d <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, v, d, kRowLanes);
+    if (sl >= d) v += u;
   }
   return v;
 }
 
-// Symbolic, once per pattern: the CSR rows of a node, one warp per node.  Lane
-// k takes the k-th block of the node's adjacency (blocks in column-node order,
-// 32 at a time); for each of the node's 6 rows a warp prefix sum of the
+// Symbolic, once per pattern: the CSR rows of a node, kRowLanes lanes per node.
+// Lane k takes the k-th block of the node's adjacency (blocks in column-node
+// order, kRowLanes at a time); for each of the node's 6 rows a prefix sum of the
 // blocks' entry counts gives every lane the place of its entries, which it
 // writes in column order: column, stiffness group and value source (the
 // scratch position of a block with one contribution, else the entry's
@@ -736,16 +739,22 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
                            int32_t* __restrict__ col_idx, int32_t* __restrict__ nnz_group,
                            uint32_t* __restrict__ src_map, int32_t* __restrict__ g_row, int32_t* __restrict__ g_col,
                            uint8_t* __restrict__ g_kind) {
-  const size_t r = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) / 32;
-  const int lane = threadIdx.x & 31;
-  if (r >= n_nodes) return;
-  const int32_t s = seg_begin[r], e = seg_end[r];
-  if (s < 0) return;
-  int64_t gnext = gbase[r];
-  int64_t next[6];
+  const size_t r = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) / kRowLanes;
+  const int lane = (int)(threadIdx.x & (kRowLanes - 1));
+  // every lane stays for the shuffles: a node past the end or without blocks has an empty range
+  int32_t s = 0, e = 0;
+  if (r < n_nodes && seg_begin[r] >= 0) {
+    s = seg_begin[r];
+    e = seg_end[r];
+  }
+  int64_t gnext = 0;
+  int64_t next[6] = {0, 0, 0, 0, 0, 0};
+  if (e > s) {
+    gnext = gbase[r];
 #pragma unroll
-  for (int a = 0; a < 6; ++a) next[a] = row_ptr[6 * r + a];
-  for (int32_t k0 = s; k0 < e; k0 += 32) {
+    for (int a = 0; a < 6; ++a) next[a] = row_ptr[6 * r + a];
+  }
+  for (int32_t k0 = s; __any_sync(0xffffffffu, k0 < e); k0 += kRowLanes) {
     const int32_t k = k0 + lane;
     uint64_t m = 0;
     uint32_t J = 0, lay = 0, t = 0;
@@ -763,7 +772,7 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
     // groups
     const uint32_t km = kinds_of(m);
     const int ng = __popc(km);
-    const int gin = warp_inclusive_sum(ng);
+    const int gin = seg_inclusive_sum(ng);
     int64_t g = gnext + gin - ng;
     int32_t kg[4];
 #pragma unroll
@@ -777,13 +786,13 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
         ++g;
       }
     }
-    gnext += __shfl_sync(0xffffffffu, gin, 31);
+    gnext += __shfl_sync(0xffffffffu, gin, kRowLanes - 1, kRowLanes);
     // rows
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
       const uint32_t rowbits = (uint32_t)((m >> (6 * a)) & 63ull);
       const int cnt = __popc(rowbits);
-      const int inc = warp_inclusive_sum(cnt);
+      const int inc = seg_inclusive_sum(cnt);
       int64_t pos = next[a] + inc - cnt;
 #pragma unroll
       for (int c = 0; c < 6; ++c)
@@ -793,7 +802,7 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
           src_map[pos] = (uint32_t)(sb + (unsigned long long)packed_pos(lay, t ? 6 * c + a : 6 * a + c));
           ++pos;
         }
-      next[a] += __shfl_sync(0xffffffffu, inc, 31);
+      next[a] += __shfl_sync(0xffffffffu, inc, kRowLanes - 1, kRowLanes);
     }
   }
 }
@@ -2832,7 +2841,7 @@ int symbolic(fem_gpu* h) {
     CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), s));
     k_slot_desc<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_pmask.p, h->blk_lay.p, h->blk_voff.p, L,
                                                   h->slot_desc.p, h->flag.p);
-    k_row_fill<<<grid_for(nn * 32, 256), 256, 0, s>>>(nn, seg_b.p, seg_e.p, sakeys.p, kb, savals.p, h->blk_mask.p,
+    k_row_fill<<<grid_for(nn * kRowLanes, 256), 256, 0, s>>>(nn, seg_b.p, seg_e.p, sakeys.p, kb, savals.p, h->blk_mask.p,
                                                     h->blk_maskT.p, h->blk_lay.p, h->blk_count.p, h->blk_voff.p, L,
                                                     h->row_ptr.p, gbase.p, h->col_idx.p, h->nnz_group.p,
                                                     h->src_map.p, h->g_row.p, h->g_col.p, h->g_kind.p);
