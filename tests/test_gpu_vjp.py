@@ -167,17 +167,17 @@ def check_coord(mesh, node0, c, got, U, L):
     """(ok, fd_used, detail) for the gradient w.r.t. one nodal coordinate"""
     fd, bound = fd_coord(mesh, node0, c, U, L, with_bound=True)
     shares = [hp_share(mesh, kind, e, U, L, node0=node0, c=c) for kind, e in touching(mesh, node0)]
-    return judge(got, fd, bound, sum(shares), sum(abs(s) for s in shares))
+    return arbitrate(got, fd, bound, sum(shares), sum(abs(s) for s in shares))
 
 
 def check_prop(mesh, kind, e, name, got, U, L):
     """(ok, fd_used, detail) for the gradient w.r.t. one element property"""
     fd, bound = fd_prop(mesh, kind, e, name, U, L, with_bound=True)
     hp = hp_share(mesh, kind, e, U, L, name=name)
-    return judge(got, fd, bound, hp, abs(hp))
+    return arbitrate(got, fd, bound, hp, abs(hp))
 
 
-def judge(got, fd, bound, hp, mag):
+def arbitrate(got, fd, bound, hp, mag):
     """The GPU gradient must lie within HP_REL * mag of the high-precision derivative (mag = the summed
     magnitude of the element shares, the scale of a sum that cancels), and within FD_REL of the
     finite-difference estimate (plus its rounding bound) wherever that estimate is itself within

@@ -14,7 +14,7 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 
 def rel_err(a, b):
-    """max |a - b| / max |b| (entries that cancel inside one element are judged against the element's scale)."""
+    """max |a - b| / max |b| (entries that cancel inside one element are measured against the element's scale)."""
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
