@@ -246,7 +246,8 @@ def run_batch(args):
                       "speedup_vs_plain_async": t_p / t_b, "speedup_vs_plain_sync": plain_sync_ms / t_b,
                       "autotune_best": table["best"], "autotune_best_ms": table["best_ms"],
                       "autotune_candidates": len(table["candidates"])},
-            "gpu_launches": None, "clocks": clocks.summary()}
+            "gpu_launches": args.steps * ((1 if table["best"]["persistent"] else sum(1 for c in counts if c)) + 2),
+            "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
     b.close()
 
