@@ -519,6 +519,25 @@ def run_results(args):
                                        f"{by:.0f} GB/s of algorithmic bytes = {by / hbm:.3f} of measured HBM",
                         "peak_source": "2 DFMA/clk/SM x 152 SMs x 2070 MHz"}
     line["clocks"] = clocks.summary()
+    # the beams of the 101 x 101 x 21 frame too (device-resident, same timing)
+    frame = meshes.beam_frame()
+    n_bm = len(frame.beams["numbers"])
+    gb = FEM(meshes.REL_TOL, meshes.ABS_TOL, frame.nodes_number)
+    meshes.load(gb, frame)
+    bdisp = torch.from_numpy(np.random.default_rng(18).standard_normal(6 * frame.nodes_number) * 1e-3).cuda()
+    bout = torch.empty((n_bm, 10), dtype=torch.float64, device="cuda")
+    bms = []
+    for it in range(args.warmup + args.steps):
+        flush.fill_(it & 0xFF)
+        torch.cuda.synchronize()
+        gb.element_results_device(bdisp.data_ptr(), 0, bout.data_ptr(), 0)
+        torch.cuda.synchronize()
+        if it >= args.warmup:
+            bms.append(gb.results_last_ms())
+    tb = float(np.mean(bms))
+    line["beam"] = {"workload": f"beam_frame_101x101x21: {n_bm:,} beams", "ms": tb, "value": n_bm / (tb * 1e-3),
+                    "unit": "elements/s"}
+    gb.close()
     if not args.no_cpu:
         threads = os.cpu_count() or 1
         secs = []
