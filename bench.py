@@ -40,13 +40,27 @@ FP64_PEAK_FLOPS = 2 * 152 * 2070e6 * 2
 # Algorithmic FP64 work per element of the numeric pass, counted from the kernels' formulation by
 # compiling element_math.cuh with an operation-counting double type (FMA = 2 flops, add/mul/div = 1):
 #   plate, R = I: core 70 add + 169 mul + 176 fma + 2 div, 10 node-pair blocks 56 mul + 154 fma
-#   beam: 57 add + 213 mul + 201 fma + 19 div + 7 sqrt (trig as polynomial fma chains)
+#   beam, I12 != 0: 57 add + 213 mul + 201 fma + 19 div + 7 sqrt (trig as polynomial fma chains) = 698;
+#   I12 == 0 (principal axes along the section axes, no arctangent and series): 515 when I11 >= I22, and
+#   714 when I11 < I22 (one turn of the principal-axes loop: arctangent, sine and cosine)
 #   truss: 20 add + 46 mul + 9 fma + 4 div + 4 sqrt
 WORK = {
     "plate": dict(elem_flops=70 + 169 + 2 * 176 + 2 + 56 + 2 * 154, pairs=10),
     "beam": dict(elem_flops=57 + 213 + 2 * 201 + 19 + 7, pairs=3),
     "truss": dict(elem_flops=20 + 46 + 2 * 9 + 4 + 4, pairs=3),
 }
+BEAM_FLOPS = {"general": 698, "aligned": 515, "aligned_turn": 714}
+
+
+def element_flops(workload, mesh):
+    """algorithmic FP64 work of one numeric pass's element kernel over the mesh"""
+    if workload != "beam":
+        return WORK[workload]["elem_flops"] * mesh.n_elements
+    b = mesh.beams
+    aligned = np.asarray(b["i12"]) == 0.0
+    turn = aligned & (np.asarray(b["i11"]) < np.asarray(b["i22"]))
+    return (BEAM_FLOPS["general"] * int((~aligned).sum()) + BEAM_FLOPS["aligned"] * int((aligned & ~turn).sum())
+            + BEAM_FLOPS["aligned_turn"] * int(turn.sum()))
 # bytes per element read by the element kernel (connectivity, coordinates of its nodes, properties)
 IN_BYTES = {"plate": 4 * 4 + 4 * 24 + 4 * 8, "beam": 2 * 4 + 2 * 24 + 11 * 8, "truss": 2 * 4 + 2 * 24 + 3 * 8}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per element of one launch of the element kernel,
@@ -660,7 +674,7 @@ def main():
     # and gathered once; the CSR source map (4 B) read and the CSR values (8 B) written once
     red_bytes = scratch * 8 + 3 * sum_slots * 8 + nnz * (4 + 8)
     t_e, t_r = float(np.mean(elem_ms)), float(np.mean(red_ms))
-    kern = {"element": dict(ms=t_e, bytes=elem_bytes, flops=w["elem_flops"] * n_el),
+    kern = {"element": dict(ms=t_e, bytes=elem_bytes, flops=element_flops(args.workload, mesh)),
             "reduce": dict(ms=t_r, bytes=red_bytes, flops=scratch)}  # <= one FP64 add per packed entry
     dom = max(kern, key=lambda k: kern[k]["ms"])
     kd = kern[dom]

@@ -325,24 +325,42 @@ __device__ __forceinline__ bool truss_block(const T x1[3], const T x2[3], T youn
 // ---------------------------------------------------------------------------
 // beam (structs/beam.rs)
 // ---------------------------------------------------------------------------
+// i12 == 0 (a section symmetric about a local axis): atan(+-0) = +0 (the arctangent's reduction takes a
+// signed zero to +0), and cos, sin of +0 are exactly 1 and +0 -- the same bits as the general evaluation,
+// without its arctangent and series
+template <class T>
+__device__ __forceinline__ bool principal_axes_aligned(T i12) {
+  if constexpr (IsDual<T>::value) return false;
+  else return i12 == 0.0;
+}
+
 template <class T>
 __device__ __forceinline__ void principal_moments(T i11, T i22, T i12, double rel_tol, T& i11p,
                                                   T& i22p, T& angle_out) {
-  T angle;
-  if (i11 != i22) {
-    angle = datan((2.0 * i12) / (i22 - i11)) / 2.0;
+  T angle, c, s, s2;
+  if (principal_axes_aligned(i12)) {
+    angle = 0.0;
+    c = 1.0;
+    s = 0.0;
+    s2 = 0.0;
   } else {
-    T i11m, i22m;
-    if (i22 < i11) {
-      i11m = i11;
-      i22m = ((fabs(i22) - fabs(i22) * rel_tol) * i22) / fabs(i22);
+    if (i11 != i22) {
+      angle = datan((2.0 * i12) / (i22 - i11)) / 2.0;
     } else {
-      i11m = ((fabs(i11) - fabs(i11) * rel_tol) * i11) / fabs(i11);
-      i22m = i22;
+      T i11m, i22m;
+      if (i22 < i11) {
+        i11m = i11;
+        i22m = ((fabs(i22) - fabs(i22) * rel_tol) * i22) / fabs(i22);
+      } else {
+        i11m = ((fabs(i11) - fabs(i11) * rel_tol) * i11) / fabs(i11);
+        i22m = i22;
+      }
+      angle = datan((2.0 * i12) / (i22m - i11m)) / 2.0;
     }
-    angle = datan((2.0 * i12) / (i22m - i11m)) / 2.0;
+    c = dcos(angle);
+    s = dsin(angle);
+    s2 = dsin(2.0 * angle);
   }
-  T c = dcos(angle), s = dsin(angle), s2 = dsin(2.0 * angle);
   T a = (i11 * (c * c) + i22 * (s * s)) - i12 * s2;
   T bb = (i11 * (s * s) + i22 * (c * c)) + i12 * s2;
   int it = 1;
