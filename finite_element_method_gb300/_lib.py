@@ -72,6 +72,7 @@ SIGNATURES = {
     "fem_gpu_results_last_ms": (c_int, [hp, POINTER(c_float)]),
     "fem_gpu_get_element_numbers": (c_int, [hp, c_int, u32p]),
     "fem_gpu_release_cached_memory": (c_int, []),
+    "fem_gpu_assemble_to_host": (c_int, [hp, i64p, i32p, dp, c_int64, i64p]),
     "fem_gpu_separate_sparse": (c_int, [hp, u8p]),
     "fem_gpu_get_separation_sizes": (c_int, [hp, i64p, i64p, i64p]),
     "fem_gpu_get_separation_indexes": (c_int, [hp, i64p, i64p]),

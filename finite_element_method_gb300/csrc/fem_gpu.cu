@@ -1371,6 +1371,9 @@ struct fem_gpu {
   float t_elem_ms = 0, t_reduce_ms = 0;
   // the numeric pass as a CUDA graph (captured at its first launch after each symbolic phase)
   cudaGraphExec_t num_graph = nullptr;
+  // a second stream for pattern read-backs that overlap the numeric pass (fem_gpu_assemble_to_host)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ev = nullptr;
   void drop_numeric_graph() {
     if (num_graph) cudaGraphExecDestroy(num_graph);
     num_graph = nullptr;
@@ -1737,6 +1740,8 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   }
   h->res_buf.release();
   h->drop_numeric_graph();
+  if (h->copy_ev) cudaEventDestroy(h->copy_ev);
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   for (auto& ev : h->ev)
     if (ev) cudaEventDestroy(ev);
   for (auto& ev : h->res_ev)
@@ -2891,6 +2896,48 @@ extern "C" int fem_gpu_assemble(fem_gpu_t* h) {
     int flag = 0;
     CK(cudaMemcpyAsync(&flag, h->flag.p, sizeof flag, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    CK(cudaEventElapsedTime(&h->t_elem_ms, h->ev[0], h->ev[1]));
+    CK(cudaEventElapsedTime(&h->t_reduce_ms, h->ev[1], h->ev[2]));
+    if (!flag) return FEM_GPU_OK;
+    h->pattern_valid = false;  // a coordinate/property update changed the exact-zero pattern
+  }
+  return h->fail(FEM_GPU_ERR_PATTERN_CHANGED, "pattern changed twice in one assemble");
+}
+
+extern "C" int fem_gpu_assemble_to_host(fem_gpu_t* h, int64_t* row_ptr, int32_t* col_idx, double* values,
+                                        int64_t nnz_capacity, int64_t* nnz) {
+  if (!h || !row_ptr || (nnz_capacity > 0 && (!col_idx || !values))) return FEM_GPU_ERR_ARGUMENT;
+  int st = ensure_ready(h);
+  if (st) return st;
+  if (!h->copy_stream) {
+    CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&h->copy_ev, cudaEventDisableTiming));
+  }
+  const size_t nrows = (size_t)h->nodes_number * 6;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    if (!h->pattern_valid) {
+      st = symbolic(h);
+      if (st) return st;
+    }
+    if (nnz) *nnz = h->nnz;
+    if (h->nnz > nnz_capacity)
+      return h->fail(FEM_GPU_ERR_ARGUMENT, "the CSR has %lld entries, the buffers room for %lld",
+                     (long long)h->nnz, (long long)nnz_capacity);
+    // the pattern goes back on the copy stream while the numeric pass runs (it writes only the values)
+    CK(cudaEventRecord(h->copy_ev, h->stream));
+    CK(cudaStreamWaitEvent(h->copy_stream, h->copy_ev, 0));
+    st = numeric_launch(h);
+    if (st) return st;
+    CK(cudaMemcpyAsync(row_ptr, h->row_ptr.p, (nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, h->copy_stream));
+    if (h->nnz)
+      CK(cudaMemcpyAsync(col_idx, h->col_idx.p, (size_t)h->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                         h->copy_stream));
+    int flag = 0;
+    CK(cudaMemcpyAsync(&flag, h->flag.p, sizeof flag, cudaMemcpyDeviceToHost, h->stream));
+    if (h->nnz)
+      CK(cudaMemcpyAsync(values, h->values.p, (size_t)h->nnz * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaStreamSynchronize(h->copy_stream));
     CK(cudaEventElapsedTime(&h->t_elem_ms, h->ev[0], h->ev[1]));
     CK(cudaEventElapsedTime(&h->t_reduce_ms, h->ev[1], h->ev[2]));
     if (!flag) return FEM_GPU_OK;

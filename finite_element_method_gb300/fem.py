@@ -182,6 +182,22 @@ class FEM:
         self._check(self._L.fem_gpu_get_csr(self._h, ptr(rp, c_int64), ptr(ci, c_int32), ptr(va, c_double)))
         return rp, ci[:nnz], va[:nnz]
 
+    def assemble_to_host(self, row_ptr, col_idx, values) -> int:
+        """assemble() with the CSR read back into the given host arrays (row_ptr of 6 * nodes_number + 1
+        int64, col_idx int32 and values float64 with room for the entries; page-locked arrays copy fastest):
+        the pattern travels back while the numeric pass runs.  Returns nnz."""
+        rp = np.asarray(row_ptr)
+        ci = np.asarray(col_idx)
+        va = np.asarray(values)
+        assert rp.dtype == np.int64 and ci.dtype == np.int32 and va.dtype == np.float64
+        assert rp.flags.c_contiguous and ci.flags.c_contiguous and va.flags.c_contiguous
+        assert rp.size >= 6 * self.nodes_number + 1
+        cap = min(ci.size, va.size)
+        nnz = c_int64(0)
+        self._check(self._L.fem_gpu_assemble_to_host(self._h, ptr(rp, c_int64), ptr(ci, c_int32), ptr(va, c_double),
+                                                     cap, ctypes.byref(nnz)))
+        return nnz.value
+
     def stiffness_values(self, out=None):
         _, nnz = self.csr_sizes()
         if out is None:

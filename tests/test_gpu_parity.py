@@ -316,3 +316,25 @@ def test_batch_matches_each_model():
         _, _, va = o.csr()
         np.testing.assert_array_equal(b.values(i).view(np.uint64), va.view(np.uint64))
     b.close()
+
+
+def test_assemble_to_host_matches_assemble():
+    m = meshes.plate_mesh(50, 40, size=5.0)
+    g, o = build_pair(m)
+    rp0, ci0, va0 = g.stiffness_csr()
+    g2 = FEM(1e-12, 1e-12, m.nodes_number)
+    meshes.load(g2, m)
+    rp = np.zeros(6 * m.nodes_number + 1, np.int64)
+    ci = np.zeros(len(ci0) - 1, np.int32)
+    va = np.zeros(len(va0) - 1, np.float64)
+    with pytest.raises(FEMError, match="entries"):  # one entry short
+        g2.assemble_to_host(rp, ci, va)
+    ci = np.zeros(len(ci0) + 5, np.int32)
+    va = np.full(len(va0) + 5, np.nan)
+    for _ in range(2):  # fresh pattern, then the kept one
+        nnz = g2.assemble_to_host(rp, ci, va)
+        assert nnz == len(ci0)
+        np.testing.assert_array_equal(rp, rp0)
+        np.testing.assert_array_equal(ci[:nnz], ci0)
+        np.testing.assert_array_equal(va[:nnz].view(np.uint64), va0.view(np.uint64))
+    g2.close()
