@@ -20,13 +20,17 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <condition_variable>
 #include <cub/cub.cuh>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <unordered_map>
 #include <unordered_set>
 #include <thread>
 #include <vector>
+
+#include <unistd.h>
 
 #include "../../include/fem_gpu.h"
 #include "element_math.cuh"
@@ -1147,6 +1151,91 @@ class FlatTable {
 constexpr int kRegParts = 16;
 inline int reg_part(uint64_t key) { return (int)(mix64(key) >> 60); }
 
+// Host worker threads for the parallel passes of bulk add_* calls.  Creating and joining 15 threads
+// costs about a quarter of a millisecond, as much as one pass over a million items, and a bulk call
+// makes four passes, so the workers stay and sleep on a condition variable between passes.  One pass
+// runs at a time: a pass that finds the pool busy (a pass of another host thread, or one started from
+// inside a worker) or that runs in a process forked after the pool started returns false, and the
+// caller runs it on threads of its own.
+class HostPool {
+ public:
+  static HostPool* get() {
+    static std::mutex m;
+    static HostPool* pool = nullptr;  // never destroyed: its workers sleep until the process ends
+    std::lock_guard<std::mutex> g(m);
+    if (!pool || pool->pid_ != getpid()) pool = new HostPool();
+    return pool;
+  }
+  // f(t) for t = 0 .. T-1, t = 0 on the calling thread
+  bool run(unsigned T, const std::function<void(unsigned)>& f) {
+    std::unique_lock<std::mutex> busy(busy_, std::try_to_lock);
+    if (!busy.owns_lock() || T - 1 > workers_.size()) return false;
+    {
+      std::lock_guard<std::mutex> g(m_);
+      job_ = &f;
+      job_threads_ = T;
+      pending_ = T - 1;
+      ++gen_;
+    }
+    work_.notify_all();
+    f(0u);
+    std::unique_lock<std::mutex> g(m_);
+    done_.wait(g, [&] { return pending_ == 0; });
+    job_ = nullptr;
+    return true;
+  }
+
+ private:
+  HostPool() : pid_(getpid()) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const unsigned T = std::max(1u, std::min<unsigned>(hw ? hw : 1u, kRegParts));
+    for (unsigned w = 1; w < T; ++w) {
+      workers_.emplace_back([this, w] { loop(w); });
+      workers_.back().detach();
+    }
+  }
+  void loop(unsigned w) {
+    uint64_t seen = 0;
+    std::unique_lock<std::mutex> g(m_);
+    for (;;) {
+      work_.wait(g, [&] { return gen_ != seen; });
+      seen = gen_;
+      if (w >= job_threads_) continue;  // (a pass of fewer threads)
+      const std::function<void(unsigned)>* job = job_;
+      g.unlock();
+      (*job)(w);
+      g.lock();
+      if (--pending_ == 0) done_.notify_one();
+    }
+  }
+  const pid_t pid_;
+  std::vector<std::thread> workers_;
+  std::mutex busy_, m_;
+  std::condition_variable work_, done_;
+  const std::function<void(unsigned)>* job_ = nullptr;
+  unsigned job_threads_ = 0, pending_ = 0;
+  uint64_t gen_ = 0;
+};
+
+// f(t) on threads t = 0 .. T-1 (t = 0 on the calling thread): the pool's workers, else threads of its own
+template <class F>
+void run_threads(unsigned T, F f) {
+  if (T > 1) {
+    const std::function<void(unsigned)> job = [&f](unsigned t) { f(t); };
+    if (HostPool::get()->run(T, job)) return;
+  }
+  std::vector<std::thread> th;
+  for (unsigned t = 1; t < T; ++t) th.emplace_back(f, t);
+  f(0u);
+  for (auto& x : th) x.join();
+}
+
+// f(t, begin, end) over [0, n) in T contiguous chunks, chunk t on thread t
+template <class F>
+void parallel_chunks(unsigned T, size_t n, F f) {
+  run_threads(T, [&](unsigned t) { f(t, n * t / T, n * (t + 1) / T); });
+}
+
 class PartTable {
  public:
   template <class Eq>
@@ -1169,10 +1258,7 @@ class PartTable {
       for (Part& p : part_) p.t.reserve(per);
       return;
     }
-    std::vector<std::thread> th;
-    for (int p = 1; p < kRegParts; ++p) th.emplace_back([this, p, per] { part_[p].t.reserve(per); });
-    part_[0].t.reserve(per);
-    for (auto& x : th) x.join();
+    run_threads(kRegParts, [&](unsigned p) { part_[p].t.reserve(per); });
   }
 
  private:
@@ -1215,14 +1301,9 @@ class NumberMap {
     for (const auto& kv : moved) table_.erase(kv.first, kv.second);
     dense_.resize(want);  // no fill: the new slots are set to -1 by several threads
     const unsigned T = want - have >= (size_t(1) << 18) ? 8u : 1u;
-    std::vector<std::thread> th;
-    for (unsigned t = 1; t < T; ++t)
-      th.emplace_back([this, t, T, have, want] {
-        std::fill(dense_.begin() + have + (want - have) * t / T, dense_.begin() + have + (want - have) * (t + 1) / T,
-                  -1);
-      });
-    std::fill(dense_.begin() + have, dense_.begin() + have + (want - have) / T, -1);
-    for (auto& x : th) x.join();
+    parallel_chunks(T, want - have, [&](unsigned, size_t b, size_t e) {
+      std::fill(dense_.begin() + have + b, dense_.begin() + have + e, -1);
+    });
     for (const auto& kv : moved) dense_[kv.first] = kv.second;
   }
   // the partition of a key for threaded inserts: blocks of 1024 direct slots (so that threads write
@@ -1283,25 +1364,25 @@ struct fem_gpu {
   size_t n_pairs = 0;
   // truss
   size_t nt = 0;
-  std::vector<uint32_t> t_num;
+  HostVec<uint32_t> t_num;
   NumberMap t_by_num;  // number -> element index
   PartTable t_pairs;   // node pair -> element index
-  std::vector<uint32_t> t_nodes;  // node numbers per truss (2 each)
+  HostVec<uint32_t> t_nodes;  // node numbers per truss (2 each)
   size_t t_pairs_built = 0;       // t_pairs holds the trusses [0, t_pairs_built) (bulk calls check on the GPU)
   DevBuf<int32_t> t_n1, t_n2;
   DevBuf<double> t_E, t_A, t_A2;
   // beam
   size_t nbm = 0;
-  std::vector<uint32_t> b_num;
+  HostVec<uint32_t> b_num;
   NumberMap b_by_num;
   PartTable b_pairs;
-  std::vector<uint32_t> b_nodes;
+  HostVec<uint32_t> b_nodes;
   size_t b_pairs_built = 0;
   DevBuf<int32_t> b_n1, b_n2;
   DevBuf<double> b_E, b_nu, b_A, b_i11, b_i22, b_i12, b_it, b_ks, b_ax, b_ay, b_az;
   // plate
   size_t np = 0;
-  std::vector<uint32_t> p_num, p_nodes;
+  HostVec<uint32_t> p_num, p_nodes;
   NumberMap p_by_num;
   PartTable p_sets;  // sorted node-number set hash -> element index
   size_t sets_built = 0;  // p_sets holds the plates [0, sets_built) (bulk calls check node sets on the GPU)
@@ -1562,33 +1643,45 @@ int cub_call(fem_gpu* h, F f) {
   return FEM_GPU_OK;
 }
 
-// The smallest of the items [0, total) that equals an earlier item (total when none): keys(key, idx) launches
-// the key kernel over [0, total), dups(skey, sidx, first) the comparison over the sorted items.
-template <class Keys, class Dups>
-int first_duplicate(fem_gpu* h, size_t total, Keys keys, Dups dups, size_t* first) {
-  *first = total;
-  if (total < 2) return FEM_GPU_OK;
-  cudaStream_t s = h->stream;
+// The smallest of the items [0, total) that equals an earlier item (total when none), in two steps so
+// that host work runs while the GPU searches: dup_start enqueues the key kernel keys(key, idx) over
+// [0, total), a stable radix sort of (key, item) and the comparison dups(skey, sidx, first) over the
+// sorted items; dup_finish waits for the result.
+struct DupSearch {
   DevBuf<unsigned long long> key, skey, out;
   DevBuf<uint32_t> idx, sidx;
-  CK(key.reserve(total, s));
-  CK(skey.reserve(total, s));
-  CK(idx.reserve(total, s));
-  CK(sidx.reserve(total, s));
-  CK(out.reserve(1, s));
+  size_t total = 0;
+};
+
+template <class Keys, class Dups>
+int dup_start(fem_gpu* h, DupSearch& d, size_t total, Keys keys, Dups dups) {
+  d.total = total;
+  if (total < 2) return FEM_GPU_OK;
+  cudaStream_t s = h->stream;
+  CK(d.key.reserve(total, s));
+  CK(d.skey.reserve(total, s));
+  CK(d.idx.reserve(total, s));
+  CK(d.sidx.reserve(total, s));
+  CK(d.out.reserve(1, s));
   const unsigned long long none = total;
-  CK(cudaMemcpyAsync(out.p, &none, sizeof none, cudaMemcpyHostToDevice, s));
-  keys(key.p, idx.p);
+  CK(cudaMemcpyAsync(d.out.p, &none, sizeof none, cudaMemcpyHostToDevice, s));
+  keys(d.key.p, d.idx.p);
   CK(cudaGetLastError());
   int st = cub_call(h, [&](void* tmp, size_t& bytes) {
-    return cub::DeviceRadixSort::SortPairs(tmp, bytes, key.p, skey.p, idx.p, sidx.p, (int64_t)total, 0, 64, s);
+    return cub::DeviceRadixSort::SortPairs(tmp, bytes, d.key.p, d.skey.p, d.idx.p, d.sidx.p, (int64_t)total, 0, 64, s);
   });
   if (st) return st;
-  dups(skey.p, sidx.p, out.p);
+  dups(d.skey.p, d.sidx.p, d.out.p);
   CK(cudaGetLastError());
+  return FEM_GPU_OK;
+}
+
+int dup_finish(fem_gpu* h, DupSearch& d, size_t* first) {
+  *first = d.total;
+  if (d.total < 2) return FEM_GPU_OK;
   unsigned long long f = 0;
-  CK(cudaMemcpyAsync(&f, out.p, sizeof f, cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
+  CK(cudaMemcpyAsync(&f, d.out.p, sizeof f, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
   *first = (size_t)f;
   return FEM_GPU_OK;
 }
@@ -1610,8 +1703,10 @@ __global__ void k_pair_dups(size_t n, const unsigned long long* __restrict__ ske
   atomicMin(first, (unsigned long long)sidx[k]);
 }
 
-template <class Launch>
-int first_failure(fem_gpu* h, size_t count, Launch launch, size_t* first_bad, int* code) {
+// The first of the items [0, count) that the validation kernel launch(status, first) rejects, with its error code
+// (*first_bad = count when none).
+template <class Launch, class Host>
+int first_failure(fem_gpu* h, size_t count, Launch launch, Host host, size_t* first_bad, int* code) {
   *first_bad = count;
   *code = 0;
   if (!count) return FEM_GPU_OK;
@@ -1621,6 +1716,7 @@ int first_failure(fem_gpu* h, size_t count, Launch launch, size_t* first_bad, in
   CK(cudaMemcpyAsync(h->vfirst.p, &init, sizeof init, cudaMemcpyHostToDevice, h->stream));
   launch(h->vstatus.p, h->vfirst.p);
   CK(cudaGetLastError());
+  host();  // host work that does not wait for the result runs while the GPU validates
   unsigned long long first = 0;
   CK(cudaMemcpyAsync(&first, h->vfirst.p, sizeof first, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -1764,19 +1860,17 @@ unsigned add_threads() {
   return std::max(1u, std::min<unsigned>(hw ? hw : 1u, kRegParts));
 }
 
-// f(t) on threads t = 0 .. T-1 (t = 0 on the calling thread)
-template <class F>
-void run_threads(unsigned T, F f) {
-  std::vector<std::thread> th;
-  for (unsigned t = 1; t < T; ++t) th.emplace_back(f, t);
-  f(0u);
-  for (auto& x : th) x.join();
-}
-
-// f(t, begin, end) over [0, n) in T contiguous chunks, chunk t on thread t
-template <class F>
-void parallel_chunks(unsigned T, size_t n, F f) {
-  run_threads(T, [&](unsigned t) { f(t, n * t / T, n * (t + 1) / T); });
+// dst += src[0, count), by several threads for bulk calls (a fresh array's first touch is most of the cost)
+void append_host(HostVec<uint32_t>& dst, const uint32_t* src, size_t count) {
+  const size_t at = dst.size();
+  dst.resize(at + count);
+  if (count < kParallelAdd) {
+    if (count) std::memcpy(dst.data() + at, src, count * sizeof(uint32_t));
+    return;
+  }
+  parallel_chunks(add_threads(), count, [&](unsigned, size_t b, size_t e) {
+    std::memcpy(dst.data() + at + b, src + b, (e - b) * sizeof(uint32_t));
+  });
 }
 
 // the thread (of T) that owns a registry partition; 0xff for an item without a key
@@ -1874,7 +1968,7 @@ void ensure_coords(fem_gpu* h) {
   h->coords_built = h->n_nodes;
 }
 
-void ensure_pairs(PartTable& reg, size_t* built, size_t count, const std::vector<uint32_t>& nodes) {
+void ensure_pairs(PartTable& reg, size_t* built, size_t count, const HostVec<uint32_t>& nodes) {
   if (*built >= count) return;
   reg.reserve(count);
   registry_catch_up(reg, *built, count - *built, [&](size_t e, uint64_t* k) {
@@ -1918,8 +2012,21 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
     std::vector<uint32_t> tmax(T, 0);
     h->node_ck.resize(start + n);
     h->idx_number.resize(start + n);
-    // the call's coordinates go up first: the GPU checks them against every node while the host checks numbers
+    // the call's coordinates go up first: the GPU looks for the smallest new node equal to an earlier node (of
+    // the model or of the call) while the host checks the numbers
     CK(upload(h->stage, 0, xyz, 3 * n, h->stream));
+    const CoordSource src{h->dx.p, h->dy.p, h->dz.p, h->stage.p, start};
+    const size_t total = start + n;
+    DupSearch dup;
+    st = dup_start(
+        h, dup, total,
+        [&](unsigned long long* key, uint32_t* idx) {
+          k_coord_keys<<<grid_for(total, 256), 256, 0, h->stream>>>(total, src, key, idx);
+        },
+        [&](const unsigned long long* skey, const uint32_t* sidx, unsigned long long* out) {
+          k_coord_dups<<<grid_for(total, 256), 256, 0, h->stream>>>(total, skey, sidx, src, out);
+        });
+    if (st) return st;
     parallel_chunks(T, n, [&](unsigned t, size_t b, size_t e) {
       uint32_t mx = 0;
       for (size_t q = b; q < e; ++q) {
@@ -1942,19 +2049,8 @@ extern "C" int fem_gpu_add_nodes(fem_gpu_t* h, const uint32_t* numbers, const do
           return true;
         },
         [&](size_t) { return true; }, [&](size_t q) { h->node_idx.prefetch(numbers[q]); }, [&](size_t) {}, &role);
-    // exact coordinates: the smallest new node equal to an earlier node (of the model or of the call)
-    const CoordSource src{h->dx.p, h->dy.p, h->dz.p, h->stage.p, start};
-    const size_t total = start + n;
     size_t fc = total;
-    st = first_duplicate(
-        h, total,
-        [&](unsigned long long* key, uint32_t* idx) {
-          k_coord_keys<<<grid_for(total, 256), 256, 0, h->stream>>>(total, src, key, idx);
-        },
-        [&](const unsigned long long* skey, const uint32_t* sidx, unsigned long long* out) {
-          k_coord_dups<<<grid_for(total, 256), 256, 0, h->stream>>>(total, skey, sidx, src, out);
-        },
-        &fc);
+    st = dup_finish(h, dup, &fc);
     if (st) return st;
     if (fc >= start && fc - start < f) {  // (nodes of the model are distinct: fc < start cannot happen)
       f = fc - start;
@@ -2077,6 +2173,18 @@ int two_node_checks(fem_gpu* h, const char* kind, NumberMap& by_num, DevBuf<int3
   // against every element's of the kind while the host checks the numbers
   CK(upload(dn1, base, i1.data(), limit, h->stream));
   CK(upload(dn2, base, i2.data(), limit, h->stream));
+  const size_t total = base + limit;
+  const int32_t *d1 = dn1.p, *d2 = dn2.p;
+  DupSearch dup;
+  int st = dup_start(
+      h, dup, total,
+      [&](unsigned long long* key, uint32_t* idx) {
+        k_pair_keys<<<grid_for(total, 256), 256, 0, h->stream>>>(total, d1, d2, key, idx);
+      },
+      [&](const unsigned long long* skey, const uint32_t* sidx, unsigned long long* out) {
+        k_pair_dups<<<grid_for(total, 256), 256, 0, h->stream>>>(total, skey, sidx, out);
+      });
+  if (st) return st;
   by_num.fit(*std::max_element(tmax.begin(), tmax.end()));
   parallel_chunks(T, n, [&](unsigned, size_t b, size_t e) {
     for (size_t q = b; q < e; ++q) pa[q] = owner.of_part(by_num.part(numbers[q]));
@@ -2090,18 +2198,8 @@ int two_node_checks(fem_gpu* h, const char* kind, NumberMap& by_num, DevBuf<int3
         return true;
       },
       [&](size_t) { return true; }, [&](size_t q) { by_num.prefetch(numbers[q]); }, [&](size_t) {}, &role);
-  const size_t total = base + limit;
   size_t fp = total;
-  const int32_t *d1 = dn1.p, *d2 = dn2.p;
-  const int st = first_duplicate(
-      h, total,
-      [&](unsigned long long* key, uint32_t* idx) {
-        k_pair_keys<<<grid_for(total, 256), 256, 0, h->stream>>>(total, d1, d2, key, idx);
-      },
-      [&](const unsigned long long* skey, const uint32_t* sidx, unsigned long long* out) {
-        k_pair_dups<<<grid_for(total, 256), 256, 0, h->stream>>>(total, skey, sidx, out);
-      },
-      &fp);
+  st = dup_finish(h, dup, &fp);
   if (st) return st;
   if (fp >= base && fp - base < f) {  // (the model's elements have distinct pairs: fp < base cannot happen)
     f = fp - base;
@@ -2158,6 +2256,18 @@ int plate_checks(fem_gpu* h, const uint32_t* numbers, const uint32_t* nodes, siz
     DevBuf<int32_t>& dst = c == 0 ? h->p_n1 : c == 1 ? h->p_n2 : c == 2 ? h->p_n3 : h->p_n4;
     CK(upload(dst, base, id[c].data(), limit, h->stream));
   }
+  const size_t total = base + limit;
+  const int32_t *n1 = h->p_n1.p, *n2 = h->p_n2.p, *n3 = h->p_n3.p, *n4 = h->p_n4.p;
+  DupSearch dup;
+  int st = dup_start(
+      h, dup, total,
+      [&](unsigned long long* key, uint32_t* idx) {
+        k_set4_keys<<<grid_for(total, 256), 256, 0, h->stream>>>(total, n1, n2, n3, n4, key, idx);
+      },
+      [&](const unsigned long long* skey, const uint32_t* sidx, unsigned long long* out) {
+        k_set4_dups<<<grid_for(total, 256), 256, 0, h->stream>>>(total, skey, sidx, n1, n2, n3, n4, out);
+      });
+  if (st) return st;
   h->p_by_num.fit(*std::max_element(tmax.begin(), tmax.end()));
   parallel_chunks(T, n, [&](unsigned, size_t b, size_t e) {
     for (size_t q = b; q < e; ++q) pa[q] = owner.of_part(h->p_by_num.part(numbers[q]));
@@ -2171,18 +2281,8 @@ int plate_checks(fem_gpu* h, const uint32_t* numbers, const uint32_t* nodes, siz
         return true;
       },
       [&](size_t) { return true; }, [&](size_t q) { h->p_by_num.prefetch(numbers[q]); }, [&](size_t) {}, &role);
-  const size_t total = base + limit;
   size_t fs = total;
-  const int32_t *n1 = h->p_n1.p, *n2 = h->p_n2.p, *n3 = h->p_n3.p, *n4 = h->p_n4.p;
-  const int st = first_duplicate(
-      h, total,
-      [&](unsigned long long* key, uint32_t* idx) {
-        k_set4_keys<<<grid_for(total, 256), 256, 0, h->stream>>>(total, n1, n2, n3, n4, key, idx);
-      },
-      [&](const unsigned long long* skey, const uint32_t* sidx, unsigned long long* out) {
-        k_set4_dups<<<grid_for(total, 256), 256, 0, h->stream>>>(total, skey, sidx, n1, n2, n3, n4, out);
-      },
-      &fs);
+  st = dup_finish(h, dup, &fs);
   if (st) return st;
   if (fs >= base && fs - base < f) {  // (the model's plates have distinct node sets: fs < base cannot happen)
     f = fs - base;
@@ -2199,8 +2299,8 @@ int plate_checks(fem_gpu* h, const uint32_t* numbers, const uint32_t* nodes, siz
                    nn[0], nn[1], nn[2], nn[3]);
   int32_t idx;
   for (int c = 0; c < 4; ++c) {
-    const int st = lookup_node(h, nn[c], &idx);
-    if (st) return st;
+    const int sl = lookup_node(h, nn[c], &idx);
+    if (sl) return sl;
   }
   return FEM_GPU_OK;
 }
@@ -2272,17 +2372,24 @@ extern "C" int fem_gpu_add_trusses(fem_gpu_t* h, const uint32_t* numbers, const 
   NodesView nd = h->nodes();
   int32_t *n1 = h->t_n1.p, *n2 = h->t_n2.p;
   double *E = h->t_E.p, *A = h->t_A.p, *A2 = h->t_A2.p;
-  st = first_failure(h, m, [&](int* s, unsigned long long* f) {
-    k_validate_truss<<<grid_for(m, 128), 128, 0, h->stream>>>(nd, n1, n2, E, A, A2, base, m, s, f);
-  }, &bad, &code);
+  st = first_failure(
+      h, m,
+      [&](int* s, unsigned long long* f) {
+        k_validate_truss<<<grid_for(m, 128), 128, 0, h->stream>>>(nd, n1, n2, E, A, A2, base, m, s, f);
+      },
+      [&] {  // the host arrays take every item now and drop the rejected ones after the result
+        append_host(h->t_num, numbers, m);
+        append_host(h->t_nodes, nodes, 2 * m);
+      },
+      &bad, &code);
+  size_t accepted = st ? 0 : std::min(m, bad);
+  h->t_num.resize(base + accepted);
+  h->t_nodes.resize(2 * (base + accepted));
   if (st) return st;
-  size_t accepted = std::min(m, bad);
   for (size_t j = accepted; j < m; ++j) {  // roll back registry entries past the failure
     h->t_by_num.erase(numbers[j], (int64_t)(base + j));
     if (!bulk) h->t_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]), (int64_t)(base + j));
   }
-  h->t_num.insert(h->t_num.end(), numbers, numbers + accepted);
-  h->t_nodes.insert(h->t_nodes.end(), nodes, nodes + 2 * accepted);
   h->nt += accepted;
   if (!bulk) h->t_pairs_built = h->nt;
   h->append_run(kTruss, base, accepted);
@@ -2396,17 +2503,24 @@ extern "C" int fem_gpu_add_beams(fem_gpu_t* h, const uint32_t* numbers, const ui
   int code;
   NodesView nd = h->nodes();
   BeamView bv = h->beams();
-  st = first_failure(h, m, [&](int* s, unsigned long long* f) {
-    k_validate_beam<<<grid_for(m, 128), 128, 0, h->stream>>>(nd, bv, base, m, s, f);
-  }, &bad, &code);
+  st = first_failure(
+      h, m,
+      [&](int* s, unsigned long long* f) {
+        k_validate_beam<<<grid_for(m, 128), 128, 0, h->stream>>>(nd, bv, base, m, s, f);
+      },
+      [&] {  // the host arrays take every item now and drop the rejected ones after the result
+        append_host(h->b_num, numbers, m);
+        append_host(h->b_nodes, nodes, 2 * m);
+      },
+      &bad, &code);
+  size_t accepted = st ? 0 : std::min(m, bad);
+  h->b_num.resize(base + accepted);
+  h->b_nodes.resize(2 * (base + accepted));
   if (st) return st;
-  size_t accepted = std::min(m, bad);
   for (size_t j = accepted; j < m; ++j) {
     h->b_by_num.erase(numbers[j], (int64_t)(base + j));
     if (!bulk) h->b_pairs.erase(pair_key(nodes[2 * j], nodes[2 * j + 1]), (int64_t)(base + j));
   }
-  h->b_num.insert(h->b_num.end(), numbers, numbers + accepted);
-  h->b_nodes.insert(h->b_nodes.end(), nodes, nodes + 2 * accepted);
   h->nbm += accepted;
   if (!bulk) h->b_pairs_built = h->nbm;
   h->append_run(kBeam, base, accepted);
@@ -2535,17 +2649,24 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
   NodesView nd = h->nodes();
   PlateView pv = h->plates();
   double abs_tol = h->abs_tol;
-  st = first_failure(h, m, [&](int* s, unsigned long long* f) {
-    k_validate_plate<<<grid_for(m, 128), 128, 0, h->stream>>>(nd, pv, abs_tol, base, m, s, f);
-  }, &bad, &code);
+  st = first_failure(
+      h, m,
+      [&](int* s, unsigned long long* f) {
+        k_validate_plate<<<grid_for(m, 128), 128, 0, h->stream>>>(nd, pv, abs_tol, base, m, s, f);
+      },
+      [&] {  // the host arrays take every item now and drop the rejected ones after the result
+        append_host(h->p_num, numbers, m);
+        append_host(h->p_nodes, nodes, 4 * m);
+      },
+      &bad, &code);
+  size_t accepted = st ? 0 : std::min(m, bad);
+  h->p_num.resize(base + accepted);
+  h->p_nodes.resize(4 * (base + accepted));
   if (st) return st;
-  size_t accepted = std::min(m, bad);
   for (size_t j = accepted; j < m; ++j) {
     h->p_by_num.erase(numbers[j], (int64_t)(base + j));
     if (sequential) h->p_sets.erase(set4_hash(sorted4(nodes + 4 * j)), (int64_t)(base + j));
   }
-  h->p_num.insert(h->p_num.end(), numbers, numbers + accepted);
-  h->p_nodes.insert(h->p_nodes.end(), nodes, nodes + 4 * accepted);
   h->np += accepted;
   if (sequential) h->sets_built = h->np;
   h->append_run(kPlate, base, accepted);

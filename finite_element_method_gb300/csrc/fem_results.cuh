@@ -282,7 +282,7 @@ extern "C" int fem_gpu_results_last_ms(fem_gpu_t* h, float* ms) {
 
 extern "C" int fem_gpu_get_element_numbers(fem_gpu_t* h, int kind, uint32_t* numbers) {
   if (!h || !numbers || kind < 0 || kind > 2) return FEM_GPU_ERR_ARGUMENT;
-  const std::vector<uint32_t>& v = kind == 0 ? h->t_num : kind == 1 ? h->b_num : h->p_num;
+  const HostVec<uint32_t>& v = kind == 0 ? h->t_num : kind == 1 ? h->b_num : h->p_num;
   if (!v.empty()) memcpy(numbers, v.data(), v.size() * sizeof(uint32_t));
   return FEM_GPU_OK;
 }
