@@ -1155,8 +1155,8 @@ inline int reg_part(uint64_t key) { return (int)(mix64(key) >> 60); }
 // costs about a quarter of a millisecond, as much as one pass over a million items, and a bulk call
 // makes four passes, so the workers stay and sleep on a condition variable between passes.  One pass
 // runs at a time: a pass that finds the pool busy (a pass of another host thread, or one started from
-// inside a worker) or that runs in a process forked after the pool started returns false, and the
-// caller runs it on threads of its own.
+// inside a pass, on a worker or on the calling thread) or that runs in a process forked after the pool
+// started returns false, and the caller runs it on threads of its own.
 class HostPool {
  public:
   static HostPool* get() {
@@ -1168,8 +1168,10 @@ class HostPool {
   }
   // f(t) for t = 0 .. T-1, t = 0 on the calling thread
   bool run(unsigned T, const std::function<void(unsigned)>& f) {
+    if (in_pass_) return false;  // a pass inside a pass (the calling thread must not try busy_ twice)
     std::unique_lock<std::mutex> busy(busy_, std::try_to_lock);
     if (!busy.owns_lock() || T - 1 > workers_.size()) return false;
+    in_pass_ = true;
     {
       std::lock_guard<std::mutex> g(m_);
       job_ = &f;
@@ -1182,6 +1184,7 @@ class HostPool {
     std::unique_lock<std::mutex> g(m_);
     done_.wait(g, [&] { return pending_ == 0; });
     job_ = nullptr;
+    in_pass_ = false;
     return true;
   }
 
@@ -1195,6 +1198,7 @@ class HostPool {
     }
   }
   void loop(unsigned w) {
+    in_pass_ = true;  // a worker runs nothing but passes
     uint64_t seen = 0;
     std::unique_lock<std::mutex> g(m_);
     for (;;) {
@@ -1215,7 +1219,9 @@ class HostPool {
   const std::function<void(unsigned)>* job_ = nullptr;
   unsigned job_threads_ = 0, pending_ = 0;
   uint64_t gen_ = 0;
+  static thread_local bool in_pass_;
 };
+thread_local bool HostPool::in_pass_ = false;
 
 // f(t) on threads t = 0 .. T-1 (t = 0 on the calling thread): the pool's workers, else threads of its own
 template <class F>
