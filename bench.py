@@ -78,6 +78,20 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def max_over_ranks(x: float) -> float:
+    """the largest of x over the ranks of the default process group (x itself when there is none): every
+    replica times the same work, and the job takes as long as its slowest replica"""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """SM clocks and throttle reasons sampled by one `nvidia-smi -lms` process that runs exactly while the timed
     region runs (started on entry, terminated on exit; every line it printed is a sample from inside)."""
@@ -657,11 +671,7 @@ def main():
             red_ms.append(b)
     torch.cuda.synchronize()
     fem.check_pattern()
-    t_step = float(np.sum(step_ms)) / args.steps
-    if world > 1:
-        tt = torch.tensor([t_step], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = max_over_ranks(float(np.sum(step_ms)) / args.steps)
     value = n_el * world / (t_step * 1e-3)
 
     # roofline of the dominant kernel
@@ -751,7 +761,7 @@ def main():
         f2.close()
     if not e2e_ms:
         e2e_ms, phases = [float("nan")], [[float("nan")] * 3]
-    e2e_t = float(np.median(e2e_ms))
+    e2e_t = max_over_ranks(float(np.median(e2e_ms)))
     ph = np.median(np.array(phases), axis=0)
     e2e = {"value": n_el * world / (e2e_t * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t,
