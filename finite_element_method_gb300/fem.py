@@ -28,6 +28,7 @@ import numpy as np
 from . import _lib
 from ._lib import ptr
 
+FEM_GPU_ERR_NODE_LIMIT = 1
 FEM_GPU_ERR_NODE_NOT_EXIST = 5
 FEM_GPU_ERR_ARGUMENT = 30
 FEM_GPU_ERR_CUDA = 40
@@ -58,6 +59,21 @@ class FEM:
         self._check(self._L.fem_gpu_create(rel_tol, abs_tol, nodes_number, ctypes.byref(h)), None)
         self._h = h
         self.rel_tol, self.abs_tol, self.nodes_number = rel_tol, abs_tol, nodes_number
+        self._node_limit = nodes_number  # the crate's props keep the nodes_number of create, reset or not
+
+    def reset(self, nodes_number: int) -> None:
+        """FEM::reset (fem.rs:155-169): drop every node, element, load and imposed displacement and size the
+        stiffness, forces and displacements for `nodes_number` nodes.  As in the crate, the tolerances and
+        the node limit stay those of create (reset leaves the crate's props untouched): add_node refuses the
+        node past the nodes_number given at creation, with the crate's message, even after a reset to more.
+        After a reset to fewer nodes the handle refuses the node past the new count; the crate would accept
+        it although its DOFs lie outside the matrix and the vectors it has just sized."""
+        h = c_void_p()
+        self._check(self._L.fem_gpu_create(self.rel_tol, self.abs_tol, nodes_number, ctypes.byref(h)), None)
+        self.close()
+        self._h = h
+        self.nodes_number = nodes_number
+        self._imposed_arr = self._displacements = self._result_forces = None
 
     # -- plumbing ---------------------------------------------------------
     def close(self):
@@ -95,10 +111,15 @@ class FEM:
     def add_nodes(self, numbers, xyz) -> int:
         numbers = _u32(numbers, (-1,))
         xyz = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64).reshape(len(numbers), 3))
+        m = len(numbers)
+        if self._node_limit < self.nodes_number:  # reset to more nodes than at creation: the old limit holds
+            m = min(m, max(self._node_limit - self.node_count(), 0))
         n = c_size_t(0)
-        st = self._L.fem_gpu_add_nodes(self._h, ptr(numbers, c_uint32), ptr(xyz, c_double), len(numbers),
-                                       ctypes.byref(n))
-        self._check(st)
+        if m:
+            st = self._L.fem_gpu_add_nodes(self._h, ptr(numbers, c_uint32), ptr(xyz, c_double), m, ctypes.byref(n))
+            self._check(st)
+        if m < len(numbers):
+            raise FEMError(FEM_GPU_ERR_NODE_LIMIT, f"Nodes number could not be greater than {self._node_limit}!")
         return n.value
 
     def add_truss(self, number, node_1_number, node_2_number, young_modulus, area, area_2=None) -> None:
