@@ -73,7 +73,7 @@ class FEM:
         self.close()
         self._h = h
         self.nodes_number = nodes_number
-        self._imposed_arr = self._displacements = self._result_forces = None
+        self._imposed_arr = self._displacements = self._result_forces = self._lookup = None
 
     # -- plumbing ---------------------------------------------------------
     def close(self):
@@ -313,17 +313,38 @@ class FEM:
 
     def add_displacement(self, node_number: int, dof_parameter, value: float = 0.0) -> None:
         """add_displacement (methods_for_bc_data_handle.rs:176-203): impose a displacement on one DOF."""
-        dof = dof_parameter if isinstance(dof_parameter, int) else self.DOF_PARAMETERS.index(dof_parameter)
-        index = self._node_index(node_number)
-        if index is None:
-            raise FEMError(FEM_GPU_ERR_NODE_NOT_EXIST, f"Node with number {node_number} does not exist!")
+        self.add_displacements([node_number], [self._dof(dof_parameter)], [value])
+
+    def add_displacements(self, node_numbers, dofs, values=0.0) -> int:
+        """add_displacement for every (node, DOF, value) in call order, stopping at the first failure like a
+        loop of single calls: a node that does not exist, or a DOF already imposed (by an earlier call or
+        earlier in this one).  The items before the failure stay imposed; returns how many were imposed."""
+        numbers = np.atleast_1d(np.asarray(node_numbers, dtype=np.int64))
+        m = len(numbers)
+        d = np.atleast_1d(np.asarray(dofs))
+        d = np.array([self._dof(x) for x in d], np.int64) if d.dtype.kind in "OU" else d.astype(np.int64)
+        d = np.broadcast_to(d, (m,))
+        if m and (d.min() < 0 or d.max() > 5):
+            raise FEMError(FEM_GPU_ERR_ARGUMENT, "DOF parameter out of range (0 X .. 5 ThZ)")
+        v = np.broadcast_to(np.asarray(values, dtype=np.float64), (m,))
         imp = self._imposed()
-        k = 6 * index + dof
-        if imp[k]:
-            raise FEMError(FEM_GPU_ERR_ARGUMENT,
-                           f"Displacement {self.DOF_PARAMETERS[dof]} already applied to node {node_number}!")
-        imp[k] = 1
-        self._displacements[k] = value
+        idx = self._node_indexes(numbers)
+        k = np.where(idx >= 0, 6 * idx + d, -1 - np.arange(m))  # (missing nodes get keys of their own)
+        bad = idx < 0
+        bad[idx >= 0] |= imp[k[idx >= 0]] != 0
+        _, first = np.unique(k, return_index=True)
+        repeat = np.ones(m, bool)
+        repeat[first] = False
+        bad |= repeat
+        f = int(np.argmax(bad)) if bad.any() else m
+        imp[k[:f]] = 1
+        self._displacements[k[:f]] = v[:f]
+        if f == m:
+            return m
+        if idx[f] < 0:
+            raise FEMError(FEM_GPU_ERR_NODE_NOT_EXIST, f"Node with number {numbers[f]} does not exist!")
+        raise FEMError(FEM_GPU_ERR_ARGUMENT,
+                       f"Displacement {self.DOF_PARAMETERS[d[f]]} already applied to node {numbers[f]}!")
 
     def _dof(self, dof_parameter):
         return dof_parameter if isinstance(dof_parameter, (int, np.integer)) else self.DOF_PARAMETERS.index(dof_parameter)
@@ -381,10 +402,32 @@ class FEM:
             self._displacements = np.zeros(6 * self.nodes_number)
         return self._imposed_arr
 
-    def _node_index(self, number):
-        numbers = self.index_node_numbers()
-        hit = np.flatnonzero(numbers == number)
-        return int(hit[0]) if hit.size else None
+    def _node_indexes(self, numbers):
+        """the node index of each node number (-1 where no node has it).  Node numbers are unique and nodes
+        are only appended, so the lookup keeps the numbers sorted up to some node count and scans the few
+        nodes added after it, sorting again once those are more than an eighth of the sorted ones."""
+        count = self.node_count()
+        lk = getattr(self, "_lookup", None)
+        if lk is None or lk[0] > count or 8 * (count - lk[0]) > max(lk[0], 8192):
+            all_numbers = self.index_node_numbers().astype(np.int64)
+            order = np.argsort(all_numbers, kind="stable")
+            self._lookup = lk = (count, all_numbers[order], order)
+        c0, srt, order = lk
+        numbers = np.asarray(numbers, dtype=np.int64)
+        out = np.full(numbers.shape, -1, np.int64)
+        if c0:
+            pos = np.minimum(np.searchsorted(srt, numbers), c0 - 1)
+            hit = srt[pos] == numbers
+            out[hit] = order[pos[hit]]
+        if count > c0:
+            tail = self.index_node_numbers()[c0:].astype(np.int64)
+            t_order = np.argsort(tail, kind="stable")
+            t_srt = tail[t_order]
+            miss = np.flatnonzero(out < 0)
+            pos = np.minimum(np.searchsorted(t_srt, numbers[miss]), len(t_srt) - 1)
+            hit = t_srt[pos] == numbers[miss]
+            out[miss[hit]] = c0 + t_order[pos[hit]]
+        return out
 
     def separate_stiffness_matrix_sparse_iterative(self, imposed=None) -> "SeparatedStiffnessSparse":
         """separate_stiffness_matrix_sparse_iterative (methods_for_separate_stiffness_matrix.rs:217-320) on the

@@ -1,8 +1,11 @@
-"""CPU checks of the host mirror's FEM::reset (fem.rs:155-169): no device work happens before the first
-add, so the handle swap, the new sizes and the kept node limit are checked here without a GPU."""
+"""CPU checks of the host mirror: FEM::reset (fem.rs:155-169) and add_displacement
+(methods_for_bc_data_handle.rs:176-203), single and bulk.  No device work happens before the first add,
+so these run without a GPU: the handle swap, the new sizes and the kept node limit, and the imposed DOFs,
+values and messages against a sequential loop over a stand-in node table."""
 import numpy as np
+import pytest
 
-from finite_element_method_gb300 import FEM
+from finite_element_method_gb300 import FEM, FEMError
 
 
 def test_reset_sizes_vectors_and_keeps_tolerances_and_limit():
@@ -19,3 +22,78 @@ def test_reset_sizes_vectors_and_keeps_tolerances_and_limit():
     assert g.displacements_vector().shape == (12,)
     g.close()
     assert g.handle is None
+
+
+class _Nodes:
+    """stands in for the node table of a handle (the add_nodes upload needs a GPU): node numbers in index order"""
+
+    def __init__(self, g):
+        self.numbers = []
+        g.node_count = lambda: len(self.numbers)
+        g.index_node_numbers = lambda: np.array(self.numbers, np.uint32)
+
+
+def _sequential(numbers, imposed, values, calls):
+    """add_displacement (methods_for_bc_data_handle.rs:176-203) one item at a time: node lookup by number,
+    the node's DOF 6 * index + p, refusal of a DOF imposed before"""
+    index = {n: i for i, n in enumerate(numbers)}
+    done = 0
+    for n, p, v in calls:
+        if n not in index:
+            return done, f"Node with number {n} does not exist!"
+        k = 6 * index[n] + p
+        if imposed[k]:
+            return done, f"Displacement {FEM.DOF_PARAMETERS[p]} already applied to node {n}!"
+        imposed[k] = 1
+        values[k] = v
+        done += 1
+    return done, None
+
+
+def test_add_displacement_single_and_bulk_messages():
+    g = FEM(1e-12, 1e-12, 10)
+    nodes = _Nodes(g)
+    nodes.numbers += [5, 3, 9]
+    g.add_displacement(3, "Y", 0.5)
+    assert g.displacements_vector()[7] == 0.5 and g._imposed()[7] == 1
+    with pytest.raises(FEMError, match=r"^Displacement Y already applied to node 3!$"):
+        g.add_displacement(3, 1, 0.0)
+    with pytest.raises(FEMError, match=r"^Node with number 7 does not exist!$"):
+        g.add_displacements([9, 7], ["ThZ", "X"], [1.0, 2.0])
+    assert g._imposed()[6 * 2 + 5] == 1  # the item before the failure stays imposed
+    with pytest.raises(FEMError, match=r"^Displacement Z already applied to node 5!$"):
+        g.add_displacements([5, 5], "Z", 0.0)  # a repeat inside one call
+    assert g.add_displacements([], [], []) == 0
+    with pytest.raises(FEMError):
+        g.add_displacements([5], [6], [0.0])
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_add_displacements_match_a_sequential_loop(seed):
+    rng = np.random.default_rng(seed)
+    cap = 30000
+    g = FEM(1e-12, 1e-12, cap)
+    nodes = _Nodes(g)
+    pool = rng.permutation(np.arange(1, 10 * cap, dtype=np.int64))
+    imposed, values = np.zeros(6 * cap, np.uint8), np.zeros(6 * cap)
+    used = 0
+    for step in range(40):
+        grow = int(rng.choice([0, 1, 37, 2000, 9000]))  # small tails and growth past a re-sort
+        grow = min(grow, cap - used)
+        nodes.numbers += [int(x) for x in pool[used:used + grow]]
+        used += grow
+        m = int(rng.integers(1, 400))
+        known = np.asarray(nodes.numbers or [1], np.int64)
+        numbers = np.where(rng.random(m) < 0.995, rng.choice(known, m), rng.choice(pool[used:used + 50] if used < cap
+                                                                                     else [0], m))
+        dofs = rng.integers(0, 6, m)
+        vals = rng.standard_normal(m)
+        want_n, want_msg = _sequential(nodes.numbers, imposed, values, zip(numbers.tolist(), dofs.tolist(), vals))
+        if want_msg is None:
+            assert g.add_displacements(numbers, dofs, vals) == m
+        else:
+            with pytest.raises(FEMError) as e:
+                g.add_displacements(numbers, dofs, vals)
+            assert str(e.value) == want_msg
+        np.testing.assert_array_equal(g._imposed(), imposed)
+        np.testing.assert_array_equal(g.displacements_vector(), values)
