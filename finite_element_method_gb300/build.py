@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-diag-suppress", "550"]
 
-SOURCES = ["fem_gpu.cu", "fem_batch.cu", "fem_adjoint.cu", "fem_noalloc.cu"]
+SOURCES = ["fem_gpu.cu", "fem_noalloc.cu"]  # the .cuh parts (batch, adjoint, loads, separation, solve, results) are included by fem_gpu.cu
 
 
 def _nvcc() -> str:
