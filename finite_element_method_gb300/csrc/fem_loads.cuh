@@ -177,7 +177,7 @@ extern "C" int fem_gpu_add_concentrated_loads(fem_gpu_t* h, const uint32_t* node
       code = h->fail(FEM_GPU_ERR_ARGUMENT, "Incorrect dof parameter number!");
       break;
     }
-    int32_t i;
+    int32_t i = 0;
     if ((code = lookup_node(h, node_numbers[k], &i))) break;
     key[k] = 6ull * (unsigned long long)i + dofs[k];
   }
