@@ -39,3 +39,22 @@ def test_no_gpu_call_surface_without_device():
     h = ctypes.c_void_p()
     assert lib.fem_gpu_create(1e-12, 1e-12, 4, ctypes.byref(h)) == 0
     assert lib.fem_gpu_destroy(h) == 0
+
+
+def test_library_exports_nothing_undeclared():
+    """the reverse direction: every fem_gpu_* symbol the library exports is declared in include/*.h"""
+    import shutil
+    import subprocess
+
+    import pytest
+
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    from finite_element_method_gb300 import build
+
+    _lib.load()
+    out = subprocess.run([nm, "-D", "--defined-only", build.LIB_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.split() and line.split()[-1].startswith("fem_gpu_")}
+    assert exported == declared_symbols()
