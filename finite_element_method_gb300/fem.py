@@ -509,12 +509,10 @@ class FEM:
         forces = getattr(self, "_result_forces", None)
         if forces is None:
             forces = self.forces_vector()
-        out = []
-        for i, number in enumerate(self.index_node_numbers()):
-            for d in range(6):
-                out.append((int(number), self.DOF_PARAMETERS[d], float(self._displacements[6 * i + d]),
-                            float(forces[6 * i + d])))
-        return out
+        numbers = self.index_node_numbers().astype(np.int64)
+        n = 6 * len(numbers)
+        return list(zip(np.repeat(numbers, 6).tolist(), list(self.DOF_PARAMETERS) * len(numbers),
+                        self._displacements[:n].tolist(), np.asarray(forces[:n], np.float64).tolist()))
 
     def element_results(self, displacements=None, out=None):
         """Every element's results on the GPU (fem_gpu_element_results) from `displacements` (default: this

@@ -97,3 +97,22 @@ def test_add_displacements_match_a_sequential_loop(seed):
             assert str(e.value) == want_msg
         np.testing.assert_array_equal(g._imposed(), imposed)
         np.testing.assert_array_equal(g.displacements_vector(), values)
+
+
+def test_extract_global_analysis_result_rows():
+    """(node number, DOF, displacement, load) for every DOF of every node in node index order
+    (methods_for_global_analysis.rs:361-387), with Python ints, names and floats as the crate's tuples"""
+    g = FEM(1e-12, 1e-12, 5)
+    nodes = _Nodes(g)
+    nodes.numbers += [7, 2, 40]
+    rng = np.random.default_rng(0)
+    forces = rng.standard_normal(30)
+    g.forces_vector = lambda: forces.copy()
+    g.add_displacements([2, 40], ["ThY", "X"], [0.25, -1.5])
+    got = g.extract_global_analysis_result()
+    disp = g.displacements_vector()
+    want = [(n, FEM.DOF_PARAMETERS[d], float(disp[6 * i + d]), float(forces[6 * i + d]))
+            for i, n in enumerate(nodes.numbers) for d in range(6)]
+    assert got == want
+    assert all(type(r[0]) is int and type(r[1]) is str and type(r[2]) is float and type(r[3]) is float for r in got)
+    assert got[6 + 4] == (2, "ThY", 0.25, float(forces[10]))
