@@ -558,8 +558,9 @@ class FEM:
         out = []
         for kind, names in (("truss", self.TRUSS_COMPONENTS), ("beam", self.BEAM_COMPONENTS),
                             ("plate", self.PLATE_COMPONENTS)):
-            for number, row in zip(self.element_numbers(kind), res[kind]):
-                out.append((int(number), [(c, float(v)) for c, v in zip(names, row)]))
+            rows = np.asarray(res[kind], np.float64).reshape(-1, len(names)).tolist()
+            out.extend((number, list(zip(names, row)))
+                       for number, row in zip(np.asarray(self.element_numbers(kind), np.int64).tolist(), rows))
         return out
 
     def vjp_last_ms(self) -> float:

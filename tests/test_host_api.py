@@ -116,3 +116,24 @@ def test_extract_global_analysis_result_rows():
     assert got == want
     assert all(type(r[0]) is int and type(r[1]) is str and type(r[2]) is float and type(r[3]) is float for r in got)
     assert got[6 + 4] == (2, "ThY", 0.25, float(forces[10]))
+
+
+def test_extract_elements_analysis_result_rows():
+    """(element number, [(component, value), ...]) for the trusses, the beams, then the plates, in call order
+    (methods_for_element_analysis.rs:27-58)"""
+    g = FEM(1e-12, 1e-12, 5)
+    rng = np.random.default_rng(1)
+    res = {"truss": rng.standard_normal((2, 1)), "beam": rng.standard_normal((1, 10)),
+           "plate": rng.standard_normal((3, 8))}
+    nums = {"truss": np.array([4, 1], np.uint32), "beam": np.array([9], np.uint32),
+            "plate": np.array([3, 8, 2], np.uint32)}
+    g.element_results = lambda displacements=None, out=None: res
+    g.element_numbers = lambda kind: nums[kind]
+    got = g.extract_elements_analysis_result()
+    want = []
+    for kind, names in (("truss", FEM.TRUSS_COMPONENTS), ("beam", FEM.BEAM_COMPONENTS),
+                        ("plate", FEM.PLATE_COMPONENTS)):
+        for number, row in zip(nums[kind], res[kind]):
+            want.append((int(number), [(c, float(v)) for c, v in zip(names, row)]))
+    assert got == want
+    assert type(got[0][0]) is int and type(got[0][1][0][1]) is float
