@@ -677,12 +677,12 @@ def main():
     # roofline of the dominant kernel
     hbm_gbs, peak_src = measured_peaks()
     w = WORK[args.workload]
-    n_blocks, n_contrib, scratch, sum_slots = fem.pattern_stats()
+    n_blocks, n_contrib, scratch, n_adj = fem.pattern_stats()
     # element kernels: inputs + per-contribution offset and mask (16 B) + packed blocks written to scratch
     elem_bytes = n_el * IN_BYTES[args.workload] + n_contrib * 16 + scratch * 8
-    # reduction: packed scratch read once; per block-sum slot an 8-byte descriptor read and the sum written
-    # and gathered once; the CSR source map (4 B) read and the CSR values (8 B) written once
-    red_bytes = scratch * 8 + 3 * sum_slots * 8 + nnz * (4 + 8)
+    # reduction: packed scratch read once, one 16-byte adjacency record per (row node, adjacent block), per
+    # node its first record (4 B) and six row starts (48 B), the CSR values (8 B) written once
+    red_bytes = scratch * 8 + n_adj * 16 + mesh.nodes_number * (4 + 48) + nnz * 8
     t_e, t_r = float(np.mean(elem_ms)), float(np.mean(red_ms))
     kern = {"element": dict(ms=t_e, bytes=elem_bytes, flops=element_flops(args.workload, mesh)),
             "reduce": dict(ms=t_r, bytes=red_bytes, flops=scratch)}  # <= one FP64 add per packed entry

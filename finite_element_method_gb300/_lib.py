@@ -79,10 +79,29 @@ SIGNATURES = {
     "fem_gpu_get_separation_block": (c_int, [hp, c_int, i64p, i32p, dp]),
     "fem_gpu_get_separation_block_device": (c_int, [hp, c_int, POINTER(c_void_p), POINTER(c_void_p),
                                                     POINTER(c_void_p)]),
+    "fem_gpu_batch_create_from_arrays": (c_int, [c_double, c_double, c_void_p, POINTER(c_void_p)]),
+    "fem_gpu_batch_size": (c_int, [hp, szp]),
+    "fem_gpu_batch_get_csr_sizes": (c_int, [hp, c_size_t, i64p, i64p]),
+    "fem_gpu_batch_get_csr": (c_int, [hp, c_size_t, i64p, i32p, dp]),
     "fem_gpu_assemble_dense_noalloc": (c_int, [c_uint32, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p,
                                                c_void_p, c_size_t, c_void_p, c_void_p, c_double, c_double, c_void_p,
                                                c_void_p]),
 }
+
+
+
+class Structures(ctypes.Structure):
+    """fem_gpu_structures_t: the host arrays of many structures, structure after structure."""
+    _fields_ = [("n_structures", c_size_t), ("nodes_number", u32p), ("node_off", szp), ("node_numbers", u32p),
+                ("xyz", dp),
+                ("truss_off", szp), ("truss_numbers", u32p), ("truss_nodes", u32p), ("truss_young", dp),
+                ("truss_area", dp), ("truss_area2", dp),
+                ("beam_off", szp), ("beam_numbers", u32p), ("beam_nodes", u32p), ("beam_young", dp),
+                ("beam_poisson", dp), ("beam_area", dp), ("beam_i11", dp), ("beam_i22", dp), ("beam_i12", dp),
+                ("beam_it", dp), ("beam_shear_factor", dp), ("beam_local_axis", dp),
+                ("plate_off", szp), ("plate_numbers", u32p), ("plate_nodes", u32p), ("plate_young", dp),
+                ("plate_poisson", dp), ("plate_thickness", dp), ("plate_shear_factor", dp)]
+
 
 _lib = None
 

@@ -237,6 +237,19 @@ __device__ __forceinline__ bool is_identity(const T R[9]) {
   return R[0] == 1.0 && R[1] == 0.0 && R[2] == 0.0 && R[3] == 0.0 && R[4] == 1.0 && R[5] == 0.0 && R[6] == 0.0 &&
          R[7] == 0.0 && R[8] == 1.0;
 }
+// The same test on the integer pipe (on GB300 an FP64 compare takes a slot of
+// the narrow FP64 pipe): 1.0 exactly, +-0.0 exactly.
+__device__ __forceinline__ bool bits_one(double v) { return __double_as_longlong(v) == 0x3ff0000000000000ll; }
+__device__ __forceinline__ bool bits_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
+// v > 0.0 (false for +-0.0 and NaN)
+__device__ __forceinline__ bool bits_positive(double v) {
+  const long long b = __double_as_longlong(v);
+  return b > 0 && b <= 0x7ff0000000000000ll;
+}
+__device__ __forceinline__ bool is_identity(const double R[9]) {
+  return bits_one(R[0]) & bits_zero(R[1]) & bits_zero(R[2]) & bits_zero(R[3]) & bits_one(R[4]) & bits_zero(R[5]) &
+         bits_zero(R[6]) & bits_zero(R[7]) & bits_one(R[8]);
+}
 
 // symmetric R^T diag(d) R (upper computed, lower mirrored)
 template <class T>
@@ -524,15 +537,40 @@ __device__ __forceinline__ bool plate_rotation(const T x2[3], const T x3[3], con
   sub3(x4, x3, e34);
   sub3(x2, x3, e32);
   cross3(e34, e32, n);
-  if (n[0] == 0.0 && n[1] == 0.0 && n[2] > 0.0 && !IsDual<T>::value) {
-    set_identity(R);
-    return true;
+  if constexpr (!IsDual<T>::value) {
+    if (bits_zero(n[0]) & bits_zero(n[1]) & bits_positive(n[2])) {
+      set_identity(R);
+      return true;
+    }
   }
   T ln = norm3(n);
   if (!(ln > 0.0)) return false;
   T target[3] = {0.0, 0.0, ln};
   align_rotation(n, target, abs_tol, R);
   return true;
+}
+
+// Local in-plane coordinates of the nodes relative to node 3 (quad.rs:340-378):
+// (x, y) of R (X_i - X_3).  When R is exactly the identity they are the
+// differences themselves (the same values); otherwise each is one product and
+// two fused multiply-adds.
+template <class T>
+__device__ __forceinline__ void plate_local_xy(const T X[4][3], const T R[9], bool ident, T xl[4], T yl[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    xl[i] = 0.0;
+    yl[i] = 0.0;
+    if (i == 2) continue;
+    if (ident) {
+      xl[i] = X[i][0] - X[2][0];
+      yl[i] = X[i][1] - X[2][1];
+    } else {
+      T dd[3];
+      sub3(X[i], X[2], dd);
+      xl[i] = fma(R[2], dd[2], fma(R[1], dd[1], R[0] * dd[0]));
+      yl[i] = fma(R[5], dd[2], fma(R[4], dd[1], R[3] * dd[0]));
+    }
+  }
 }
 
 // Everything the plate's 6x6 node-pair blocks are made of (see
@@ -595,11 +633,12 @@ __device__ __forceinline__ void plate_core(const T xl[4], const T yl[4], T young
   T Wr[4], Ws[4];
 #pragma unroll
   for (int ip = 0; ip < 4; ++ip) {
-    T sp = 1.0 + ips[ip], sm = 1.0 - ips[ip], rp = 1.0 + ipr[ip], rm = 1.0 - ipr[ip];
-    T P1 = J11[ip] * sp, P2 = J11[ip] * sm, P3 = J01[ip] * rp, P4 = J01[ip] * rm;
-    T Q1 = J00[ip] * rp, Q2 = J00[ip] * rm, Q3 = J10[ip] * sp, Q4 = J10[ip] * sm;
-    T gx[4] = {P1 - P3, (-P1) - P4, P4 - P2, P2 + P3};
-    T gy[4] = {Q1 - Q3, Q2 + Q3, Q4 - Q2, (-Q1) - Q4};
+    const double sp = 1.0 + ips[ip], sm = 1.0 - ips[ip], rp = 1.0 + ipr[ip], rm = 1.0 - ipr[ip];
+    // gx = [J11 sp - J01 rp, -J11 sp - J01 rm, J01 rm - J11 sm, J11 sm + J01 rp],
+    // gy = [J00 rp - J10 sp, J00 rm + J10 sp, J10 sm - J00 rm, -J00 rp - J10 sm]: one product and one fma each
+    const T P3 = J01[ip] * rp, P4 = J01[ip] * rm, Q1 = J00[ip] * rp, Q2 = J00[ip] * rm;
+    T gx[4] = {fma(J11[ip], sp, -P3), fma(-J11[ip], sp, -P4), fma(-J11[ip], sm, P4), fma(J11[ip], sm, P3)};
+    T gy[4] = {fma(-J10[ip], sp, Q1), fma(J10[ip], sp, Q2), fma(J10[ip], sm, -Q2), fma(-J10[ip], sm, -Q1)};
     T a[4], bq[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {

@@ -185,14 +185,10 @@ __global__ void __launch_bounds__(kPlateLanes* kPlatesPerCta) k_vjp_plate(size_t
   double R[9];
   if (!plate_rotation(X[1], X[2], X[3], abs_tol, R)) set_identity(R);
   const bool ident = is_identity(R);
-  double xlv[4] = {0.0, 0.0, 0.0, 0.0}, ylv[4] = {0.0, 0.0, 0.0, 0.0}, dv[4][3];
+  double xlv[4], ylv[4], dv[4][3];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    sub3(X[i], X[2], dv[i]);
-    if (i == 2) continue;
-    xlv[i] = (R[0] * dv[i][0] + R[1] * dv[i][1]) + R[2] * dv[i][2];
-    ylv[i] = (R[3] * dv[i][0] + R[4] * dv[i][1]) + R[5] * dv[i][2];
-  }
+  for (int i = 0; i < 4; ++i) sub3(X[i], X[2], dv[i]);
+  plate_local_xy(X, R, ident, xlv, ylv);
 
   // 1. Sh = R Ws R^T by 3x3 sub-blocks, Ws from the element's stiffness blocks; lane p fills sub-block row p
   {

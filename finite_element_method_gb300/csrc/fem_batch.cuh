@@ -2,9 +2,9 @@
 // by fem_gpu.cu, whose kernels and handle it reuses).
 //
 // A batch is the disjoint union of assembled models: their nodes, elements,
-// packed scratch, block-sum descriptors and CSR source maps are concatenated
-// once (with node, scratch, slot and entry offsets applied on the device), so
-// one numeric pass over the union assembles every structure -- the result for
+// packed scratch, adjacency records and CSR row starts are concatenated once
+// (with node, scratch, record and entry offsets applied on the device), so one
+// numeric pass over the union assembles every structure -- the result for
 // structure i is the slice [nnz_off[i], nnz_off[i] + nnz[i]) of the union's
 // CSR values, with the model's own row_ptr / col_idx.  Each block's
 // contributions come from one model and keep that model's element order, so
@@ -59,15 +59,17 @@ __global__ void k_add_pack(unsigned long long* a, size_t n, unsigned long long d
     a[i] = top | ((a[i] & ~(3ull << 62)) + d);
   }
 }
-__global__ void k_add_desc(uint2* a, size_t n, uint32_t d) {
+__global__ void k_add_adj(AdjRec* a, size_t n, uint32_t dv) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i < n) a[i].x += d;
+  if (i < n) a[i].voff += dv;
 }
-// model source s: below vs_off_m it is scratch (shift by the model's scratch
-// offset), above it is an S slot (re-based into the union's S)
-__global__ void k_fix_src(uint32_t* a, size_t n, uint32_t vs_off_m, uint32_t v_shift, uint32_t s_base) {
+__global__ void k_add_u32(uint32_t* a, size_t n, uint32_t d) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i < n) a[i] = a[i] < vs_off_m ? a[i] + v_shift : s_base + (a[i] - vs_off_m);
+  if (i < n) a[i] += d;
+}
+__global__ void k_add_i64(int64_t* a, size_t n, int64_t d) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) a[i] += d;
 }
 
 struct BatchConfig {
@@ -75,11 +77,34 @@ struct BatchConfig {
   int block = 128;         // threads per CTA of the plain element launches
   int ctas_per_sm = 2;     // persistent grid = SMs x this
   int tile[3] = {512, 256, 128};  // persistent tile size per kind (truss, beam, plate)
-  int sum_block = 256;     // threads per CTA of the block sums / gather
+  int sum_block = 256;     // kept for the autotuner's table format: the node-row reduction has a fixed shape
+};
+
+// The device arrays one numeric pass of a batch reads and writes: owned by the
+// batch (a union of assembled models) or by its union model (a batch built from
+// host arrays).
+struct BatchData {
+  NodesView nd{};
+  TrussView tv{};
+  BeamView bv{};
+  PlateView pv{};
+  const unsigned long long *pk_t = nullptr, *pk_b = nullptr, *pk_p = nullptr;
+  double* V = nullptr;
+  const AdjRec* adj = nullptr;
+  const uint32_t* adj_begin = nullptr;
+  const int64_t* row_ptr = nullptr;
+  double* values = nullptr;
+  size_t n_rnodes = 0;
 };
 
 struct fem_gpu_batch {
   std::vector<fem_gpu*> models;
+  // a batch built from host arrays: the union model that holds every structure, each structure's node
+  // slots [cap_off[i], cap_off[i] + cap_n[i]) and its row starts relative to its first entry
+  fem_gpu* un = nullptr;
+  std::vector<size_t> cap_off, cap_n;
+  DevBuf<int64_t> row_local;
+  BatchData d;
   cudaStream_t stream = nullptr;
   std::string err;
   int sm_count = 0;
@@ -91,11 +116,11 @@ struct fem_gpu_batch {
   DevBuf<double> t_E, t_A, t_A2, b_E, b_nu, b_A, b_i11, b_i22, b_i12, b_it, b_ks, b_ax, b_ay, b_az, p_E, p_nu, p_t,
       p_ks;
   DevBuf<unsigned long long> pk_t, pk_b, pk_p;
-  DevBuf<uint2> desc;
-  size_t n_desc = 0, n_sums = 0;
+  size_t n_rnodes = 0;       // row nodes of the union's reduction (the models' node capacities)
+  DevBuf<AdjRec> adj;
+  DevBuf<uint32_t> adj_begin;
+  DevBuf<int64_t> row_ptr;   // union row starts (the models' row_ptr shifted by their entry offsets)
   DevBuf<double> V;
-  unsigned long long vs_off = 0;
-  DevBuf<uint32_t> src_map;
   DevBuf<double> values;
   int64_t nnz = 0;
   std::vector<int64_t> nnz_off, nnz_n;
@@ -165,28 +190,24 @@ int batch_build_tiles(fem_gpu_batch* b) {
 int batch_enqueue(fem_gpu_batch* b) {
   cudaStream_t s = b->stream;
   BCK(cudaMemsetAsync(b->flag.p, 0, sizeof(int), s));
-  BlockSink st{nullptr, b->V.p, b->pk_t.p, b->flag.p};
-  BlockSink sb{nullptr, b->V.p, b->pk_b.p, b->flag.p};
-  BlockSink sp{nullptr, b->V.p, b->pk_p.p, b->flag.p};
-  const NodesView nd = b->nodes();
+  const BatchData& d = b->d;
+  BlockSink st{nullptr, d.V, d.pk_t, b->flag.p};
+  BlockSink sb{nullptr, d.V, d.pk_b, b->flag.p};
+  BlockSink sp{nullptr, d.V, d.pk_p, b->flag.p};
   if (b->cfg.persistent) {
     BCK(cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned int), s));
     const unsigned grid = (unsigned)std::max(1, b->sm_count * b->cfg.ctas_per_sm);
-    k_elements_persistent<<<grid, 128, 0, s>>>(nd, b->trusses(), b->beams(), b->plates(), b->rel_tol, b->abs_tol, st,
-                                               sb, sp, b->tiles.p, b->n_tiles, b->counter.p);
+    k_elements_persistent<<<grid, 128, 0, s>>>(d.nd, d.tv, d.bv, d.pv, b->rel_tol, b->abs_tol, st, sb, sp, b->tiles.p,
+                                               b->n_tiles, b->counter.p);
   } else {
     const unsigned bs = (unsigned)b->cfg.block;
-    if (b->np) k_plate<<<grid_for(b->np, bs), bs, 0, s>>>(nd, b->plates(), b->abs_tol, b->np, sp);
-    if (b->nbm) k_beam<<<grid_for(b->nbm, bs), bs, 0, s>>>(nd, b->beams(), b->rel_tol, b->abs_tol, b->nbm, sb);
-    if (b->nt) k_truss<<<grid_for(b->nt, bs), bs, 0, s>>>(nd, b->trusses(), b->abs_tol, b->nt, st);
+    if (b->np) k_plate<<<grid_for(b->np, bs), bs, 0, s>>>(d.nd, d.pv, b->abs_tol, b->np, sp);
+    if (b->nbm) k_beam<<<grid_for(b->nbm, bs), bs, 0, s>>>(d.nd, d.bv, b->rel_tol, b->abs_tol, b->nbm, sb);
+    if (b->nt) k_truss<<<grid_for(b->nt, bs), bs, 0, s>>>(d.nd, d.tv, b->abs_tol, b->nt, st);
   }
-  const unsigned rb = (unsigned)b->cfg.sum_block;
-  if (b->n_desc)
-    k_block_sums<<<grid_for(b->n_desc, rb), rb, 0, s>>>(b->n_desc, b->n_sums, b->desc.p, b->V.p, b->V.p + b->vs_off,
-                                                       b->flag.p);
   if (b->nnz)
-    k_gather_values<<<grid_for(((size_t)b->nnz + kGatherPerThread - 1) / kGatherPerThread, rb), rb, 0, s>>>(
-        (size_t)b->nnz, b->src_map.p, b->V.p, b->vs_off, b->values.p, b->flag.p);
+    k_node_rows<<<grid_for(d.n_rnodes, kRedWarps), kRedWarps * 32, 0, s>>>(d.n_rnodes, d.adj_begin, d.adj, d.row_ptr,
+                                                                           d.V, d.values, b->flag.p);
   BCK(cudaGetLastError());
   return FEM_GPU_OK;
 }
@@ -267,7 +288,7 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
     b->abs_tol = b->models[0]->abs_tol;
   }
   // sizes and offsets
-  size_t nn = 0, nt = 0, nbm = 0, np = 0, nsum = 0, nchk = 0;
+  size_t nn = 0, nt = 0, nbm = 0, np = 0, nr = 0, na = 0;
   unsigned long long vw = 0;
   int64_t nz = 0;
   for (fem_gpu* m : b->models) {
@@ -279,8 +300,8 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
     nt += m->nt;
     nbm += m->nbm;
     np += m->np;
-    nsum += m->s_words;
-    nchk += m->n_desc - m->s_words;
+    nr += m->nodes_number;
+    na += m->n_blocks ? m->n_adj : 0;
     vw += ((unsigned long long)m->v_words + 3ull) & ~3ull;
     b->nnz_off.push_back(nz);
     b->nnz_n.push_back(m->nnz);
@@ -290,12 +311,10 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
   b->nt = nt;
   b->nbm = nbm;
   b->np = np;
-  b->n_sums = nsum;
-  b->n_desc = nsum + nchk;
-  b->vs_off = vw;
+  b->n_rnodes = nr;
   b->nnz = nz;
-  if (b->vs_off + b->n_sums + 4 >= (1ull << 32)) {
-    b->err = "batch too large: more than 2^32 doubles of scratch and sums";
+  if (vw + 4 >= (1ull << 32)) {
+    b->err = "batch too large: more than 2^32 doubles of scratch";
     return FEM_GPU_ERR_ARGUMENT;
   }
   cudaStream_t s = b->stream;
@@ -315,11 +334,12 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
   BCK(b->pk_t.reserve(nt * kPairs2 + 1, s));
   BCK(b->pk_b.reserve(nbm * kPairs2 + 1, s));
   BCK(b->pk_p.reserve(np * kPairs4 + 1, s));
-  BCK(b->desc.reserve(b->n_desc + 1, s));
-  BCK(b->V.reserve(b->vs_off + b->n_sums + 4, s));
-  BCK(b->src_map.reserve((size_t)nz + 8, s));
+  BCK(b->adj.reserve(na + 1, s));
+  BCK(b->adj_begin.reserve(nr + 1, s));
+  BCK(b->row_ptr.reserve(6 * nr + 1, s));
+  BCK(b->V.reserve(vw + 4, s));
   BCK(b->values.reserve((size_t)nz + 8, s));
-  size_t on = 0, ot = 0, ob = 0, op = 0, osum = 0, ochk = nsum;
+  size_t on = 0, ot = 0, ob = 0, op = 0, orn = 0, oa = 0;
   unsigned long long ov = 0;
   int64_t oz = 0;
   for (fem_gpu* m : b->models) {
@@ -365,34 +385,50 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
     BCK(append_d2d(b->pk_p, op * kPairs4, m->off_p, m->np * kPairs4, s));
     if (m->np)
       k_add_pack<<<grid_for(m->np * kPairs4, 256), 256, 0, s>>>(b->pk_p.p + op * kPairs4, m->np * kPairs4, ov);
-    // block-sum descriptors: S slots first (all models), then the check-only ones
-    if (m->s_words) {
-      BCK(cudaMemcpyAsync(b->desc.p + osum, m->slot_desc.p, m->s_words * sizeof(uint2), cudaMemcpyDeviceToDevice, s));
-      k_add_desc<<<grid_for(m->s_words, 256), 256, 0, s>>>(b->desc.p + osum, m->s_words, (uint32_t)ov);
+    // reduction: the model's row nodes, adjacency records and row starts, shifted into the union
+    const size_t rn = m->nodes_number, ma = m->n_blocks ? m->n_adj : 0;
+    if (ma) {
+      BCK(cudaMemcpyAsync(b->adj.p + oa, m->adj.p, ma * sizeof(AdjRec), cudaMemcpyDeviceToDevice, s));
+      k_add_adj<<<grid_for(ma, 256), 256, 0, s>>>(b->adj.p + oa, ma, (uint32_t)ov);
+      BCK(cudaMemcpyAsync(b->adj_begin.p + orn, m->adj_begin.p, rn * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+      k_add_u32<<<grid_for(rn, 256), 256, 0, s>>>(b->adj_begin.p + orn, rn, (uint32_t)oa);
+    } else {
+      BCK(cudaMemsetAsync(b->adj_begin.p + orn, 0, rn * sizeof(uint32_t), s));
+      k_add_u32<<<grid_for(rn, 256), 256, 0, s>>>(b->adj_begin.p + orn, rn, (uint32_t)oa);
     }
-    const size_t nck = m->n_desc - m->s_words;
-    if (nck) {
-      BCK(cudaMemcpyAsync(b->desc.p + ochk, m->slot_desc.p + m->s_words, nck * sizeof(uint2),
-                          cudaMemcpyDeviceToDevice, s));
-      k_add_desc<<<grid_for(nck, 256), 256, 0, s>>>(b->desc.p + ochk, nck, (uint32_t)ov);
-    }
-    // CSR sources
-    if (m->nnz) {
-      BCK(cudaMemcpyAsync(b->src_map.p + oz, m->src_map.p, (size_t)m->nnz * sizeof(uint32_t),
-                          cudaMemcpyDeviceToDevice, s));
-      k_fix_src<<<grid_for((size_t)m->nnz, 256), 256, 0, s>>>(b->src_map.p + oz, (size_t)m->nnz, (uint32_t)m->vs_off,
-                                                              (uint32_t)ov, (uint32_t)(b->vs_off + osum));
-    }
+    BCK(cudaMemcpyAsync(b->row_ptr.p + 6 * orn, m->row_ptr.p, 6 * rn * sizeof(int64_t), cudaMemcpyDeviceToDevice, s));
+    k_add_i64<<<grid_for(6 * rn, 256), 256, 0, s>>>(b->row_ptr.p + 6 * orn, 6 * rn, oz);
     BCK(cudaGetLastError());
     on += m->n_nodes;
     ot += m->nt;
     ob += m->nbm;
     op += m->np;
-    osum += m->s_words;
-    ochk += nck;
+    orn += rn;
+    oa += ma;
     ov += ((unsigned long long)m->v_words + 3ull) & ~3ull;
     oz += m->nnz;
   }
+  {
+    const uint32_t end_a = (uint32_t)oa;
+    const int64_t end_z = oz;
+    BCK(cudaMemcpyAsync(b->adj_begin.p + orn, &end_a, sizeof end_a, cudaMemcpyHostToDevice, s));
+    BCK(cudaMemcpyAsync(b->row_ptr.p + 6 * orn, &end_z, sizeof end_z, cudaMemcpyHostToDevice, s));
+    BCK(cudaStreamSynchronize(s));  // the two host values above are on this stack frame
+  }
+  BatchData& d = b->d;
+  d.nd = b->nodes();
+  d.tv = b->trusses();
+  d.bv = b->beams();
+  d.pv = b->plates();
+  d.pk_t = b->pk_t.p;
+  d.pk_b = b->pk_b.p;
+  d.pk_p = b->pk_p.p;
+  d.V = b->V.p;
+  d.adj = b->adj.p;
+  d.adj_begin = b->adj_begin.p;
+  d.row_ptr = b->row_ptr.p;
+  d.values = b->values.p;
+  d.n_rnodes = b->n_rnodes;
   BCK(cudaStreamSynchronize(s));
   return batch_make_graph(b);
 }
@@ -410,13 +446,16 @@ extern "C" int fem_gpu_batch_destroy(fem_gpu_batch_t* b) {
   b->pk_t.release();
   b->pk_b.release();
   b->pk_p.release();
-  b->desc.release();
-  b->src_map.release();
+  b->adj.release();
+  b->adj_begin.release();
+  b->row_ptr.release();
   b->flag.release();
   b->tiles.release();
   b->counter.release();
+  b->row_local.release();
   for (auto& e : b->ev)
     if (e) cudaEventDestroy(e);
+  if (b->un) fem_gpu_destroy(b->un);
   cudaStream_t s = b->stream;
   delete b;  // the remaining device arrays are freed in the stream's order: the stream goes last
   if (s) cudaStreamDestroy(s);
@@ -447,17 +486,17 @@ extern "C" int fem_gpu_batch_assemble(fem_gpu_batch_t* b) {
 }
 
 extern "C" int fem_gpu_batch_get_values(fem_gpu_batch_t* b, size_t i, double* values) {
-  if (!b || i >= b->models.size() || (!values && b->nnz_n[i])) return FEM_GPU_ERR_ARGUMENT;
+  if (!b || i >= b->nnz_n.size() || (!values && b->nnz_n[i])) return FEM_GPU_ERR_ARGUMENT;
   if (b->nnz_n[i])
-    BCK(cudaMemcpyAsync(values, b->values.p + b->nnz_off[i], (size_t)b->nnz_n[i] * sizeof(double),
+    BCK(cudaMemcpyAsync(values, b->d.values + b->nnz_off[i], (size_t)b->nnz_n[i] * sizeof(double),
                         cudaMemcpyDeviceToHost, b->stream));
   BCK(cudaStreamSynchronize(b->stream));
   return FEM_GPU_OK;
 }
 
 extern "C" int fem_gpu_batch_get_values_device(fem_gpu_batch_t* b, size_t i, const double** values) {
-  if (!b || i >= b->models.size() || !values) return FEM_GPU_ERR_ARGUMENT;
-  *values = b->values.p + b->nnz_off[i];
+  if (!b || i >= b->nnz_n.size() || !values) return FEM_GPU_ERR_ARGUMENT;
+  *values = b->d.values + b->nnz_off[i];
   return FEM_GPU_OK;
 }
 
@@ -520,24 +559,6 @@ extern "C" int fem_gpu_batch_autotune(fem_gpu_batch_t* b, int reps, const char* 
       best_cfg = c;
     }
   }
-  // the reduction's block size, with the best element phase
-  for (int rb : {128, 512}) {
-    BatchConfig c = best_cfg;
-    c.sum_block = rb;
-    b->cfg = c;
-    int st = batch_make_graph(b);
-    if (st) return st;
-    float ms = 0;
-    st = batch_time(b, reps, &ms);
-    if (st) return st;
-    char row[320];
-    snprintf(row, sizeof row, ", {\"config\": %s, \"ms\": %.4f}", config_json(c).c_str(), ms);
-    rows += row;
-    if (ms < best) {
-      best = ms;
-      best_cfg = c;
-    }
-  }
   b->cfg = best_cfg;
   int st = batch_make_graph(b);
   if (st) return st;
@@ -545,7 +566,7 @@ extern "C" int fem_gpu_batch_autotune(fem_gpu_batch_t* b, int reps, const char* 
   snprintf(head, sizeof head,
            "{\"sm_count\": %d, \"structures\": %zu, \"elements\": {\"truss\": %zu, \"beam\": %zu, \"plate\": %zu}, "
            "\"best\": %s, \"best_ms\": %.4f, \"candidates\": [",
-           b->sm_count, b->models.size(), b->nt, b->nbm, b->np, config_json(best_cfg).c_str(), best);
+           b->sm_count, b->nnz_n.size(), b->nt, b->nbm, b->np, config_json(best_cfg).c_str(), best);
   std::string js = std::string(head) + rows + "]}";
   if (cache_path && *cache_path) {
     FILE* f = fopen(cache_path, "w");

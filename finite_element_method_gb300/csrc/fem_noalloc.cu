@@ -12,10 +12,12 @@
 //
 // The working array is sized for kNoallocMaxPairs = 32768 node-pair blocks
 // (3 per truss or beam, 10 per plate: at most 3276 plates or 10922 two-node
-// elements per call); every GPU that loads this library holds it (about
-// 10 MB) until the process exits.  Its device address is looked up once per
-// device, on the first call made with that device current; make that first
-// call before any stream capture.
+// elements per call); it takes about 10 MB on every GPU where the library's
+// device code is loaded, until the process exits.  Under CUDA's default lazy
+// module loading that happens when the library's kernels are first used on a
+// device, not when the library is opened.  Its device address is looked up
+// once per device, on the first call made with that device current; make that
+// first call before any stream capture.
 // All calls on a device share it, and it keeps the last call's contents:
 // calls that overlap on the GPU (different streams, or threads calling at the
 // same time) race on it and must be serialised by the caller.
@@ -31,23 +33,28 @@ using namespace femgpu;
 
 namespace {
 
-constexpr size_t kNoallocMaxPairs = 32768;
+constexpr size_t kNoallocMaxPairs = 32768;          // a power of two (the sort below relies on it)
+constexpr int kPairBits = 15;                         // bits of a block index below kNoallocMaxPairs
+constexpr uint32_t kNoallocMaxNodes = 1u << 24;       // node indices fit 24 bits of a sort key
 // layout of the working array, in 8-byte words:
 //   [0, 36 P)          element node-pair blocks (36 doubles each), element order
 //   [36 P, 37 P)       node-pair key (lo << 32 | hi) per block
-//   [37 P, 37.5 P)     next block with the same key (int32), -1 = none
-//   [37.5 P, 38 P)     1 if the block is the first of its key (int32)
-//   [38 P]             error flag
+//   [37 P, 38 P)       sort keys (lo << 39 | hi << 15 | block), sorted in place
+//   [38 P, 38.5 P)     next block with the same key (int32), -1 = none
+//   [38.5 P, 39 P)     1 if the block is the first of its key (int32)
+//   [39 P]             error flag
 constexpr size_t kWordsV = 36 * kNoallocMaxPairs;
 constexpr size_t kWordsKey = kNoallocMaxPairs;
+constexpr size_t kWordsSort = kNoallocMaxPairs;
 constexpr size_t kWordsLinks = kNoallocMaxPairs;  // next + head, two int32 per word
-constexpr size_t kNoallocWords = kWordsV + kWordsKey + kWordsLinks + 1;
+constexpr size_t kNoallocWords = kWordsV + kWordsKey + kWordsSort + kWordsLinks + 1;
 
 static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoallocWords];
 
 struct Scratch {
   double* V;
   unsigned long long* key;
+  unsigned long long* sort;
   int32_t* next;
   int32_t* head;
   int* flag;
@@ -57,10 +64,11 @@ __host__ __device__ inline Scratch carve(unsigned long long* base) {
   Scratch s;
   s.V = reinterpret_cast<double*>(base);
   s.key = base + kWordsV;
-  int32_t* links = reinterpret_cast<int32_t*>(base + kWordsV + kWordsKey);
+  s.sort = base + kWordsV + kWordsKey;
+  int32_t* links = reinterpret_cast<int32_t*>(base + kWordsV + kWordsKey + kWordsSort);
   s.next = links;
   s.head = links + kNoallocMaxPairs;
-  s.flag = reinterpret_cast<int*>(base + kWordsV + kWordsKey + kWordsLinks);
+  s.flag = reinterpret_cast<int*>(base + kWordsV + kWordsKey + kWordsSort + kWordsLinks);
   return s;
 }
 
@@ -182,13 +190,24 @@ __global__ void k_na_plate(Scratch s, const double* __restrict__ xyz, uint32_t n
   bool ok = true;
 #pragma unroll
   for (int k = 0; k < 4; ++k) ok = ok && !bad_node(nidx[k], n_nodes);
+  // a node used twice would make two of the element's node pairs one block
+  // (the handle path rejects such plates: their nodes lie on a line)
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int l = k + 1; l < 4; ++l) ok = ok && nidx[k] != nidx[l];
   double X[4][3];
   double R[9];
   set_identity(R);
   if (ok) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) get_node(xyz, nidx[k], X[k]);
-    ok = plate_rotation(X[1], X[2], X[3], abs_tol, R);
+    // the geometry checks of the handle path (structs/plate.rs:58-158): nodes on a line,
+    // not on one plane, not convex
+    bool hull_ok = false;
+    ok = !quad_on_line(X[0], X[1], X[2], X[3]) && quad_on_plane(X[0], X[1], X[2], X[3], abs_tol) &&
+         quad_hull_size(X[0], X[1], X[2], X[3], abs_tol, hull_ok) == 4 && hull_ok;
+    if (ok) ok = plate_rotation(X[1], X[2], X[3], abs_tol, R);
   }
   if (!ok) {
     atomicOr(s.flag, 1);
@@ -201,19 +220,12 @@ __global__ void k_na_plate(Scratch s, const double* __restrict__ xyz, uint32_t n
     }
     set_identity(R);
   }
-  double xl[4] = {0.0, 0.0, 0.0, 0.0}, yl[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    if (i == 2) continue;
-    double dd[3];
-    sub3(X[i], X[2], dd);
-    xl[i] = (R[0] * dd[0] + R[1] * dd[1]) + R[2] * dd[2];
-    yl[i] = (R[3] * dd[0] + R[4] * dd[1]) + R[5] * dd[2];
-  }
+  const bool ident = is_identity(R);
+  double xl[4], yl[4];
+  plate_local_xy(X, R, ident, xl, yl);
   const double* p = pr + 4 * e;
   PlateCore C;
   plate_core(xl, yl, p[0], p[1], p[2], p[3], C);
-  bool ident = is_identity(R);
   const int PI[10] = {0, 0, 0, 0, 1, 1, 1, 2, 2, 3};
   const int PJ[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
 #pragma unroll 1
@@ -235,25 +247,50 @@ __global__ void k_na_plate(Scratch s, const double* __restrict__ xyz, uint32_t n
   }
 }
 
+// sort keys: the block's node pair above its index, so that sorting them puts
+// the blocks of one node pair together in element order; padding sorts last
+__global__ void k_na_sort_keys(Scratch s, size_t P, size_t P2) {
+  size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (q >= P2) return;
+  if (q >= P) {
+    s.sort[q] = ~0ull;
+    return;
+  }
+  const unsigned long long k = s.key[q];
+  const unsigned long long lo = k >> 32, hi = k & 0xffffffffull;
+  s.sort[q] = (lo << (24 + kPairBits)) | (hi << kPairBits) | (unsigned long long)q;
+}
+
+// bitonic sort of the P2 (a power of two, <= kNoallocMaxPairs) sort keys by
+// one block of threads; the keys are distinct (they hold the block index)
+__global__ void __launch_bounds__(1024) k_na_sort(Scratch s, size_t P2) {
+  unsigned long long* a = s.sort;
+  for (size_t k = 2; k <= P2; k <<= 1)
+    for (size_t j = k >> 1; j > 0; j >>= 1) {
+      for (size_t i = threadIdx.x; i < P2; i += blockDim.x) {
+        const size_t l = i ^ j;
+        if (l > i) {
+          const unsigned long long x = a[i], y = a[l];
+          if ((x > y) == ((i & k) == 0)) {
+            a[i] = y;
+            a[l] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+}
+
 // next[q]: the following block with the same key; head[q]: q is its key's first block
 __global__ void k_na_links(Scratch s, size_t P) {
-  size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (q >= P) return;
-  unsigned long long k = s.key[q];
-  int32_t nx = -1;
-  for (size_t r = q + 1; r < P; ++r)
-    if (s.key[r] == k) {
-      nx = (int32_t)r;
-      break;
-    }
-  int32_t hd = 1;
-  for (size_t r = 0; r < q; ++r)
-    if (s.key[r] == k) {
-      hd = 0;
-      break;
-    }
-  s.next[q] = nx;
-  s.head[q] = hd;
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  const unsigned long long mask = (1ull << kPairBits) - 1ull;
+  const unsigned long long v = s.sort[i];
+  const int32_t q = (int32_t)(v & mask);
+  const unsigned long long k = v >> kPairBits;
+  s.head[q] = (i == 0 || (s.sort[i - 1] >> kPairBits) != k) ? 1 : 0;
+  s.next[q] = (i + 1 < P && (s.sort[i + 1] >> kPairBits) == k) ? (int32_t)(s.sort[i + 1] & mask) : -1;
 }
 
 __global__ void k_na_zero(double* K, size_t n) {
@@ -310,6 +347,8 @@ extern "C" int fem_gpu_assemble_dense_noalloc(uint32_t n_nodes, const double* xy
   if (n_nodes == 0 || !xyz || !K || (n_truss && (!truss_nodes || !truss_props)) ||
       (n_beam && (!beam_nodes || !beam_props)) || (n_plate && (!plate_nodes || !plate_props)))
     return FEM_GPU_ERR_ARGUMENT;
+  // node indices must fit the sort keys; this also keeps (6 n_nodes)^2 doubles far inside size_t
+  if (n_nodes >= kNoallocMaxNodes) return FEM_GPU_ERR_ARGUMENT;
   if (n_truss > kNoallocMaxPairs || n_beam > kNoallocMaxPairs || n_plate > kNoallocMaxPairs)
     return FEM_GPU_ERR_NOALLOC_LIMIT;
   size_t P = 3 * n_truss + 3 * n_beam + 10 * n_plate;
@@ -319,6 +358,7 @@ extern "C" int fem_gpu_assemble_dense_noalloc(uint32_t n_nodes, const double* xy
   Scratch s = carve(base);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   size_t n_dof = (size_t)6 * n_nodes;
+  (void)cudaGetLastError();  // a launch error reported below is one of this call's
   if (cudaMemsetAsync(s.flag, 0, sizeof(int), st) != cudaSuccess) return FEM_GPU_ERR_CUDA;
   k_na_zero<<<1024, 256, 0, st>>>(K, n_dof * n_dof);
   if (n_truss) k_na_truss<<<grid_of(n_truss, 128), 128, 0, st>>>(s, xyz, n_nodes, truss_nodes, truss_props, n_truss, 0, abs_tol);
@@ -329,6 +369,10 @@ extern "C" int fem_gpu_assemble_dense_noalloc(uint32_t n_nodes, const double* xy
     k_na_plate<<<grid_of(n_plate, 128), 128, 0, st>>>(s, xyz, n_nodes, plate_nodes, plate_props, n_plate,
                                                       3 * n_truss + 3 * n_beam, abs_tol);
   if (P) {
+    size_t P2 = 1;
+    while (P2 < P) P2 <<= 1;
+    k_na_sort_keys<<<grid_of(P2, 256), 256, 0, st>>>(s, P, P2);
+    k_na_sort<<<1, 1024, 0, st>>>(s, P2);
     k_na_links<<<grid_of(P, 256), 256, 0, st>>>(s, P);
     k_na_sum<<<grid_of(P * 36, 288), 288, 0, st>>>(s, P, n_dof, K);
   }

@@ -285,7 +285,7 @@ class FEM:
         return n.value
 
     def pattern_stats(self):
-        """(global node-pair blocks, element node-pair contributions, packed scratch doubles, block-sum slots)."""
+        """(global node-pair blocks, element node-pair contributions, packed scratch doubles, adjacency records)."""
         a, b, c, d = c_int64(0), c_int64(0), c_int64(0), c_int64(0)
         self._check(self._L.fem_gpu_get_pattern_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
                                                       ctypes.byref(d)))
@@ -608,6 +608,127 @@ class Batch:
             self.close()
             raise FEMError(st, msg)
 
+    @classmethod
+    def from_meshes(cls, meshes, rel_tol: float, abs_tol: float, nodes_number=None) -> "Batch":
+        """One batch standing for `FEM(rel_tol, abs_tol, n)` + add_nodes + add_trusses + add_beams +
+        add_plates + assemble per mesh (fem_gpu_batch_create_from_arrays): the checks of every mesh run in
+        bulk on the GPU, one symbolic phase covers all meshes and one graph launch assembles them.
+        `nodes_number` (per mesh) defaults to each mesh's node count.  A failing mesh raises its first
+        failing call's error, the message prefixed by "structure i: "."""
+        self = cls.__new__(cls)
+        self._L = _lib.load()
+        self.models = None
+        S = len(meshes)
+        keep = []
+
+        def arr(a, dt, shape=None):
+            a = np.ascontiguousarray(a, dtype=dt)
+            if shape is not None:
+                a = a.reshape(shape)
+            keep.append(a)
+            return a
+
+        def cat(parts, dt, width=None):
+            parts = [np.asarray(x, dtype=dt).reshape(-1) for x in parts]
+            return arr(np.concatenate(parts) if parts else np.zeros(0, dt), dt)
+
+        def offsets(counts):
+            return arr(np.concatenate([[0], np.cumsum(counts)]), np.uintp)
+
+        for m in meshes:
+            if tuple(k for k in m.order if getattr(m, k) is not None) != tuple(
+                    k for k in ("trusses", "beams", "plates") if getattr(m, k) is not None):
+                raise ValueError("a batch adds each mesh's trusses, then beams, then plates")
+        nn = [m.nodes_number for m in meshes]
+        cap = arr(nn if nodes_number is None else nodes_number, np.uint32)
+        st = _lib.Structures()
+        st.n_structures = S
+        st.nodes_number = ptr(cap, c_uint32)
+        st.node_off = ptr(offsets(nn), ctypes.c_size_t)
+        st.node_numbers = ptr(cat([m.node_numbers for m in meshes], np.uint32), c_uint32)
+        st.xyz = ptr(cat([m.xyz for m in meshes], np.float64), c_double)
+
+        def part(m, kind):
+            d = getattr(m, kind)
+            return d if d is not None and len(d["numbers"]) else None
+
+        def count(m, kind):
+            d = part(m, kind)
+            return 0 if d is None else len(d["numbers"])
+
+        def col(kind, key, width=1, fill=None):
+            out = []
+            for m in meshes:
+                d = part(m, kind)
+                if d is None:
+                    continue
+                v = d.get(key)
+                if v is None:
+                    v = np.full(len(d["numbers"]) * width, fill)
+                out.append(np.broadcast_to(np.asarray(v, np.float64), (len(d["numbers"]),) if width == 1 else
+                                           (len(d["numbers"]), width)).reshape(-1))
+            return cat(out, np.float64)
+
+        if any(count(m, "trusses") for m in meshes):
+            st.truss_off = ptr(offsets([count(m, "trusses") for m in meshes]), ctypes.c_size_t)
+            st.truss_numbers = ptr(cat([part(m, "trusses")["numbers"] for m in meshes if part(m, "trusses")],
+                                       np.uint32), c_uint32)
+            st.truss_nodes = ptr(cat([part(m, "trusses")["nodes"] for m in meshes if part(m, "trusses")], np.uint32),
+                                 c_uint32)
+            st.truss_young = ptr(col("trusses", "young"), c_double)
+            st.truss_area = ptr(col("trusses", "area"), c_double)
+            st.truss_area2 = ptr(col("trusses", "area_2", fill=np.nan), c_double)
+        if any(count(m, "beams") for m in meshes):
+            st.beam_off = ptr(offsets([count(m, "beams") for m in meshes]), ctypes.c_size_t)
+            st.beam_numbers = ptr(cat([part(m, "beams")["numbers"] for m in meshes if part(m, "beams")], np.uint32),
+                                  c_uint32)
+            st.beam_nodes = ptr(cat([part(m, "beams")["nodes"] for m in meshes if part(m, "beams")], np.uint32),
+                                c_uint32)
+            for field, key in (("beam_young", "young"), ("beam_poisson", "poisson"), ("beam_area", "area"),
+                               ("beam_i11", "i11"), ("beam_i22", "i22"), ("beam_i12", "i12"), ("beam_it", "it"),
+                               ("beam_shear_factor", "shear_factor")):
+                setattr(st, field, ptr(col("beams", key), c_double))
+            st.beam_local_axis = ptr(col("beams", "axis", width=3), c_double)
+        if any(count(m, "plates") for m in meshes):
+            st.plate_off = ptr(offsets([count(m, "plates") for m in meshes]), ctypes.c_size_t)
+            st.plate_numbers = ptr(cat([part(m, "plates")["numbers"] for m in meshes if part(m, "plates")],
+                                       np.uint32), c_uint32)
+            st.plate_nodes = ptr(cat([part(m, "plates")["nodes"] for m in meshes if part(m, "plates")], np.uint32),
+                                 c_uint32)
+            for field, key in (("plate_young", "young"), ("plate_poisson", "poisson"),
+                               ("plate_thickness", "thickness"), ("plate_shear_factor", "shear_factor")):
+                setattr(st, field, ptr(col("plates", key), c_double))
+        h = c_void_p()
+        code = self._L.fem_gpu_batch_create_from_arrays(rel_tol, abs_tol, ctypes.byref(st), ctypes.byref(h))
+        self._h = h
+        del keep
+        if code:
+            msg = self._L.fem_gpu_batch_last_error(h).decode() if h else f"status {code}"
+            self.close()
+            raise FEMError(code, msg)
+        return self
+
+    def __len__(self) -> int:
+        n = ctypes.c_size_t(0)
+        self._check(self._L.fem_gpu_batch_size(self._h, ctypes.byref(n)))
+        return n.value
+
+    def csr_sizes(self, i):
+        rows, nnz = c_int64(0), c_int64(0)
+        self._check(self._L.fem_gpu_batch_get_csr_sizes(self._h, i, ctypes.byref(rows), ctypes.byref(nnz)))
+        return rows.value, nnz.value
+
+    def csr(self, i, row_ptr=None, col_idx=None, values=None):
+        """Structure i's CSR (row_ptr, col_idx, values) as its own plain assembly gives it; pass
+        arrays (for instance pinned ones) to receive it in place."""
+        rows, nnz = self.csr_sizes(i)
+        rp = np.zeros(rows + 1, np.int64) if row_ptr is None else row_ptr
+        ci = np.zeros(max(nnz, 1), np.int32) if col_idx is None else col_idx
+        va = np.zeros(max(nnz, 1), np.float64) if values is None else values
+        self._check(self._L.fem_gpu_batch_get_csr(self._h, i, ptr(rp, c_int64), ptr(ci, c_int32),
+                                                  ptr(va, c_double)))
+        return rp, ci[:nnz], va[:nnz]
+
     def close(self):
         h = getattr(self, "_h", None)
         if h:
@@ -631,7 +752,7 @@ class Batch:
         self._check(self._L.fem_gpu_batch_assemble_async(self._h))
 
     def values(self, i):
-        _, nnz = self.models[i].csr_sizes()
+        _, nnz = self.csr_sizes(i)
         out = np.zeros(max(nnz, 1), np.float64)
         self._check(self._L.fem_gpu_batch_get_values(self._h, i, ptr(out, c_double)))
         return out[:nnz]

@@ -157,9 +157,10 @@ int fem_gpu_numeric_launch_count(fem_gpu_t* h, int* n_launches);
 
 /* Sizes of the stored pattern: global node-pair blocks, element node-pair
  * contributions, doubles of packed element-block scratch one numeric pass
- * writes and reads, and packed block-sum slots the CSR values are gathered from. */
+ * writes and reads, and adjacency records (one per row node and adjacent
+ * block, 16 bytes each) the reduction into CSR values reads. */
 int fem_gpu_get_pattern_stats(fem_gpu_t* h, int64_t* n_blocks, int64_t* n_contributions, int64_t* scratch_doubles,
-                              int64_t* sum_slots);
+                              int64_t* adjacency_records);
 
 /* Per-kernel timing of the last numeric pass, measured with CUDA events on the
  * handle's stream (milliseconds): element kernels (all types) and the reduction. */
@@ -202,13 +203,64 @@ int fem_gpu_batch_get_values_device(fem_gpu_batch_t* b, size_t i, const double**
 int fem_gpu_batch_get_stream(fem_gpu_batch_t* b, void** stream);
 /* device time of the last synchronous fem_gpu_batch_assemble (CUDA events), ms */
 int fem_gpu_batch_last_ms(fem_gpu_batch_t* b, float* ms);
-/* Measure the candidate launch configurations (plain element launches of 64,
- * 128 or 256 threads; one persistent launch with 1 or 2 CTAs per SM and four
- * tile-size sets; reduction blocks of 128, 256, 512 threads) with `reps` graph
- * replays each, keep the fastest, write the table as JSON to cache_path (if
- * not NULL) and into summary (if not NULL, at most cap bytes). */
+/* Measure the candidate launch configurations of the element phase (plain
+ * element launches of 64, 128 or 256 threads; one persistent launch with 1 or
+ * 2 CTAs per SM and four tile-size sets) with `reps` graph replays each, keep
+ * the fastest, write the table as JSON to cache_path (if not NULL) and into
+ * summary (if not NULL, at most cap bytes). */
 int fem_gpu_batch_autotune(fem_gpu_batch_t* b, int reps, const char* cache_path, char* summary, size_t cap);
-/* apply a configuration read back from that table */
+/* A batch built from the host arrays of many independent structures, laid
+ * out structure after structure (offset arrays of n_structures + 1 entries
+ * starting at 0; element nodes are node NUMBERS of the element's structure).
+ * It stands for one plain call sequence per structure --
+ * fem_gpu_create(rel_tol, abs_tol, nodes_number[i]), fem_gpu_add_nodes,
+ * fem_gpu_add_trusses, fem_gpu_add_beams, fem_gpu_add_plates, fem_gpu_assemble
+ * -- with every check of those calls run in bulk on the GPU, one symbolic
+ * phase over all structures and one CUDA-graph numeric pass.  On failure the
+ * status and message are those of the structure's first failing call, the
+ * message prefixed by "structure i: ".  Structure i's CSR (fem_gpu_batch_get_csr)
+ * is bit-identical to its plain assembly.  truss_area2 may be NULL (no second
+ * area); a NULL offset array means no element of that kind. */
+typedef struct fem_gpu_structures {
+  size_t n_structures;
+  const uint32_t* nodes_number; /* per structure: the nodes_number of its fem_gpu_create */
+  const size_t* node_off;
+  const uint32_t* node_numbers;
+  const double* xyz; /* 3 per node */
+  const size_t* truss_off;
+  const uint32_t* truss_numbers;
+  const uint32_t* truss_nodes; /* 2 per truss */
+  const double* truss_young;
+  const double* truss_area;
+  const double* truss_area2;
+  const size_t* beam_off;
+  const uint32_t* beam_numbers;
+  const uint32_t* beam_nodes; /* 2 per beam */
+  const double* beam_young;
+  const double* beam_poisson;
+  const double* beam_area;
+  const double* beam_i11;
+  const double* beam_i22;
+  const double* beam_i12;
+  const double* beam_it;
+  const double* beam_shear_factor;
+  const double* beam_local_axis; /* 3 per beam */
+  const size_t* plate_off;
+  const uint32_t* plate_numbers;
+  const uint32_t* plate_nodes; /* 4 per plate */
+  const double* plate_young;
+  const double* plate_poisson;
+  const double* plate_thickness;
+  const double* plate_shear_factor;
+} fem_gpu_structures_t;
+int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, const fem_gpu_structures_t* structures,
+                                     fem_gpu_batch_t** out);
+/* structures (or models) in the batch, and structure i's CSR: sizes, then host copies (any may be NULL) */
+int fem_gpu_batch_size(const fem_gpu_batch_t* b, size_t* n_structures);
+int fem_gpu_batch_get_csr_sizes(fem_gpu_batch_t* b, size_t i, int64_t* n_rows, int64_t* nnz);
+int fem_gpu_batch_get_csr(fem_gpu_batch_t* b, size_t i, int64_t* row_ptr, int32_t* col_idx, double* values);
+/* apply a configuration read back from that table (sum_block, 128, 256 or 512,
+ * is recorded in the table only: the node-row reduction has one shape) */
 int fem_gpu_batch_configure(fem_gpu_batch_t* b, int persistent, int block, int ctas_per_sm, int tile_truss,
                             int tile_beam, int tile_plate, int sum_block);
 
@@ -316,11 +368,15 @@ int fem_gpu_release_cached_memory(void);
  * Elements are taken in the call order trusses, beams, plates, and every
  * entry of K is the sum of its element contributions in that order -- the
  * values fem_gpu_assemble puts in the CSR for the same model, with zeros
- * where the CSR has no entry.  No validation beyond index range and
- * degenerate geometry (FEM_GPU_ERR_ARGUMENT).  Working memory is one fixed
- * device array of 32768 node-pair blocks (3 per truss or beam, 10 per
- * plate; about 10 MB held by every GPU that loads the library): larger
- * structures return FEM_GPU_ERR_NOALLOC_LIMIT.  The array's address is
+ * where the CSR has no entry.  No validation beyond index range, n_nodes
+ * below 2^24, and degenerate geometry -- coincident nodes of a truss or beam;
+ * a plate with a repeated node, nodes on a line, off one plane or not convex
+ * (FEM_GPU_ERR_ARGUMENT).  Working memory is one fixed device array of 32768
+ * node-pair blocks (3 per truss or beam, 10 per plate; about 10 MB on every
+ * GPU where the library's device code is loaded -- with CUDA's default lazy
+ * loading, from the first use of its kernels on that GPU -- until the
+ * process exits): larger structures return FEM_GPU_ERR_NOALLOC_LIMIT.  The
+ * call allocates no device memory.  The array's address is
  * looked up on the first call on each device (make it before any stream
  * capture); all calls share it, so calls that overlap on the GPU race and
  * must be serialised by the caller.  Synchronises `stream` (a cudaStream_t,

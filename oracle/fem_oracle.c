@@ -545,10 +545,11 @@ static void plate_local_matrix(const double xl[4], const double yl[4], double yo
   double Wr[4], Ws[4];
   for (int ip = 0; ip < 4; ++ip) {
     double sp = 1.0 + ips[ip], sm = 1.0 - ips[ip], rp = 1.0 + ipr[ip], rm = 1.0 - ipr[ip];
-    double P1 = J11[ip] * sp, P2 = J11[ip] * sm, P3 = J01[ip] * rp, P4 = J01[ip] * rm;
-    double Q1 = J00[ip] * rp, Q2 = J00[ip] * rm, Q3 = J10[ip] * sp, Q4 = J10[ip] * sm;
-    double gx[4] = {P1 - P3, (-P1) - P4, P4 - P2, P2 + P3};
-    double gy[4] = {Q1 - Q3, Q2 + Q3, Q4 - Q2, (-Q1) - Q4};
+    /* gx = [J11 sp - J01 rp, -J11 sp - J01 rm, J01 rm - J11 sm, J11 sm + J01 rp],
+     * gy = [J00 rp - J10 sp, J00 rm + J10 sp, J10 sm - J00 rm, -J00 rp - J10 sm]: one product and one fma each */
+    double P3 = J01[ip] * rp, P4 = J01[ip] * rm, Q1 = J00[ip] * rp, Q2 = J00[ip] * rm;
+    double gx[4] = {fma(J11[ip], sp, -P3), fma(-J11[ip], sp, -P4), fma(-J11[ip], sm, P4), fma(J11[ip], sm, P3)};
+    double gy[4] = {fma(-J10[ip], sp, Q1), fma(J10[ip], sp, Q2), fma(J10[ip], sm, -Q2), fma(-J10[ip], sm, -Q1)};
     double a[4], bq[4];
     for (int i = 0; i < 4; ++i) {
       a[i] = q[ip] * gx[i];
@@ -753,20 +754,27 @@ int orc_plate_global_matrix(const double x1[3], const double x2[3], const double
   double R[9];
   int st = orc_plate_rotation(x2, x3, x4, rel_tol, abs_tol, R);
   if (st) return st;
-  /* node directions relative to node 3, rotated (quad.rs:340-378) */
+  /* node directions relative to node 3, rotated (quad.rs:340-378): the differences themselves when R is
+   * exactly the identity, else one product and two fused multiply-adds per coordinate */
   const double* X[4] = {x1, x2, x3, x4};
+  const int ident = is_identity(R);
   double xl[4] = {0, 0, 0, 0}, yl[4] = {0, 0, 0, 0};
   for (int i = 0; i < 4; ++i) {
     if (i == 2) continue;
+    if (ident) {
+      xl[i] = X[i][0] - x3[0];
+      yl[i] = X[i][1] - x3[1];
+      continue;
+    }
     double dd[3];
     sub3(X[i], x3, dd);
-    xl[i] = (R[0] * dd[0] + R[1] * dd[1]) + R[2] * dd[2];
-    yl[i] = (R[3] * dd[0] + R[4] * dd[1]) + R[5] * dd[2];
+    xl[i] = fma(R[2], dd[2], fma(R[1], dd[1], R[0] * dd[0]));
+    yl[i] = fma(R[5], dd[2], fma(R[4], dd[1], R[3] * dd[0]));
   }
   double* K = out576;
   memset(K, 0, sizeof(double) * 576);
   plate_local_matrix(xl, yl, young, poisson, thickness, shear_factor, K);
-  if (is_identity(R)) return ORC_OK; /* T^T K T == K bit for bit when T == I */
+  if (ident) return ORC_OK; /* T^T K T == K bit for bit when T == I */
   /* T^T K T with T = diag(R x 8) (plate.rs:726-1002, methods_for_plate_data_handle.rs:109-112),
    * node-pair blocks i <= j, 3x3 sub-blocks, lower triangle mirrored */
   double Kg[576];

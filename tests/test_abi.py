@@ -58,3 +58,16 @@ def test_library_exports_nothing_undeclared():
                          check=True).stdout
     exported = {line.split()[-1] for line in out.splitlines() if line.split() and line.split()[-1].startswith("fem_gpu_")}
     assert exported == declared_symbols()
+
+
+def test_structures_layout_matches_header():
+    """the ctypes mirror of fem_gpu_structures_t lists the header's fields in the header's order"""
+    import sys
+
+    sys.path.insert(0, os.path.join(ROOT, "rust"))
+    import gen_ffi
+
+    (name, fields), = [s for s in gen_ffi.structs() if s[0] == "fem_gpu_structures_t"]
+    assert [f for _, f in fields] == [f for f, _ in _lib.Structures._fields_]
+    sizes = {"size_t": ctypes.sizeof(ctypes.c_size_t)}
+    assert ctypes.sizeof(_lib.Structures) == sum(sizes.get(t, ctypes.sizeof(ctypes.c_void_p)) for t, _ in fields)

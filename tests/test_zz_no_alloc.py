@@ -17,6 +17,7 @@ from finite_element_method_gb300 import FEM, _lib, meshes
 pytestmark = pytest.mark.gpu
 
 REL_TOL = 1e-12
+FEM_GPU_ERR_ARGUMENT = 30
 FEM_GPU_ERR_NOALLOC_LIMIT = 43
 
 
@@ -48,7 +49,7 @@ def dense_from_handle(mesh):
     return K
 
 
-def dense_noalloc(mesh, torch):
+def noalloc_inputs(mesh, torch):
     dev = torch.device("cuda:0")
     t, b, p = mesh.trusses, mesh.beams, mesh.plates
     xyz = torch.tensor(mesh.xyz, dtype=torch.float64, device=dev)
@@ -63,14 +64,22 @@ def dense_noalloc(mesh, torch):
                       dtype=torch.float64, device=dev)
     n = 6 * mesh.nodes_number
     K = torch.full((n, n), float("nan"), dtype=torch.float64, device=dev)  # every entry must be written
-    stream = torch.cuda.current_stream(dev).cuda_stream
-    L = _lib.load()
-    st = L.fem_gpu_assemble_dense_noalloc(mesh.nodes_number, xyz.data_ptr(), len(t["numbers"]), tn.data_ptr(),
-                                          tp.data_ptr(), len(b["numbers"]), bn.data_ptr(), bp.data_ptr(),
-                                          len(p["numbers"]), pn.data_ptr(), pp.data_ptr(), meshes.REL_TOL,
-                                          meshes.ABS_TOL, K.data_ptr(), ctypes.c_void_p(stream))
+    return dict(n_nodes=mesh.nodes_number, xyz=xyz, tn=tn, tp=tp, bn=bn, bp=bp, pn=pn, pp=pp, K=K)
+
+
+def call_noalloc(a, torch):
+    stream = torch.cuda.current_stream(a["K"].device).cuda_stream
+    return _lib.load().fem_gpu_assemble_dense_noalloc(
+        a["n_nodes"], a["xyz"].data_ptr(), a["tn"].shape[0], a["tn"].data_ptr(), a["tp"].data_ptr(),
+        a["bn"].shape[0], a["bn"].data_ptr(), a["bp"].data_ptr(), a["pn"].shape[0], a["pn"].data_ptr(),
+        a["pp"].data_ptr(), meshes.REL_TOL, meshes.ABS_TOL, a["K"].data_ptr(), ctypes.c_void_p(stream))
+
+
+def dense_noalloc(mesh, torch):
+    a = noalloc_inputs(mesh, torch)
+    st = call_noalloc(a, torch)
     assert st == 0, st
-    return K.cpu().numpy()
+    return a["K"].cpu().numpy()
 
 
 def check_equal(Kn, Kh):
@@ -102,3 +111,43 @@ def test_noalloc_rejects_oversized_structure():
     st = L.fem_gpu_assemble_dense_noalloc(4, xyz.data_ptr(), 0, None, None, 0, None, None, 3277, nodes.data_ptr(),
                                           props.data_ptr(), 1e-12, 1e-12, K.data_ptr(), None)
     assert st == FEM_GPU_ERR_NOALLOC_LIMIT
+
+
+def test_noalloc_second_call_allocates_nothing():
+    """The property the entry point exists for: with its inputs and output in
+    place, a call leaves the device's free memory exactly where it was."""
+    torch = pytest.importorskip("torch")
+    mesh = mixed_structure((3, 3, 2), (20, 20), seed=43)
+    a = noalloc_inputs(mesh, torch)
+    assert call_noalloc(a, torch) == 0  # first call on the device: loads the module, looks up the array
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    assert call_noalloc(a, torch) == 0
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
+    check_equal(a["K"].cpu().numpy(), dense_from_handle(mesh))
+
+
+def test_noalloc_rejects_bad_elements_then_recovers():
+    """Out-of-range node index, a zero-length truss, a plate with a repeated
+    node and a plate off its plane each fail with FEM_GPU_ERR_ARGUMENT; a valid call afterwards still
+    matches the handle path (the error flag is cleared per call)."""
+    torch = pytest.importorskip("torch")
+    mesh = mixed_structure((3, 3, 2), (20, 20), seed=44)
+    cases = []
+    a = noalloc_inputs(mesh, torch)
+    a["tn"][1, 1] = mesh.nodes_number  # one past the last node
+    cases.append(a)
+    a = noalloc_inputs(mesh, torch)
+    a["tn"][0, 1] = a["tn"][0, 0]  # both ends on one node: zero length
+    cases.append(a)
+    a = noalloc_inputs(mesh, torch)
+    a["pn"][2, 3] = a["pn"][2, 0]  # plate nodes a, b, c, a
+    cases.append(a)
+    a = noalloc_inputs(mesh, torch)
+    a["xyz"][int(a["pn"][3, 3]), 2] += 1.0  # one node of a plate lifted off the slab: not on one plane
+    cases.append(a)
+    for a in cases:
+        assert call_noalloc(a, torch) == FEM_GPU_ERR_ARGUMENT
+    check_equal(dense_noalloc(mesh, torch), dense_from_handle(mesh))
