@@ -39,13 +39,19 @@ FP64_PEAK_FLOPS = 2 * 152 * 2070e6 * 2
 
 # Algorithmic FP64 work per element of the numeric pass, counted from the kernels' formulation by
 # compiling element_math.cuh with an operation-counting double type (FMA = 2 flops, add/mul/div = 1):
-#   plate, R = I: core 70 add + 169 mul + 176 fma + 2 div, 10 node-pair blocks 56 mul + 154 fma
+#   plate in a global plane (R = I): rotation test and local coordinates 15 add + 6 mul, core 20 add +
+#   145 mul + 208 fma + 2 div, 10 node-pair blocks 20 mul + 154 fma = 932
+#   plate off the global planes (general R): rotation and local coordinates 30 add + 39 mul + 21 fma + 3 div +
+#   3 sqrt, core as above, 10 blocks with their rotation R^T K R on the structural entries 548 mul + 616 fma
+#   = 2480
 #   beam, I12 != 0: 57 add + 213 mul + 201 fma + 19 div + 7 sqrt (trig as polynomial fma chains) = 698;
 #   I12 == 0 (principal axes along the section axes, no arctangent and series): 515 when I11 >= I22, and
 #   714 when I11 < I22 (one turn of the principal-axes loop: arctangent, sine and cosine)
 #   truss: 20 add + 46 mul + 9 fma + 4 div + 4 sqrt
+PLATE_FLOPS = {"flat": (15 + 6) + (20 + 145 + 2 * 208 + 2) + (20 + 2 * 154),
+               "tilted": (30 + 39 + 2 * 21 + 3 + 3) + (20 + 145 + 2 * 208 + 2) + (548 + 2 * 616)}
 WORK = {
-    "plate": dict(elem_flops=70 + 169 + 2 * 176 + 2 + 56 + 2 * 154, pairs=10),
+    "plate": dict(elem_flops=PLATE_FLOPS["flat"], pairs=10),
     "beam": dict(elem_flops=57 + 213 + 2 * 201 + 19 + 7, pairs=3),
     "truss": dict(elem_flops=20 + 46 + 2 * 9 + 4 + 4, pairs=3),
 }
@@ -54,6 +60,8 @@ BEAM_FLOPS = {"general": 698, "aligned": 515, "aligned_turn": 714}
 
 def element_flops(workload, mesh):
     """algorithmic FP64 work of one numeric pass's element kernel over the mesh"""
+    if workload == "plate" and mesh.meta.get("rotation") is not None:
+        return PLATE_FLOPS["tilted"] * mesh.n_elements
     if workload != "beam":
         return WORK[workload]["elem_flops"] * mesh.n_elements
     b = mesh.beams
@@ -139,9 +147,20 @@ class ClockSampler:
                 "reasons": sorted(self.reasons), "samples": len(self.samples)}
 
 
-def make_mesh(workload, nx=1000):
+def tilt_rotation(seed=7):
+    """the seeded orthogonal matrix that takes the plate mesh off the global planes (--tilt)"""
+    q, _ = np.linalg.qr(np.random.default_rng(seed).normal(size=(3, 3)))
+    return q
+
+
+def make_mesh(workload, nx=1000, tilt=False):
     if workload == "plate":
         n = nx
+        if tilt:
+            m = meshes.plate_mesh(n, n, rotation=tilt_rotation())
+            m.meta["rotation"] = "seeded orthogonal Q (numpy PCG64 seed 7)"
+            return m, (f"plate_mesh_{n}x{n} tilted by a seeded orthogonal Q ({n * n:,} 4-node plates off the "
+                       f"global planes, general rotation, {(n + 1) ** 2:,} nodes, 6 DOF/node)")
         return meshes.plate_mesh(n, n), (f"plate_mesh_{n}x{n} ({n * n:,} 4-node plates, {(n + 1) ** 2:,} nodes, "
                                          "6 DOF/node)")
     if workload == "beam":
@@ -202,25 +221,67 @@ def run_reference(args):
 
 
 def run_batch(args):
-    """512 independent structures (log-uniform sizes, mixed kinds): one batched numeric pass (a CUDA graph with
-    the autotuned element phase) against 512 plain per-structure numeric passes on the same GPU."""
+    """512 independent structures (log-uniform sizes in [1e3, 2e5], seeded kind mix).  (a) From host arrays:
+    one plain call sequence per structure (FEM + add_nodes + add_* + assemble) against one batch built from the
+    same arrays (Batch.from_meshes: the checks of every structure in bulk on the GPU, one symbolic phase, one
+    graph-captured numeric pass).  (b) The numeric pass alone: one batched pass (a CUDA graph with the autotuned
+    element phase) against 512 plain per-structure passes.  Returns the result line."""
     import torch
 
     from finite_element_method_gb300 import Batch
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     structures = meshes.batch_structures(n_structures=64 if args.small else 512)
-    models = []
-    t0 = time.perf_counter()
-    for m in structures:
-        g = FEM(meshes.REL_TOL, meshes.ABS_TOL, m.nodes_number)
-        meshes.load(g, m)
-        g.assemble()
-        models.append(g)
-    setup_s = time.perf_counter() - t0
     n_el = sum(m.n_elements for m in structures)
     counts = np.array([m.counts() for m in structures]).sum(0)
-    b = Batch(models)
+    tol = (meshes.REL_TOL, meshes.ABS_TOL)
+
+    def plain_sequences(keep):
+        models = []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for m in structures:
+            g = FEM(*tol, m.nodes_number)
+            meshes.load(g, m)
+            g.assemble()
+            if keep:
+                models.append(g)
+            else:
+                g.close()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, models
+
+    def batch_build():
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b = Batch.from_meshes(structures, *tol)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, b
+
+    # each path once untimed (device memory pool growth, module loading), then timed
+    plain_sequences(False)
+    _, b = batch_build()
+    b.close()
+    reps = max(1, min(3, args.e2e_steps))
+    t_plain = []
+    for _ in range(reps - 1):
+        t_plain.append(plain_sequences(False)[0])
+    t, models = plain_sequences(True)
+    t_plain.append(t)
+    t_batch = []
+    for _ in range(reps - 1):
+        t, b = batch_build()
+        b.close()
+        t_batch.append(t)
+    t, b = batch_build()
+    t_batch.append(t)
+    # identical results
+    for i in (0, len(structures) // 2, len(structures) - 1):
+        rp, ci, va = models[i].stiffness_csr()
+        brp, bci, bva = b.csr(i)
+        assert np.array_equal(rp, brp) and np.array_equal(ci, bci)
+        assert np.array_equal(va.view(np.uint64), bva.view(np.uint64))
+    # (b) numeric passes
     t0 = time.perf_counter()
     table = b.autotune(reps=5, cache_path=os.path.join(ROOT, "finite_element_method_gb300", "lib",
                                                        "batch_autotune.json"))
@@ -241,7 +302,6 @@ def run_batch(args):
             e1.synchronize()
             batch_ms.append(e0.elapsed_time(e1))
     b.assemble()  # checks the patterns
-    # plain: one numeric pass per structure, each on its model's own stream, then a device synchronisation
     plain_ms = []
     for _ in range(args.warmup):
         for g in models:
@@ -255,29 +315,33 @@ def run_batch(args):
             g.assemble_numeric_async()
         torch.cuda.synchronize()
         plain_ms.append((time.perf_counter() - t0) * 1e3)
-    # the plain synchronous API call per structure (assemble: numeric pass + pattern check)
     t0 = time.perf_counter()
     for g in models:
         g.assemble()
     plain_sync_ms = (time.perf_counter() - t0) * 1e3
-    # identical results
-    for i in (0, len(models) // 2, len(models) - 1):
-        assert np.array_equal(b.values(i).view(np.uint64), models[i].stiffness_values().view(np.uint64))
+    for g in models:
+        g.close()
     t_b, t_p = float(np.median(batch_ms)), float(np.median(plain_ms))
+    tp_e2e, tb_e2e = float(np.median(t_plain)), float(np.median(t_batch))
     line = {"metric": "elements/s assembled to FP64 CSR (batched)", "value": n_el / (t_b * 1e-3),
             "unit": "elements/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_b,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"batch of {len(structures)} structures, log-uniform sizes in [1e3, 2e5], "
                        f"{n_el:,} elements (truss {counts[0]:,}, beam {counts[1]:,}, plate {counts[2]:,})",
-                       "l2": "flushed (256 MB write) between steps", "setup_s": setup_s, "autotune_s": tune_s},
-            "batch": {"batched_ms": t_b, "plain_async_ms": t_p, "plain_sync_ms": plain_sync_ms,
-                      "speedup_vs_plain_async": t_p / t_b, "speedup_vs_plain_sync": plain_sync_ms / t_b,
+                       "l2": "flushed (256 MB write) between steps", "autotune_s": tune_s},
+            "batch": {"from_arrays": {"plain_sequences_s": tp_e2e, "batch_s": tb_e2e,
+                                      "speedup": tp_e2e / tb_e2e,
+                                      "what": "host arrays in, every structure's CSR assembled on the device: "
+                                              "FEM + add_nodes + add_* + assemble per structure, against "
+                                              "Batch.from_meshes (median of %d)" % reps},
+                      "numeric": {"batched_ms": t_b, "plain_async_ms": t_p, "plain_sync_ms": plain_sync_ms,
+                                  "speedup_vs_plain_async": t_p / t_b, "speedup_vs_plain_sync": plain_sync_ms / t_b},
                       "autotune_best": table["best"], "autotune_best_ms": table["best_ms"],
                       "autotune_candidates": len(table["candidates"])},
             "gpu_launches": args.steps * ((1 if table["best"]["persistent"] else sum(1 for c in counts if c)) + 2),
             "clocks": clocks.summary()}
-    print(json.dumps(line), flush=True)
     b.close()
+    return line
 
 
 def run_adjoint(args):
@@ -325,7 +389,8 @@ def run_adjoint(args):
                         "accuracy": "tests/test_gpu_vjp.py: central differences (step 1e-6 relative) on 200 "
                                     "parameters of this model and a 50-digit reference derivative"},
             "clocks": clocks.summary()}
-    print(json.dumps(line), flush=True)
+    g.close()
+    return line
 
 
 def run_separate(args):
@@ -580,63 +645,17 @@ def run_results(args):
     g.close()
 
 
-def ptr_u8(a):
-    import ctypes
-
-    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
-
-
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
-    ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="plate", choices=["plate", "beam", "truss", "batch", "adjoint", "separate", "loads", "pcg",
-                                                         "results"])
-    ap.add_argument("--pairs", type=int, default=64, help="(u, lambda) pairs of the adjoint workload")
-    ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--nx", type=int, default=1000, help="plate mesh size (nx x nx); 1000 is the full workload")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--pcg-iters", type=int, default=200, help="PCG iterations per step of the pcg workload")
-    ap.add_argument("--small", action="store_true",
-                    help="profiling-sized batch (64 structures) and adjoint (21x21x5 frame + 200x200 slab) cases")
-    args = ap.parse_args()
-    args.warmup = max(args.warmup, 3)
-    if args.impl == "reference":
-        run_reference(args)
-        return
-    if args.workload == "batch":
-        run_batch(args)
-        return
-    if args.workload == "adjoint":
-        run_adjoint(args)
-        return
-    if args.workload == "separate":
-        run_separate(args)
-        return
-    if args.workload == "loads":
-        run_loads(args)
-        return
-    if args.workload == "results":
-        run_results(args)
-        return
-    if args.workload == "pcg":
-        run_pcg(args)
-        return
-
+def run_numeric(args):
+    """The numeric pass of the plate, beam or truss workload (the line's value), its roofline, the CPU
+    baseline and the e2e drop-in sequence.  Returns the result line."""
     import torch
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
 
-        dist.init_process_group("nccl")
-
-    mesh, desc = make_mesh(args.workload, args.nx)
+    mesh, desc = make_mesh(args.workload, args.nx, args.tilt)
     n_el = mesh.n_elements
     fem = FEM(meshes.REL_TOL, meshes.ABS_TOL, mesh.nodes_number)
     t0 = time.perf_counter()
@@ -677,12 +696,12 @@ def main():
     # roofline of the dominant kernel
     hbm_gbs, peak_src = measured_peaks()
     w = WORK[args.workload]
-    n_blocks, n_contrib, scratch, n_adj = fem.pattern_stats()
+    n_blocks, n_contrib, scratch, sum_slots = fem.pattern_stats()
     # element kernels: inputs + per-contribution offset and mask (16 B) + packed blocks written to scratch
     elem_bytes = n_el * IN_BYTES[args.workload] + n_contrib * 16 + scratch * 8
-    # reduction: packed scratch read once, one 16-byte adjacency record per (row node, adjacent block), per
-    # node its first record (4 B) and six row starts (48 B), the CSR values (8 B) written once
-    red_bytes = scratch * 8 + n_adj * 16 + mesh.nodes_number * (4 + 48) + nnz * 8
+    # reduction: packed scratch read once; per block-sum slot an 8-byte descriptor read and the sum written
+    # and gathered once; the CSR source map (4 B) read and the CSR values (8 B) written once
+    red_bytes = scratch * 8 + 3 * sum_slots * 8 + nnz * (4 + 8)
     t_e, t_r = float(np.mean(elem_ms)), float(np.mean(red_ms))
     kern = {"element": dict(ms=t_e, bytes=elem_bytes, flops=element_flops(args.workload, mesh)),
             "reduce": dict(ms=t_r, bytes=red_bytes, flops=scratch)}  # <= one FP64 add per packed entry
@@ -696,7 +715,7 @@ def main():
                 "frac": frac_fp64}
     else:
         roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_gbs, "unit": "GB/s", "frac": frac_hbm}
-    traffic = TRAFFIC_PER_ELEMENT.get(args.workload) if dom == "element" else None
+    traffic = TRAFFIC_PER_ELEMENT.get(args.workload) if dom == "element" and not args.tilt else None
     roof.update({"kernel": dom, "traffic": None if traffic is None else int(traffic * n_el),
                  "traffic_source": "ncu DRAM bytes of k_plate on the 500 x 500 mesh, scaled per plate"
                  if traffic is not None else None,
@@ -783,11 +802,107 @@ def main():
                        "between steps", "parallelism": f"replicas x{world}", "setup_s": setup_s},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks.summary()}
+    fem.close()
+    return line
+
+
+
+
+def ptr_u8(a):
+    import ctypes
+
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="plate", choices=["plate", "beam", "truss", "batch", "adjoint", "separate", "loads", "pcg",
+                                                         "results"])
+    ap.add_argument("--pairs", type=int, default=64, help="(u, lambda) pairs of the adjoint workload")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--tilt", action="store_true",
+                    help="plate workload: the mesh tilted off the global planes (general rotation path)")
+    ap.add_argument("--nx", type=int, default=1000, help="plate mesh size (nx x nx); 1000 is the full workload")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-aux", action="store_true",
+                    help="default workload: skip the beam frame, batch and adjoint results appended as aux")
+    ap.add_argument("--pcg-iters", type=int, default=200, help="PCG iterations per step of the pcg workload")
+    ap.add_argument("--small", action="store_true",
+                    help="profiling-sized batch (64 structures) and adjoint (21x21x5 frame + 200x200 slab) cases")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    if args.workload == "batch":
+        print(json.dumps(run_batch(args)), flush=True)
+        return
+    if args.workload == "adjoint":
+        print(json.dumps(run_adjoint(args)), flush=True)
+        return
+    if args.workload == "separate":
+        run_separate(args)
+        return
+    if args.workload == "loads":
+        run_loads(args)
+        return
+    if args.workload == "results":
+        run_results(args)
+        return
+    if args.workload == "pcg":
+        run_pcg(args)
+        return
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    line = run_numeric(args)
+    if args.workload == "plate" and not args.no_aux and world == 1 and not args.tilt:
+        line["aux"] = aux_results(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
-    fem.close()
+
+
+def aux_results(args):
+    """Compact results of the other configurations, measured in the same run: the beam frame's numeric pass
+    (value, roofline), the batch of 512 structures (from host arrays and the numeric pass alone, against
+    plain per-structure calls) and the adjoint vjp's cost against the forward pass; each with its clocks."""
+    import copy
+
+    out = {}
+    a = copy.copy(args)
+    a.workload, a.e2e_steps, a.no_cpu, a.small = "beam", 0, True, False
+    beam = run_numeric(a)
+    out["beam_frame"] = {"workload": beam["config"]["workload"], "value": beam["value"], "unit": beam["unit"],
+                         "ms_per_step": beam["ms_per_step"],
+                         "roofline": {k: beam["roofline"][k] for k in ("bound", "achieved", "peak", "unit", "frac",
+                                                                       "kernel")},
+                         "clocks": beam["clocks"]}
+    a = copy.copy(args)
+    a.e2e_steps = 2
+    batch = run_batch(a)
+    out["batch"] = {"workload": batch["config"]["workload"], "value": batch["value"], "unit": batch["unit"],
+                    "from_arrays": batch["batch"]["from_arrays"], "numeric": batch["batch"]["numeric"],
+                    "clocks": batch["clocks"]}
+    adj = run_adjoint(copy.copy(args))
+    out["adjoint"] = {"workload": adj["config"]["workload"], "vjp_ms": adj["adjoint"]["vjp_ms"],
+                      "forward_numeric_ms": adj["adjoint"]["forward_numeric_ms"],
+                      "vjp_over_forward": adj["adjoint"]["vjp_over_forward"],
+                      "vjp_per_pair_over_forward": adj["adjoint"]["vjp_per_pair_over_forward"],
+                      "clocks": adj["clocks"]}
+    return out
 
 
 if __name__ == "__main__":

@@ -579,7 +579,7 @@ __device__ __forceinline__ void plate_local_xy(const T X[4][3], const T R[9], bo
 template <class T>
 struct PlateCoreT {
   T Sxx[10], Syy[10], Sxy[16];  // upper-triangle index for Sxx/Syy
-  T cmq, cbq, gam, nu;
+  T tb, gam, nu;  // tb = t^2 / 12: bending over membrane stiffness (the S sums carry the membrane factor)
   T F12[3], G12[3], F43[3];
   T E12[3], E43[3];
   T P14[6], P23[6], P1423[9];  // upper-triangle index for P14/P23
@@ -630,6 +630,16 @@ __device__ __forceinline__ void plate_core(const T xl[4], const T yl[4], T young
   }
 #pragma unroll
   for (int k = 0; k < 16; ++k) C.Sxy[k] = 0.0;
+  // material (plate.rs:532-548, :580-597, :629-636), one reciprocal: cm/16 = E t / (16 (1 - nu^2)) scales the
+  // membrane sums through the integration-point weights; bending is (t^2 / 12) times membrane; shear c_s/64
+  T dinv = 1.0 / (1.0 - poisson * poisson);
+  T Et = young * thickness;
+  const T cmq = (Et * dinv) * 0.0625;
+  C.tb = (thickness * thickness) * 0x1.5555555555555p-4;
+  T omn = 1.0 - poisson;
+  T cq = ((Et * shear_factor) * omn) * (dinv * 0x1p-7);
+  C.gam = omn * 0.5;
+  C.nu = poisson;
   T Wr[4], Ws[4];
 #pragma unroll
   for (int ip = 0; ip < 4; ++ip) {
@@ -639,11 +649,12 @@ __device__ __forceinline__ void plate_core(const T xl[4], const T yl[4], T young
     const T P3 = J01[ip] * rp, P4 = J01[ip] * rm, Q1 = J00[ip] * rp, Q2 = J00[ip] * rm;
     T gx[4] = {fma(J11[ip], sp, -P3), fma(-J11[ip], sp, -P4), fma(-J11[ip], sm, P4), fma(J11[ip], sm, P3)};
     T gy[4] = {fma(-J10[ip], sp, Q1), fma(J10[ip], sp, Q2), fma(J10[ip], sm, -Q2), fma(-J10[ip], sm, -Q1)};
+    const T qm = cmq * q[ip];
     T a[4], bq[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      a[i] = q[ip] * gx[i];
-      bq[i] = q[ip] * gy[i];
+      a[i] = qm * gx[i];
+      bq[i] = qm * gy[i];
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -659,14 +670,6 @@ __device__ __forceinline__ void plate_core(const T xl[4], const T yl[4], T young
     Wr[ip] = fma(J11[ip], J11[ip], J10[ip] * J10[ip]) * q[ip];
     Ws[ip] = fma(J01[ip], J01[ip], J00[ip] * J00[ip]) * q[ip];
   }
-  T dinv = 1.0 / (1.0 - poisson * poisson);
-  T Et = young * thickness;
-  C.cmq = (Et * dinv) * 0.0625;
-  C.cbq = ((C.cmq * thickness) * thickness) * 0x1.5555555555555p-4;
-  T omn = 1.0 - poisson;
-  T cq = ((Et * shear_factor) * omn) * (dinv * 0x1p-7);
-  C.gam = omn * 0.5;
-  C.nu = poisson;
   const double al2 = al * al, be2 = be * be, ab = al * be;
   T W0p = Wr[0] + Wr[1], W0m = Wr[2] + Wr[3];
   T W1p = Ws[0] + Ws[3], W1m = Ws[1] + Ws[2];
@@ -713,11 +716,10 @@ __device__ __forceinline__ void plate_local_block(const PlateCoreT<T>& C, int i,
   T tvv = fma(C.gam, Sxx, Syy);
   T tuv_ij = fma(C.gam, C.Sxy[4 * j + i], C.nu * C.Sxy[4 * i + j]);
   T tuv_ji = fma(C.gam, C.Sxy[4 * i + j], C.nu * C.Sxy[4 * j + i]);
-  blk[0] = C.cmq * tuu;
-  blk[7] = C.cmq * tvv;
-  T uv = C.cmq * tuv_ij;
-  blk[1] = uv;
-  blk[6] = (i == j) ? uv : C.cmq * tuv_ji;
+  blk[0] = tuu;
+  blk[7] = tvv;
+  blk[1] = tuv_ij;
+  blk[6] = (i == j) ? tuv_ij : tuv_ji;
   const int g0i = i < 2 ? 0 : 1, g0j = j < 2 ? 0 : 1;
   const T s0i = (i == 1 || i == 2) ? -1.0 : 1.0, s0j = (j == 1 || j == 2) ? -1.0 : 1.0;
   const int g1i = (i == 0 || i == 3) ? 0 : 1, g1j = (j == 0 || j == 3) ? 0 : 1;
@@ -745,10 +747,10 @@ __device__ __forceinline__ void plate_local_block(const PlateCoreT<T>& C, int i,
       T sh = fma(f, e, t1);
       T v = sh;
       if (a >= 1 && b >= 1) {
-        if (a == 2 && b == 2) v = fma(C.cbq, tuu, sh);
-        else if (a == 1 && b == 1) v = fma(C.cbq, tvv, sh);
-        else if (a == 2 && b == 1) v = fma(-C.cbq, tuv_ij, sh);
-        else v = fma(-C.cbq, tuv_ji, sh);
+        if (a == 2 && b == 2) v = fma(C.tb, tuu, sh);
+        else if (a == 1 && b == 1) v = fma(C.tb, tvv, sh);
+        else if (a == 2 && b == 1) v = fma(-C.tb, tuv_ij, sh);
+        else v = fma(-C.tb, tuv_ji, sh);
       }
       blk[6 * (2 + a) + 2 + b] = v;
       if (i == j) blk[6 * (2 + b) + 2 + a] = v;
@@ -774,11 +776,10 @@ __device__ __forceinline__ void plate_block_ct(const PlateCoreT<T>& C, T blk[36]
   const T tvv = fma(C.gam, Sxx, Syy);
   const T tuv_ij = fma(C.gam, C.Sxy[4 * J + I], C.nu * C.Sxy[4 * I + J]);
   const T tuv_ji = fma(C.gam, C.Sxy[4 * I + J], C.nu * C.Sxy[4 * J + I]);
-  blk[0] = C.cmq * tuu;
-  blk[7] = C.cmq * tvv;
-  const T uv = C.cmq * tuv_ij;
-  blk[1] = uv;
-  blk[6] = (I == J) ? uv : C.cmq * tuv_ji;
+  blk[0] = tuu;
+  blk[7] = tvv;
+  blk[1] = tuv_ij;
+  blk[6] = (I == J) ? tuv_ij : tuv_ji;
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -802,10 +803,10 @@ __device__ __forceinline__ void plate_block_ct(const PlateCoreT<T>& C, T blk[36]
       const T sh = fma(f, e, t1);
       T v = sh;
       if (a >= 1 && b >= 1) {
-        if (a == 2 && b == 2) v = fma(C.cbq, tuu, sh);
-        else if (a == 1 && b == 1) v = fma(C.cbq, tvv, sh);
-        else if (a == 2 && b == 1) v = fma(-C.cbq, tuv_ij, sh);
-        else v = fma(-C.cbq, tuv_ji, sh);
+        if (a == 2 && b == 2) v = fma(C.tb, tuu, sh);
+        else if (a == 1 && b == 1) v = fma(C.tb, tvv, sh);
+        else if (a == 2 && b == 1) v = fma(-C.tb, tuv_ij, sh);
+        else v = fma(-C.tb, tuv_ji, sh);
       }
       blk[6 * (2 + a) + 2 + b] = v;
       if (I == J) blk[6 * (2 + b) + 2 + a] = v;
@@ -833,6 +834,83 @@ __device__ __forceinline__ void plate_rotate_block(const T R[9], bool diag, cons
         for (int b = 0; b < 3; ++b) {
           out[6 * (3 * p + a) + 3 * q + b] = o[3 * a + b];
           if (diag) out[6 * (3 * q + b) + 3 * p + a] = o[3 * a + b];
+        }
+    }
+}
+
+// R^T M R of one 3x3 sub-block whose zero entries are known at compile time
+// (NZ: 9-bit row-major mask of the entries that can be non-zero): the same
+// fma chains as rt_m_r with the terms of structural zeros left out.  Leaving out
+// a term 0 * x of a chain changes no non-zero result (x + (+-0) = x), only the
+// sign of a result that is zero, and zeros are never stored.
+template <unsigned NZ, bool SYM, class T>
+__device__ __forceinline__ void rt_m_r_sparse(const T R[9], const T M[9], T out[9]) {
+  T Y[9];
+  bool yrow[3] = {false, false, false};  // row k of Y = M R can be non-zero
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      bool started = false;
+      T acc = 0.0;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        if (!((NZ >> (3 * k + j)) & 1u)) continue;
+        acc = started ? fma(M[3 * k + j], R[3 * j + b], acc) : M[3 * k + j] * R[3 * j + b];
+        started = true;
+      }
+      Y[3 * k + b] = acc;
+      yrow[k] = yrow[k] || started;
+    }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      if (SYM && b < a) continue;
+      bool started = false;
+      T acc = 0.0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (!yrow[k]) continue;
+        acc = started ? fma(R[3 * k + a], Y[3 * k + b], acc) : R[3 * k + a] * Y[3 * k + b];
+        started = true;
+      }
+      out[3 * a + b] = acc;
+      if (SYM) out[3 * b + a] = acc;
+    }
+}
+
+// plate_rotate_block for the blocks plate_block_ct builds: in the local block
+// only the membrane u-v entries, w-w, the w-thx-thy coupling, thx-thy and (on
+// diagonal blocks) thz-thz can be non-zero, so each 3x3 sub-block of R^T K R
+// takes only those terms.  Non-zero results are bit-identical to
+// plate_rotate_block's.
+template <bool DIAG, class T>
+__device__ __forceinline__ void plate_rotate_block_ct(const T R[9], const T blk[36], T out[36]) {
+  constexpr unsigned kNz00 = 0x11Bu;                  // (u,u) (u,v) (v,u) (v,v) (w,w)
+  constexpr unsigned kNz01 = 0x0C0u;                  // (w,thx) (w,thy)
+  constexpr unsigned kNz10 = 0x024u;                  // (thx,w) (thy,w)
+  constexpr unsigned kNz11 = DIAG ? 0x11Bu : 0x01Bu;  // thx-thy 2x2, thz-thz on diagonal blocks
+  T M[9], o[9];
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (DIAG && p == 1 && q == 0) continue;
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) M[3 * a + b] = blk[6 * (3 * p + a) + 3 * q + b];
+      if (p == 0 && q == 0) rt_m_r_sparse<kNz00, DIAG>(R, M, o);
+      else if (p == 0) rt_m_r_sparse<kNz01, false>(R, M, o);
+      else if (q == 0) rt_m_r_sparse<kNz10, false>(R, M, o);
+      else rt_m_r_sparse<kNz11, DIAG>(R, M, o);
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          out[6 * (3 * p + a) + 3 * q + b] = o[3 * a + b];
+          if (DIAG) out[6 * (3 * q + b) + 3 * p + a] = o[3 * a + b];
         }
     }
 }

@@ -2,9 +2,9 @@
 // by fem_gpu.cu, whose kernels and handle it reuses).
 //
 // A batch is the disjoint union of assembled models: their nodes, elements,
-// packed scratch, adjacency records and CSR row starts are concatenated once
-// (with node, scratch, record and entry offsets applied on the device), so one
-// numeric pass over the union assembles every structure -- the result for
+// packed scratch, block-sum descriptors and CSR source maps are concatenated
+// once (with node, scratch, slot and entry offsets applied on the device), so
+// one numeric pass over the union assembles every structure -- the result for
 // structure i is the slice [nnz_off[i], nnz_off[i] + nnz[i]) of the union's
 // CSR values, with the model's own row_ptr / col_idx.  Each block's
 // contributions come from one model and keep that model's element order, so
@@ -59,17 +59,15 @@ __global__ void k_add_pack(unsigned long long* a, size_t n, unsigned long long d
     a[i] = top | ((a[i] & ~(3ull << 62)) + d);
   }
 }
-__global__ void k_add_adj(AdjRec* a, size_t n, uint32_t dv) {
+__global__ void k_add_desc(uint2* a, size_t n, uint32_t d) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i < n) a[i].voff += dv;
+  if (i < n) a[i].x += d;
 }
-__global__ void k_add_u32(uint32_t* a, size_t n, uint32_t d) {
+// model source s: below vs_off_m it is scratch (shift by the model's scratch
+// offset), above it is an S slot (re-based into the union's S)
+__global__ void k_fix_src(uint32_t* a, size_t n, uint32_t vs_off_m, uint32_t v_shift, uint32_t s_base) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i < n) a[i] += d;
-}
-__global__ void k_add_i64(int64_t* a, size_t n, int64_t d) {
-  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i < n) a[i] += d;
+  if (i < n) a[i] = a[i] < vs_off_m ? a[i] + v_shift : s_base + (a[i] - vs_off_m);
 }
 
 struct BatchConfig {
@@ -77,7 +75,7 @@ struct BatchConfig {
   int block = 128;         // threads per CTA of the plain element launches
   int ctas_per_sm = 2;     // persistent grid = SMs x this
   int tile[3] = {512, 256, 128};  // persistent tile size per kind (truss, beam, plate)
-  int sum_block = 256;     // kept for the autotuner's table format: the node-row reduction has a fixed shape
+  int sum_block = 256;     // threads per CTA of the block sums / gather
 };
 
 // The device arrays one numeric pass of a batch reads and writes: owned by the
@@ -90,11 +88,11 @@ struct BatchData {
   PlateView pv{};
   const unsigned long long *pk_t = nullptr, *pk_b = nullptr, *pk_p = nullptr;
   double* V = nullptr;
-  const AdjRec* adj = nullptr;
-  const uint32_t* adj_begin = nullptr;
-  const int64_t* row_ptr = nullptr;
+  const uint2* desc = nullptr;      // block-sum descriptors (sums first, then the check-only ones)
+  size_t n_desc = 0, n_sums = 0;
+  unsigned long long vs_off = 0;    // S starts here in V
+  const uint32_t* src_map = nullptr;
   double* values = nullptr;
-  size_t n_rnodes = 0;
 };
 
 struct fem_gpu_batch {
@@ -116,11 +114,11 @@ struct fem_gpu_batch {
   DevBuf<double> t_E, t_A, t_A2, b_E, b_nu, b_A, b_i11, b_i22, b_i12, b_it, b_ks, b_ax, b_ay, b_az, p_E, p_nu, p_t,
       p_ks;
   DevBuf<unsigned long long> pk_t, pk_b, pk_p;
-  size_t n_rnodes = 0;       // row nodes of the union's reduction (the models' node capacities)
-  DevBuf<AdjRec> adj;
-  DevBuf<uint32_t> adj_begin;
-  DevBuf<int64_t> row_ptr;   // union row starts (the models' row_ptr shifted by their entry offsets)
+  DevBuf<uint2> desc;
+  size_t n_desc = 0, n_sums = 0;
   DevBuf<double> V;
+  unsigned long long vs_off = 0;
+  DevBuf<uint32_t> src_map;
   DevBuf<double> values;
   int64_t nnz = 0;
   std::vector<int64_t> nnz_off, nnz_n;
@@ -205,9 +203,12 @@ int batch_enqueue(fem_gpu_batch* b) {
     if (b->nbm) k_beam<<<grid_for(b->nbm, bs), bs, 0, s>>>(d.nd, d.bv, b->rel_tol, b->abs_tol, b->nbm, sb);
     if (b->nt) k_truss<<<grid_for(b->nt, bs), bs, 0, s>>>(d.nd, d.tv, b->abs_tol, b->nt, st);
   }
+  const unsigned rb = (unsigned)b->cfg.sum_block;
+  if (d.n_desc)
+    k_block_sums<<<grid_for(d.n_desc, rb), rb, 0, s>>>(d.n_desc, d.n_sums, d.desc, d.V, d.V + d.vs_off, b->flag.p);
   if (b->nnz)
-    k_node_rows<<<grid_for(d.n_rnodes, kRedWarps), kRedWarps * 32, 0, s>>>(d.n_rnodes, d.adj_begin, d.adj, d.row_ptr,
-                                                                           d.V, d.values, b->flag.p);
+    k_gather_values<<<grid_for(((size_t)b->nnz + kGatherPerThread - 1) / kGatherPerThread, rb), rb, 0, s>>>(
+        (size_t)b->nnz, d.src_map, d.V, d.vs_off, d.values, b->flag.p);
   BCK(cudaGetLastError());
   return FEM_GPU_OK;
 }
@@ -288,7 +289,7 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
     b->abs_tol = b->models[0]->abs_tol;
   }
   // sizes and offsets
-  size_t nn = 0, nt = 0, nbm = 0, np = 0, nr = 0, na = 0;
+  size_t nn = 0, nt = 0, nbm = 0, np = 0, nsum = 0, nchk = 0;
   unsigned long long vw = 0;
   int64_t nz = 0;
   for (fem_gpu* m : b->models) {
@@ -300,8 +301,8 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
     nt += m->nt;
     nbm += m->nbm;
     np += m->np;
-    nr += m->nodes_number;
-    na += m->n_blocks ? m->n_adj : 0;
+    nsum += m->s_words;
+    nchk += m->n_desc - m->s_words;
     vw += ((unsigned long long)m->v_words + 3ull) & ~3ull;
     b->nnz_off.push_back(nz);
     b->nnz_n.push_back(m->nnz);
@@ -311,10 +312,12 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
   b->nt = nt;
   b->nbm = nbm;
   b->np = np;
-  b->n_rnodes = nr;
+  b->n_sums = nsum;
+  b->n_desc = nsum + nchk;
+  b->vs_off = vw;
   b->nnz = nz;
-  if (vw + 4 >= (1ull << 32)) {
-    b->err = "batch too large: more than 2^32 doubles of scratch";
+  if (b->vs_off + b->n_sums + 4 >= (1ull << 32)) {
+    b->err = "batch too large: more than 2^32 doubles of scratch and sums";
     return FEM_GPU_ERR_ARGUMENT;
   }
   cudaStream_t s = b->stream;
@@ -334,12 +337,11 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
   BCK(b->pk_t.reserve(nt * kPairs2 + 1, s));
   BCK(b->pk_b.reserve(nbm * kPairs2 + 1, s));
   BCK(b->pk_p.reserve(np * kPairs4 + 1, s));
-  BCK(b->adj.reserve(na + 1, s));
-  BCK(b->adj_begin.reserve(nr + 1, s));
-  BCK(b->row_ptr.reserve(6 * nr + 1, s));
-  BCK(b->V.reserve(vw + 4, s));
+  BCK(b->desc.reserve(b->n_desc + 1, s));
+  BCK(b->V.reserve(b->vs_off + b->n_sums + 4, s));
+  BCK(b->src_map.reserve((size_t)nz + 8, s));
   BCK(b->values.reserve((size_t)nz + 8, s));
-  size_t on = 0, ot = 0, ob = 0, op = 0, orn = 0, oa = 0;
+  size_t on = 0, ot = 0, ob = 0, op = 0, osum = 0, ochk = nsum;
   unsigned long long ov = 0;
   int64_t oz = 0;
   for (fem_gpu* m : b->models) {
@@ -385,36 +387,35 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
     BCK(append_d2d(b->pk_p, op * kPairs4, m->off_p, m->np * kPairs4, s));
     if (m->np)
       k_add_pack<<<grid_for(m->np * kPairs4, 256), 256, 0, s>>>(b->pk_p.p + op * kPairs4, m->np * kPairs4, ov);
-    // reduction: the model's row nodes, adjacency records and row starts, shifted into the union
-    const size_t rn = m->nodes_number, ma = m->n_blocks ? m->n_adj : 0;
-    if (ma) {
-      BCK(cudaMemcpyAsync(b->adj.p + oa, m->adj.p, ma * sizeof(AdjRec), cudaMemcpyDeviceToDevice, s));
-      k_add_adj<<<grid_for(ma, 256), 256, 0, s>>>(b->adj.p + oa, ma, (uint32_t)ov);
-      BCK(cudaMemcpyAsync(b->adj_begin.p + orn, m->adj_begin.p, rn * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
-      k_add_u32<<<grid_for(rn, 256), 256, 0, s>>>(b->adj_begin.p + orn, rn, (uint32_t)oa);
-    } else {
-      BCK(cudaMemsetAsync(b->adj_begin.p + orn, 0, rn * sizeof(uint32_t), s));
-      k_add_u32<<<grid_for(rn, 256), 256, 0, s>>>(b->adj_begin.p + orn, rn, (uint32_t)oa);
+    // block-sum descriptors: S slots first (all models), then the check-only ones
+    if (m->s_words) {
+      BCK(cudaMemcpyAsync(b->desc.p + osum, m->slot_desc.p, m->s_words * sizeof(uint2), cudaMemcpyDeviceToDevice, s));
+      k_add_desc<<<grid_for(m->s_words, 256), 256, 0, s>>>(b->desc.p + osum, m->s_words, (uint32_t)ov);
     }
-    BCK(cudaMemcpyAsync(b->row_ptr.p + 6 * orn, m->row_ptr.p, 6 * rn * sizeof(int64_t), cudaMemcpyDeviceToDevice, s));
-    k_add_i64<<<grid_for(6 * rn, 256), 256, 0, s>>>(b->row_ptr.p + 6 * orn, 6 * rn, oz);
+    const size_t nck = m->n_desc - m->s_words;
+    if (nck) {
+      BCK(cudaMemcpyAsync(b->desc.p + ochk, m->slot_desc.p + m->s_words, nck * sizeof(uint2),
+                          cudaMemcpyDeviceToDevice, s));
+      k_add_desc<<<grid_for(nck, 256), 256, 0, s>>>(b->desc.p + ochk, nck, (uint32_t)ov);
+    }
+    // CSR sources
+    if (m->nnz) {
+      BCK(cudaMemcpyAsync(b->src_map.p + oz, m->src_map.p, (size_t)m->nnz * sizeof(uint32_t),
+                          cudaMemcpyDeviceToDevice, s));
+      k_fix_src<<<grid_for((size_t)m->nnz, 256), 256, 0, s>>>(b->src_map.p + oz, (size_t)m->nnz, (uint32_t)m->vs_off,
+                                                              (uint32_t)ov, (uint32_t)(b->vs_off + osum));
+    }
     BCK(cudaGetLastError());
     on += m->n_nodes;
     ot += m->nt;
     ob += m->nbm;
     op += m->np;
-    orn += rn;
-    oa += ma;
+    osum += m->s_words;
+    ochk += nck;
     ov += ((unsigned long long)m->v_words + 3ull) & ~3ull;
     oz += m->nnz;
   }
-  {
-    const uint32_t end_a = (uint32_t)oa;
-    const int64_t end_z = oz;
-    BCK(cudaMemcpyAsync(b->adj_begin.p + orn, &end_a, sizeof end_a, cudaMemcpyHostToDevice, s));
-    BCK(cudaMemcpyAsync(b->row_ptr.p + 6 * orn, &end_z, sizeof end_z, cudaMemcpyHostToDevice, s));
-    BCK(cudaStreamSynchronize(s));  // the two host values above are on this stack frame
-  }
+  BCK(cudaStreamSynchronize(s));
   BatchData& d = b->d;
   d.nd = b->nodes();
   d.tv = b->trusses();
@@ -424,11 +425,12 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
   d.pk_b = b->pk_b.p;
   d.pk_p = b->pk_p.p;
   d.V = b->V.p;
-  d.adj = b->adj.p;
-  d.adj_begin = b->adj_begin.p;
-  d.row_ptr = b->row_ptr.p;
+  d.desc = b->desc.p;
+  d.n_desc = b->n_desc;
+  d.n_sums = b->n_sums;
+  d.vs_off = b->vs_off;
+  d.src_map = b->src_map.p;
   d.values = b->values.p;
-  d.n_rnodes = b->n_rnodes;
   BCK(cudaStreamSynchronize(s));
   return batch_make_graph(b);
 }
@@ -446,9 +448,8 @@ extern "C" int fem_gpu_batch_destroy(fem_gpu_batch_t* b) {
   b->pk_t.release();
   b->pk_b.release();
   b->pk_p.release();
-  b->adj.release();
-  b->adj_begin.release();
-  b->row_ptr.release();
+  b->desc.release();
+  b->src_map.release();
   b->flag.release();
   b->tiles.release();
   b->counter.release();
@@ -553,6 +554,24 @@ extern "C" int fem_gpu_batch_autotune(fem_gpu_batch_t* b, int reps, const char* 
     if (st) return st;
     char row[320];
     snprintf(row, sizeof row, "%s{\"config\": %s, \"ms\": %.4f}", k ? ", " : "", config_json(c).c_str(), ms);
+    rows += row;
+    if (ms < best) {
+      best = ms;
+      best_cfg = c;
+    }
+  }
+  // the reduction's block size, with the best element phase
+  for (int rb : {128, 512}) {
+    BatchConfig c = best_cfg;
+    c.sum_block = rb;
+    b->cfg = c;
+    int st = batch_make_graph(b);
+    if (st) return st;
+    float ms = 0;
+    st = batch_time(b, reps, &ms);
+    if (st) return st;
+    char row[320];
+    snprintf(row, sizeof row, ", {\"config\": %s, \"ms\": %.4f}", config_json(c).c_str(), ms);
     rows += row;
     if (ms < best) {
       best = ms;

@@ -18,7 +18,7 @@
 //     stiffness rows [6 cap_off[i], 6 cap_off[i + 1]);
 //   * one symbolic phase builds the union's pattern, and the numeric pass of
 //     every structure is one CUDA-graph launch (persistent or plain element
-//     launches, as the autotuner picks, then the node-row reduction).
+//     launches, as the autotuner picks, then the block sums and the gather).
 //
 // Node-pair blocks never span structures and each structure keeps its call
 // order (its trusses, then its beams, then its plates, each in input order), so
@@ -547,11 +547,12 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
   d.pk_b = h->off_b.p;
   d.pk_p = h->off_p.p;
   d.V = h->V.p;
-  d.adj = h->adj.p;
-  d.adj_begin = h->adj_begin.p;
-  d.row_ptr = h->row_ptr.p;
+  d.desc = h->slot_desc.p;
+  d.n_desc = h->n_desc;
+  d.n_sums = h->s_words;
+  d.vs_off = h->vs_off;
+  d.src_map = h->src_map.p;
   d.values = h->values.p;
-  d.n_rnodes = NS;
   return batch_make_graph(b);
 }
 

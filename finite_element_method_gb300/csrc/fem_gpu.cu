@@ -469,7 +469,7 @@ __device__ __forceinline__ void plate_pair(const PlateCore& C, const double R[9]
   plate_block_ct<I, J>(C, blk);
   if (!ident) {
     double o[36];
-    plate_rotate_block(R, I == J, blk, o);
+    plate_rotate_block_ct<I == J>(R, blk, o);
 #pragma unroll
     for (int k = 0; k < 36; ++k) blk[k] = o[k];
   }
@@ -620,12 +620,12 @@ __global__ void k_row_counts(size_t n_nodes, const int32_t* __restrict__ seg_beg
 // ---------------------------------------------------------------------------
 // compacted scratch layout
 // ---------------------------------------------------------------------------
-// Block b stores count_b contributions of c_b doubles each (c_b = 13, 14 or
-// 36 by its packing), contiguous and in element order, at blk_voff[b] (an
-// exclusive scan of count_b * c_b).
+// Block b stores count_b contributions of c_b = popcount(mask_b) doubles each,
+// contiguous and in element order, at blk_voff[b] (an exclusive scan of
+// count_b * c_b).
 __global__ void k_block_sizes(size_t nb, const uint32_t* __restrict__ blk_count, const uint64_t* __restrict__ blk_mask,
                               const int32_t* __restrict__ blk_I, const int32_t* __restrict__ blk_J, uint8_t* blk_lay,
-                              unsigned long long* sizes) {
+                              uint64_t* blk_pmask, unsigned long long* sizes) {
   size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (b >= nb) return;
   const uint64_t m = blk_mask[b];
@@ -636,6 +636,11 @@ __global__ void k_block_sizes(size_t nb, const uint32_t* __restrict__ blk_count,
     lay = kLayOff13;
   }
   blk_lay[b] = (uint8_t)lay;
+  // the pattern over packed positions: bit j set when packed entry j is a pattern entry
+  uint64_t pm = 0;
+  for (int j = 0; j < lay_size(lay); ++j)
+    if ((m >> c_lay_en[lay][j]) & 1ull) pm |= 1ull << j;
+  blk_pmask[b] = pm;
   sizes[b] = (unsigned long long)blk_count[b] * (unsigned long long)lay_size(lay);
 }
 
@@ -658,9 +663,38 @@ __global__ void k_pair_offsets(const uint32_t* __restrict__ svals, const uint32_
 }
 
 // ---------------------------------------------------------------------------
-// kernel: deterministic node-row reduction into CSR
+// kernel: deterministic block reduction into CSR
 // ---------------------------------------------------------------------------
 constexpr int kFlagPattern = 1;                      // bit of *flag: the exact-zero pattern changed
+
+// Block-sum slots.  A packed entry of a block with one contribution needs no
+// sum: its CSR value is gathered straight from the scratch.  Entries of blocks
+// with 2, 3, 4 and 5+ contributions get a slot in S, grouped by that count so a
+// warp adds the same number of terms on every lane (on GB300 the FP64 adds of
+// the reduction are themselves a throughput limit).  Blocks with one
+// contribution keep a check-only descriptor for each packed entry outside the
+// pattern (to see the exact-zero pattern change).  Categories: 0 = one
+// contribution, 1..4 = 2, 3, 4, 5+ contributions.
+constexpr int kSlotCats = 5;
+__host__ __device__ __forceinline__ int slot_cat(uint32_t count) { return count <= 1 ? 0 : count >= 5 ? 4 : (int)count - 1; }
+
+__global__ void k_slot_sizes(size_t nb, const uint32_t* __restrict__ blk_count, const uint64_t* __restrict__ blk_pmask,
+                             const uint8_t* __restrict__ blk_lay, unsigned long long* sz /* kSlotCats x (nb + 1) */) {
+  size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const int c = lay_size(blk_lay[b]);
+  const int cat = slot_cat(blk_count[b]);
+#pragma unroll
+  for (int g = 0; g < kSlotCats; ++g) sz[(size_t)g * (nb + 1) + b] = 0;
+  sz[(size_t)cat * (nb + 1) + b] = cat == 0 ? (unsigned long long)(c - __popcll(blk_pmask[b])) : (unsigned long long)c;
+}
+
+struct SlotLayout {
+  const unsigned long long* base;  // kSlotCats x (nb + 1): per category, exclusive scan over blocks
+  size_t stride;                   // nb + 1
+  unsigned long long off[kSlotCats];  // first descriptor of each category (category 0 last)
+  unsigned long long vs_off;          // S starts at this scratch position
+};
 
 // position of a block entry in its packing (-1: not packed)
 // (the packed entries are listed in ascending entry order, so the position is the number of set entries below)
@@ -688,15 +722,20 @@ __device__ __forceinline__ int seg_inclusive_sum(int v) {
 // Lane k takes the k-th block of the node's adjacency (blocks in column-node
 // order, kRowLanes at a time); for each of the node's 6 rows a prefix sum of the
 // blocks' entry counts gives every lane the place of its entries, which it
-// writes in column order: column and stiffness group.  A block stored with the
-// row node second (t = 1) is read transposed.  The node's groups are placed the
-// same way.
+// writes in column order: column, stiffness group and value source (the
+// scratch position of a block with one contribution, else the entry's
+// block-sum slot in S -- both in one buffer, S starting at vs_off).  A block
+// stored with the row node second (t = 1) is read transposed.  The node's
+// groups are placed the same way.
 __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin, const int32_t* __restrict__ seg_end,
                            const uint64_t* __restrict__ akeys, int kb, const uint32_t* __restrict__ avals,
                            const uint64_t* __restrict__ blk_mask, const uint64_t* __restrict__ blk_maskT,
+                           const uint8_t* __restrict__ blk_lay, const uint32_t* __restrict__ blk_count,
+                           const unsigned long long* __restrict__ blk_voff, SlotLayout L,
                            const int64_t* __restrict__ row_ptr, const int64_t* __restrict__ gbase,
-                           int32_t* __restrict__ col_idx, int32_t* __restrict__ nnz_group, int32_t* __restrict__ g_row,
-                           int32_t* __restrict__ g_col, uint8_t* __restrict__ g_kind) {
+                           int32_t* __restrict__ col_idx, int32_t* __restrict__ nnz_group,
+                           uint32_t* __restrict__ src_map, int32_t* __restrict__ g_row, int32_t* __restrict__ g_col,
+                           uint8_t* __restrict__ g_kind) {
   const size_t r = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) / kRowLanes;
   const int lane = (int)(threadIdx.x & (kRowLanes - 1));
   // every lane stays for the shuffles: a node past the end or without blocks has an empty range
@@ -715,12 +754,17 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
   for (int32_t k0 = s; __any_sync(0xffffffffu, k0 < e); k0 += kRowLanes) {
     const int32_t k = k0 + lane;
     uint64_t m = 0;
-    uint32_t J = 0;
+    uint32_t J = 0, lay = 0, t = 0;
+    unsigned long long sb = 0;
     if (k < e) {
       const uint32_t v = avals[k];
       const uint32_t b = v >> 1;
+      t = v & 1u;
       J = (uint32_t)(akeys[k] & ((1ull << kb) - 1ull));
-      m = (v & 1u) ? blk_maskT[b] : blk_mask[b];
+      m = t ? blk_maskT[b] : blk_mask[b];
+      lay = blk_lay[b];
+      const int cat = slot_cat(blk_count[b]);
+      sb = cat == 0 ? blk_voff[b] : L.vs_off + L.off[cat] + L.base[(size_t)cat * L.stride + b];
     }
     // groups
     const uint32_t km = kinds_of(m);
@@ -752,6 +796,7 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
         if (rowbits & (1u << c)) {
           col_idx[pos] = (int32_t)(6 * J + c);
           nnz_group[pos] = kg[2 * (a / 3) + c / 3];
+          src_map[pos] = (uint32_t)(sb + (unsigned long long)packed_pos(lay, t ? 6 * c + a : 6 * a + c));
           ++pos;
         }
       next[a] += __shfl_sync(0xffffffffu, inc, kRowLanes - 1, kRowLanes);
@@ -759,180 +804,123 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
   }
 }
 
-// One record per (row node, adjacent block), in (row node, column node) order:
-// where the block's contributions start in the scratch, how many there are, how
-// they are packed, and the block's non-zero mask as the row node sees it
-// (transposed when the row node is the block's higher node).
-struct __align__(16) AdjRec {
-  uint32_t voff;  // scratch position of the block's first contribution
-  uint32_t meta;  // contributions (bits 0-23) | packing (bits 24-25) | transposed (bit 26)
-  uint64_t mask;  // 36-bit non-zero mask in the row node's orientation
-};
-static_assert(sizeof(AdjRec) == 16, "an adjacency record is one 16-byte load");
-
-// Symbolic, once per pattern: the adjacency records and each node's record count.
-__global__ void k_adj_records(size_t na, const uint64_t* __restrict__ akeys, int kb, const uint32_t* __restrict__ avals,
-                              const uint32_t* __restrict__ blk_count, const uint8_t* __restrict__ blk_lay,
-                              const unsigned long long* __restrict__ blk_voff, const uint64_t* __restrict__ blk_mask,
-                              const uint64_t* __restrict__ blk_maskT, AdjRec* __restrict__ adj,
-                              uint32_t* __restrict__ node_n) {
-  const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (k >= na) return;
-  const uint32_t v = avals[k], b = v >> 1, t = v & 1u;
-  AdjRec rec;
-  rec.voff = (uint32_t)blk_voff[b];
-  rec.meta = (blk_count[b] & 0xffffffu) | ((uint32_t)blk_lay[b] << 24) | (t << 26);
-  rec.mask = t ? blk_maskT[b] : blk_mask[b];
-  adj[k] = rec;
-  atomicAdd(&node_n[akeys[k] >> kb], 1u);
-}
-
-// Symbolic checks of the limits of the packed layout: a block's contribution
-// count fits 24 bits (bit 0 of *flag), a node's six rows hold fewer than
-// kRedMaxNodeEntries entries (bit 1).
-__global__ void k_slot_checks(size_t nb, const uint32_t* __restrict__ blk_count, int* flag) {
+// Symbolic, once per pattern: the descriptors -- the scratch position of the
+// first contribution, the number of contributions (bits 0-23), the packed
+// block size, i.e. the stride between contributions (bits 24-30), and whether
+// the entry is a pattern entry (bit 31).
+__global__ void k_slot_desc(size_t nb, const uint32_t* __restrict__ blk_count, const uint64_t* __restrict__ blk_pmask,
+                            const uint8_t* __restrict__ blk_lay, const unsigned long long* __restrict__ blk_voff,
+                            SlotLayout L, uint2* desc, int* too_many) {
   const size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (b < nb && blk_count[b] >= (1u << 24)) atomicOr(flag, 1);
-}
-constexpr int kRedWarps = 8;                       // warps per CTA, one row node per warp at a time
-constexpr int kRedChunk = 16;                      // adjacent blocks taken per round
-constexpr int kRedStage = 512;                     // doubles of scratch staged in shared memory per warp
-constexpr int kRedOut = kRedChunk * 36;            // outputs of one round at most
-constexpr uint32_t kRedMaxNodeEntries = 1u << 22;  // CSR entries in a node's six rows (positions use 22 bits)
-
-__global__ void k_node_sizes(size_t n_nodes, const int64_t* __restrict__ row_ptr, int* flag) {
-  const size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (r < n_nodes && row_ptr[6 * r + 6] - row_ptr[6 * r] >= (int64_t)kRedMaxNodeEntries) atomicOr(flag, 2);
-}
-
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
-__device__ __forceinline__ uint32_t warp_inclusive_sum(uint32_t v) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const uint32_t u = __shfl_up_sync(0xffffffffu, v, d);
-    if (lane >= d) v += u;
+  if (b >= nb) return;
+  const int c = lay_size(blk_lay[b]);
+  const uint32_t cnt = blk_count[b];
+  if (cnt >= (1u << 24)) atomicOr(too_many, 1);
+  const uint64_t pm = blk_pmask[b];
+  const int cat = slot_cat(cnt);
+  const unsigned long long voff = blk_voff[b];
+  const uint32_t hi = (cnt & 0xffffffu) | ((uint32_t)c << 24);
+  if (cat == 0) {
+    // one contribution: pattern entries are gathered straight from the scratch; the others get a check
+    unsigned long long at = L.off[0] + L.base[b];
+    for (int j = 0; j < c; ++j)
+      if (!((pm >> j) & 1ull)) desc[at++] = make_uint2((uint32_t)(voff + (unsigned long long)j), hi);
+  } else {
+    const unsigned long long at = L.off[cat] + L.base[(size_t)cat * L.stride + b];
+    for (int j = 0; j < c; ++j)
+      desc[at + j] = make_uint2((uint32_t)(voff + (unsigned long long)j), hi | ((uint32_t)((pm >> j) & 1ull) << 31));
   }
-  return v;
 }
 
-// Numeric pass, part 2: the CSR values of every row node, one warp per node.
-// The node's adjacent blocks are taken kRedChunk at a time in column order:
-// their contributions (contiguous per block, element order) are copied into
-// shared memory with asynchronous 8-byte copies while the block lanes list
-// the round's outputs in CSR order -- for row a, block by block, column by
-// column: (position in the node's rows, block, packed position).  Then every
-// output sums its block's contributions left to right (element call order,
-// as the reference's accumulation) and is written in place; a node's outputs
-// are consecutive, so the stores are coalesced.  An off-diagonal block is read
-// by both of its nodes, the second time mostly from L2.  No atomics on values.
-// A pattern entry whose contributions are all zero, or a packed entry outside
-// the pattern with a non-zero contribution, raises kFlagPattern (the exact-zero
-// pattern changed); the second test runs once per block, from its lower node.
-__global__ void __launch_bounds__(kRedWarps * 32) k_node_rows(size_t n_nodes, const uint32_t* __restrict__ adj_begin,
-                                                              const AdjRec* __restrict__ adj,
-                                                              const int64_t* __restrict__ row_ptr,
-                                                              const double* __restrict__ V, double* __restrict__ values,
-                                                              int* flag) {
-  __shared__ double s_stage[kRedWarps][kRedStage];
-  __shared__ uint32_t s_out[kRedWarps][kRedOut];
-  __shared__ const double* s_src[kRedWarps][kRedChunk];
-  __shared__ uint32_t s_meta[kRedWarps][kRedChunk];
-  const unsigned full = 0xffffffffu;
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const size_t r = (size_t)blockIdx.x * kRedWarps + w;
-  if (r >= n_nodes) return;  // uniform over the warp
-  const uint32_t b0 = adj_begin[r], b1 = adj_begin[r + 1];
-  if (b0 == b1) return;
-  const int64_t rs0 = row_ptr[6 * r];
-  const uint32_t my_start = lane < 6 ? (uint32_t)(row_ptr[6 * r + lane] - rs0) : 0u;
-  uint32_t rowoff[6] = {0, 0, 0, 0, 0, 0};  // entries of each row written by earlier rounds
-  bool bad = false;
-  for (uint32_t c0 = b0; c0 < b1; c0 += kRedChunk) {
-    const uint32_t nk = min((uint32_t)kRedChunk, b1 - c0);
-    const bool mine = (uint32_t)lane < nk;
-    uint4 raw = make_uint4(0u, 0u, 0u, 0u);
-    if (mine) raw = reinterpret_cast<const uint4*>(adj)[c0 + lane];
-    const uint32_t voff = raw.x, meta = raw.y;
-    const uint64_t mask = ((uint64_t)raw.w << 32) | raw.z;
-    const uint32_t cnt = meta & 0xffffffu, lay = (meta >> 24) & 3u, tr = (meta >> 26) & 1u;
-    const uint32_t csz = mine ? (uint32_t)lay_size(lay) : 0u;
-    const uint32_t sz = cnt * csz;
-    // the round's blocks are staged in order while they fit; a larger one is read from global memory
-    const uint32_t incl = warp_inclusive_sum(sz);
-    const bool staged = mine && incl <= (uint32_t)kRedStage;
-    const uint32_t soff = incl - sz;
-    unsigned todo = __ballot_sync(full, staged);
-    while (todo) {
-      const int k = __ffs(todo) - 1;
-      todo &= todo - 1;
-      const uint32_t n = __shfl_sync(full, sz, k), o = __shfl_sync(full, soff, k), v = __shfl_sync(full, voff, k);
-      for (uint32_t i = lane; i < n; i += 32) cp_async8(&s_stage[w][o + i], V + v + i);
+// Numeric pass, part 1: one thread per descriptor.  Slots in S (descriptors
+// below n_sums) sum their contributions in element order (left to right, as
+// the reference's call-order accumulation): descriptors are grouped by
+// contribution count, so every lane of a warp adds the same number of terms.
+// Check-only descriptors (one contribution, outside the pattern) only test
+// their entry.  No atomics on values.  A non-pattern entry with a non-zero, or
+// a pattern slot whose contributions are all zero, raises kFlagPattern (the
+// exact-zero pattern changed).
+__global__ void __launch_bounds__(512) k_block_sums(size_t n_desc, size_t n_sums, const uint2* __restrict__ desc,
+                                                    const double* __restrict__ V, double* __restrict__ S, int* flag) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n_desc) return;
+  const uint2 d = desc[i];
+  const uint32_t n = d.y & 0xffffffu, stride = (d.y >> 24) & 0x7fu;
+  const bool inpat = (d.y >> 31) != 0;
+  const double* src = V + d.x;
+  bool nz;
+  double sum;
+  switch (n) {
+    case 1:
+      if (nonzero(src[0])) atomicOr(flag, kFlagPattern);
+      return;
+    case 2: {
+      const double a = src[0], b = src[stride];
+      nz = nonzero(a) | nonzero(b);
+      sum = a + b;
+      break;
     }
-    if (mine) {
-      s_src[w][lane] = staged ? &s_stage[w][soff] : V + voff;
-      s_meta[w][lane] = meta;
+    case 3: {
+      const double a = src[0], b = src[stride], c = src[2 * stride];
+      nz = nonzero(a) | nonzero(b) | nonzero(c);
+      sum = (a + b) + c;
+      break;
     }
-    // the round's outputs in CSR order
-    uint32_t n_out = 0;
-#pragma unroll
-    for (int a = 0; a < 6; ++a) {
-      const uint32_t bits = mine ? (uint32_t)((mask >> (6 * a)) & 63ull) : 0u;
-      const uint32_t c = __popc(bits);
-      const uint32_t inc = warp_inclusive_sum(c);
-      const uint32_t tot = __shfl_sync(full, inc, 31);
-      uint32_t pos = __shfl_sync(full, my_start, a) + rowoff[a] + inc - c;
-      uint32_t o = n_out + inc - c;
-      uint32_t bb = bits;
-      while (bb) {
-        const int cc = __ffs(bb) - 1;
-        bb &= bb - 1;
-        const int en = tr ? 6 * cc + a : 6 * a + cc;
-        s_out[w][o++] = (pos++ << 10) | ((uint32_t)lane << 6) | (uint32_t)packed_pos(lay, en);
-      }
-      rowoff[a] += tot;
-      n_out += tot;
+    case 4: {
+      const double a = src[0], b = src[stride], c = src[2 * stride], e = src[3 * stride];
+      nz = nonzero(a) | nonzero(b) | nonzero(c) | nonzero(e);
+      sum = ((a + b) + c) + e;
+      break;
     }
-    cp_async_wait_all();
-    __syncwarp();
-    for (uint32_t o = lane; o < n_out; o += 32) {
-      const uint32_t d = s_out[w][o];
-      const uint32_t k = (d >> 6) & (kRedChunk - 1), p = d & 63u;
-      const double* src = s_src[w][k];
-      const uint32_t m = s_meta[w][k];
-      const uint32_t n = m & 0xffffffu, stride = (uint32_t)lay_size((m >> 24) & 3u);
-      double sum = src[p];
-      bool nz = nonzero(sum);
-      for (uint32_t j = 1; j < n; ++j) {
-        const double x = src[(size_t)j * stride + p];
+    default: {
+      sum = src[0];
+      nz = nonzero(sum);
+      for (uint32_t k = 1; k < n; ++k) {
+        const double x = src[(size_t)k * stride];
         nz |= nonzero(x);
         sum = sum + x;
       }
-      values[rs0 + (d >> 10)] = sum;
-      bad |= !nz;
     }
-    // packed entries outside the pattern, once per block (from its lower node: not transposed)
-    unsigned chk = __ballot_sync(full, mine && !tr && (uint32_t)__popcll(mask) < csz);
-    while (chk) {
-      const int k = __ffs(chk) - 1;
-      chk &= chk - 1;
-      const uint64_t mk = __shfl_sync(full, mask, k);
-      const uint32_t lk = __shfl_sync(full, lay, k), nk_ = __shfl_sync(full, cnt, k);
-      const uint32_t st = (uint32_t)lay_size(lk);
-      const double* src = s_src[w][k];
-      for (uint32_t p = lane; p < st; p += 32) {
-        if ((mk >> c_lay_en[lk][p]) & 1ull) continue;
-        for (uint32_t j = 0; j < nk_; ++j) bad |= nonzero(src[(size_t)j * st + p]);
-      }
-    }
-    __syncwarp();  // the next round reuses the stage and the output list
   }
-  if (__any_sync(full, bad) && lane == 0) atomicOr(flag, kFlagPattern);
+  if (i < n_sums) S[i] = sum;
+  if (nz != inpat) atomicOr(flag, kFlagPattern);
+}
+
+// Numeric pass, part 2: CSR values in storage order, each read from its source
+// (the scratch for one-contribution entries, S otherwise; S starts at vs_off of
+// the same buffer); eight consecutive entries per thread so their loads
+// overlap.  A one-contribution pattern entry that reads zero raises kFlagPattern.
+constexpr int kGatherPerThread = 8;
+__global__ void __launch_bounds__(512) k_gather_values(size_t nnz, const uint32_t* __restrict__ src_map,
+                                                       const double* __restrict__ VS, unsigned long long vs_off,
+                                                       double* __restrict__ values, int* flag) {
+  const size_t k0 = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) * kGatherPerThread;
+  if (k0 >= nnz) return;
+  bool zero_direct = false;
+  if (k0 + kGatherPerThread <= nnz) {
+    // src_map and values are 256-byte aligned and k0 % 8 == 0
+    const uint4 s0 = reinterpret_cast<const uint4*>(src_map + k0)[0];
+    const uint4 s1 = reinterpret_cast<const uint4*>(src_map + k0)[1];
+    const uint32_t sx[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+    double a[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] = VS[sx[q]];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) zero_direct |= sx[q] < vs_off && !nonzero(a[q]);
+    double2* out = reinterpret_cast<double2*>(values + k0);
+    out[0] = make_double2(a[0], a[1]);
+    out[1] = make_double2(a[2], a[3]);
+    out[2] = make_double2(a[4], a[5]);
+    out[3] = make_double2(a[6], a[7]);
+  } else {
+    for (size_t k = k0; k < nnz; ++k) {
+      const uint32_t sx = src_map[k];
+      const double v = VS[sx];
+      zero_direct |= sx < vs_off && !nonzero(v);
+      values[k] = v;
+    }
+  }
+  if (zero_direct) atomicOr(flag, kFlagPattern);
 }
 
 // ---------------------------------------------------------------------------
@@ -1437,9 +1425,14 @@ struct fem_gpu {
   DevBuf<uint64_t> mask_t, mask_b, mask_p;
   DevBuf<unsigned long long> off_t, off_b, off_p, blk_voff;  // packed offsets (offset | packing << 62)
   DevBuf<uint8_t> blk_lay;
-  size_t n_adj = 0;                  // adjacency records (row node, adjacent block)
-  DevBuf<AdjRec> adj;                // per record: scratch position, count, packing, orientation, mask
-  DevBuf<uint32_t> adj_begin;        // per node: its first record (n_nodes + 1)
+  DevBuf<uint64_t> blk_pmask;  // pattern bits over packed positions
+  DevBuf<unsigned long long> sbase;  // kSlotCats x (n_blocks + 1) slot scans
+  unsigned long long slot_off[kSlotCats] = {0, 0, 0, 0, 0};
+  unsigned long long vs_off = 0;     // S starts here in V
+  size_t n_desc = 0;
+  DevBuf<uint32_t> src_map;          // per CSR entry: its slot in S
+  DevBuf<uint2> slot_desc;           // per slot: scratch start, count | stride << 24 | in-pattern << 31
+  size_t s_words = 0;
   size_t v_words = 0;
   DevBuf<double> V;
   DevBuf<uint32_t> blk_start, blk_count;
@@ -1796,8 +1789,10 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   h->off_p.release();
   h->blk_voff.release();
   h->blk_lay.release();
-  h->adj.release();
-  h->adj_begin.release();
+  h->blk_pmask.release();
+  h->sbase.release();
+  h->src_map.release();
+  h->slot_desc.release();
   h->mask_t.release();
   h->mask_b.release();
   h->mask_p.release();
@@ -2720,9 +2715,13 @@ int numeric_enqueue(fem_gpu* h) {
   int r = launch_elements(h, st, sb, sp);
   if (r) return r;
   CK(cudaEventRecordWithFlags(h->ev[1], h->stream, cudaEventRecordExternal));
-  if (h->n_blocks)
-    k_node_rows<<<grid_for(h->nodes_number, kRedWarps), kRedWarps * 32, 0, h->stream>>>(
-        h->nodes_number, h->adj_begin.p, h->adj.p, h->row_ptr.p, h->V.p, h->values.p, h->flag.p);
+  if (h->n_blocks) {
+    if (h->n_desc)
+      k_block_sums<<<grid_for(h->n_desc, 256), 256, 0, h->stream>>>(h->n_desc, h->s_words, h->slot_desc.p, h->V.p,
+                                                                     h->V.p + h->vs_off, h->flag.p);
+    k_gather_values<<<grid_for(((size_t)h->nnz + kGatherPerThread - 1) / kGatherPerThread, 256), 256, 0,
+                      h->stream>>>((size_t)h->nnz, h->src_map.p, h->V.p, h->vs_off, h->values.p, h->flag.p);
+  }
   CK(cudaGetLastError());
   CK(cudaEventRecordWithFlags(h->ev[2], h->stream, cudaEventRecordExternal));
   return FEM_GPU_OK;
@@ -2854,8 +2853,9 @@ int symbolic(fem_gpu* h) {
     CK(h->blk_voff.reserve(nb + 1, s));
     CK(h->blk_lay.reserve(nb + 1, s));
     CK(cudaMemsetAsync(sizes.p + nb, 0, sizeof(unsigned long long), s));
+    CK(h->blk_pmask.reserve(nb + 1, s));
     k_block_sizes<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_mask.p, h->blk_I.p, h->blk_J.p,
-                                                    h->blk_lay.p, sizes.p);
+                                                    h->blk_lay.p, h->blk_pmask.p, sizes.p);
     st = cub_call(h, [&](void* tmp, size_t& bytes) {
       return cub::DeviceScan::ExclusiveSum(tmp, bytes, sizes.p, h->blk_voff.p, (int64_t)(nb + 1), s);
     });
@@ -2921,42 +2921,61 @@ int symbolic(fem_gpu* h) {
   CK(h->col_idx.reserve(nnz + 1, s));
   CK(h->values.reserve(nnz + 1, s));
   CK(h->nnz_group.reserve(nnz + 1, s));
+  CK(h->src_map.reserve(nnz + 1, s));
   CK(h->g_row.reserve(ng + 1, s));
   CK(h->g_col.reserve(ng + 1, s));
   CK(h->g_kind.reserve(ng + 1, s));
-  // the adjacency records the numeric pass reduces from, and the CSR columns and groups
+  // block-sum slots by contribution count, their descriptors, then the CSR rows with the source of every entry
   {
-    if (h->v_words + 4 >= (1ull << 32))
-      return h->fail(FEM_GPU_ERR_ARGUMENT, "model too large: %llu doubles of scratch (limit 2^32)",
-                     (unsigned long long)h->v_words);
-    CK(h->V.reserve(h->v_words + 4, s));
-    h->n_adj = na;
-    CK(h->adj.reserve(na + 1, s));
-    CK(h->adj_begin.reserve(nn + 1, s));
-    DevBuf<uint32_t> node_n;
-    CK(node_n.reserve(nn + 1, s));
-    CK(cudaMemsetAsync(node_n.p, 0, (nn + 1) * sizeof(uint32_t), s));
-    k_adj_records<<<grid_for(na, 256), 256, 0, s>>>(na, sakeys.p, kb, savals.p, h->blk_count.p, h->blk_lay.p,
-                                                    h->blk_voff.p, h->blk_mask.p, h->blk_maskT.p, h->adj.p, node_n.p);
-    st = cub_call(h, [&](void* tmp, size_t& bytes) {
-      return cub::DeviceScan::ExclusiveSum(tmp, bytes, node_n.p, h->adj_begin.p, (int64_t)(nn + 1), s);
-    });
-    if (st) return st;
+    const size_t st_ = nb + 1;
+    DevBuf<unsigned long long> sz;
+    CK(sz.reserve(kSlotCats * st_, s));
+    CK(h->sbase.reserve(kSlotCats * st_, s));
+    for (int g = 0; g < kSlotCats; ++g) CK(cudaMemsetAsync(sz.p + g * st_ + nb, 0, sizeof(unsigned long long), s));
+    k_slot_sizes<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_pmask.p, h->blk_lay.p, sz.p);
+    for (int g = 0; g < kSlotCats; ++g) {
+      st = cub_call(h, [&](void* tmp, size_t& bytes) {
+        return cub::DeviceScan::ExclusiveSum(tmp, bytes, sz.p + g * st_, h->sbase.p + g * st_, (int64_t)st_, s);
+      });
+      if (st) return st;
+    }
+    unsigned long long tot[kSlotCats];
+    for (int g = 0; g < kSlotCats; ++g)
+      CK(cudaMemcpyAsync(&tot[g], h->sbase.p + g * st_ + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    // descriptor order: 2, 3, 4, 5+ contributions (the S slots), then the check-only ones
+    unsigned long long at = 0;
+    for (int g = 1; g < kSlotCats; ++g) {
+      h->slot_off[g] = at;
+      at += tot[g];
+    }
+    h->s_words = (size_t)at;
+    h->slot_off[0] = at;
+    h->n_desc = (size_t)(at + tot[0]);
+    h->vs_off = ((unsigned long long)h->v_words + 3ull) & ~3ull;  // S 32-byte aligned after the scratch
+    if (h->vs_off + h->s_words + 4 >= (1ull << 32))
+      return h->fail(FEM_GPU_ERR_ARGUMENT, "model too large: %llu doubles of scratch and sums (limit 2^32)",
+                     (unsigned long long)(h->vs_off + h->s_words));
+    CK(h->V.reserve(h->vs_off + h->s_words + 4, s));
+    SlotLayout L;
+    L.base = h->sbase.p;
+    L.stride = st_;
+    for (int g = 0; g < kSlotCats; ++g) L.off[g] = h->slot_off[g];
+    L.vs_off = h->vs_off;
+    CK(h->slot_desc.reserve(h->n_desc + 1, s));
     CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), s));
-    k_slot_checks<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->flag.p);
-    k_node_sizes<<<grid_for(nn, 256), 256, 0, s>>>(nn, h->row_ptr.p, h->flag.p);
-    k_row_fill<<<grid_for(nn * kRowLanes, 256), 256, 0, s>>>(nn, seg_b.p, seg_e.p, sakeys.p, kb, savals.p,
-                                                             h->blk_mask.p, h->blk_maskT.p, h->row_ptr.p, gbase.p,
-                                                             h->col_idx.p, h->nnz_group.p, h->g_row.p, h->g_col.p,
-                                                             h->g_kind.p);
+    k_slot_desc<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_pmask.p, h->blk_lay.p, h->blk_voff.p, L,
+                                                  h->slot_desc.p, h->flag.p);
+    k_row_fill<<<grid_for(nn * kRowLanes, 256), 256, 0, s>>>(nn, seg_b.p, seg_e.p, sakeys.p, kb, savals.p, h->blk_mask.p,
+                                                    h->blk_maskT.p, h->blk_lay.p, h->blk_count.p, h->blk_voff.p, L,
+                                                    h->row_ptr.p, gbase.p, h->col_idx.p, h->nnz_group.p,
+                                                    h->src_map.p, h->g_row.p, h->g_col.p, h->g_kind.p);
     CK(cudaGetLastError());
     int too_many = 0;
     CK(cudaMemcpyAsync(&too_many, h->flag.p, sizeof too_many, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    if (too_many & 1) return h->fail(FEM_GPU_ERR_ARGUMENT, "a node pair is shared by 2^24 or more elements");
-    if (too_many & 2)
-      return h->fail(FEM_GPU_ERR_ARGUMENT, "a node's six stiffness rows hold 2^22 or more entries");
-    node_n.release();
+    if (too_many) return h->fail(FEM_GPU_ERR_ARGUMENT, "a node pair is shared by 2^24 or more elements");
+    sz.release();
   }
   CK(cudaStreamSynchronize(s));
   // temporaries
@@ -3218,18 +3237,18 @@ extern "C" int fem_gpu_get_stream(fem_gpu_t* h, void** stream) {
 
 extern "C" int fem_gpu_numeric_launch_count(fem_gpu_t* h, int* n_launches) {
   if (!h || !n_launches) return FEM_GPU_ERR_ARGUMENT;
-  *n_launches = (h->nt ? 1 : 0) + (h->nbm ? 1 : 0) + (h->np ? 1 : 0) + (h->n_blocks ? 1 : 0);
+  *n_launches = (h->nt ? 1 : 0) + (h->nbm ? 1 : 0) + (h->np ? 1 : 0) + (h->n_blocks ? 2 : 0);
   return FEM_GPU_OK;
 }
 
 extern "C" int fem_gpu_get_pattern_stats(fem_gpu_t* h, int64_t* n_blocks, int64_t* n_contributions,
-                                         int64_t* scratch_doubles, int64_t* adjacency_records) {
+                                         int64_t* scratch_doubles, int64_t* sum_slots) {
   if (!h) return FEM_GPU_ERR_ARGUMENT;
   if (!h->pattern_valid) return h->fail(FEM_GPU_ERR_STATE, "call fem_gpu_assemble first");
   if (n_blocks) *n_blocks = (int64_t)h->n_blocks;
   if (n_contributions) *n_contributions = (int64_t)h->n_pairs;
   if (scratch_doubles) *scratch_doubles = (int64_t)h->v_words;
-  if (adjacency_records) *adjacency_records = (int64_t)h->n_adj;
+  if (sum_slots) *sum_slots = (int64_t)h->s_words;
   return FEM_GPU_OK;
 }
 

@@ -285,7 +285,7 @@ class FEM:
         return n.value
 
     def pattern_stats(self):
-        """(global node-pair blocks, element node-pair contributions, packed scratch doubles, adjacency records)."""
+        """(global node-pair blocks, element node-pair contributions, packed scratch doubles, block-sum slots)."""
         a, b, c, d = c_int64(0), c_int64(0), c_int64(0), c_int64(0)
         self._check(self._L.fem_gpu_get_pattern_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
                                                       ctypes.byref(d)))

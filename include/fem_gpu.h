@@ -157,10 +157,9 @@ int fem_gpu_numeric_launch_count(fem_gpu_t* h, int* n_launches);
 
 /* Sizes of the stored pattern: global node-pair blocks, element node-pair
  * contributions, doubles of packed element-block scratch one numeric pass
- * writes and reads, and adjacency records (one per row node and adjacent
- * block, 16 bytes each) the reduction into CSR values reads. */
+ * writes and reads, and packed block-sum slots the CSR values are gathered from. */
 int fem_gpu_get_pattern_stats(fem_gpu_t* h, int64_t* n_blocks, int64_t* n_contributions, int64_t* scratch_doubles,
-                              int64_t* adjacency_records);
+                              int64_t* sum_slots);
 
 /* Per-kernel timing of the last numeric pass, measured with CUDA events on the
  * handle's stream (milliseconds): element kernels (all types) and the reduction. */
@@ -203,11 +202,11 @@ int fem_gpu_batch_get_values_device(fem_gpu_batch_t* b, size_t i, const double**
 int fem_gpu_batch_get_stream(fem_gpu_batch_t* b, void** stream);
 /* device time of the last synchronous fem_gpu_batch_assemble (CUDA events), ms */
 int fem_gpu_batch_last_ms(fem_gpu_batch_t* b, float* ms);
-/* Measure the candidate launch configurations of the element phase (plain
- * element launches of 64, 128 or 256 threads; one persistent launch with 1 or
- * 2 CTAs per SM and four tile-size sets) with `reps` graph replays each, keep
- * the fastest, write the table as JSON to cache_path (if not NULL) and into
- * summary (if not NULL, at most cap bytes). */
+/* Measure the candidate launch configurations (plain element launches of 64,
+ * 128 or 256 threads; one persistent launch with 1 or 2 CTAs per SM and four
+ * tile-size sets; reduction blocks of 128, 256, 512 threads) with `reps` graph
+ * replays each, keep the fastest, write the table as JSON to cache_path (if
+ * not NULL) and into summary (if not NULL, at most cap bytes). */
 int fem_gpu_batch_autotune(fem_gpu_batch_t* b, int reps, const char* cache_path, char* summary, size_t cap);
 /* A batch built from the host arrays of many independent structures, laid
  * out structure after structure (offset arrays of n_structures + 1 entries
@@ -259,8 +258,7 @@ int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, const fem_g
 int fem_gpu_batch_size(const fem_gpu_batch_t* b, size_t* n_structures);
 int fem_gpu_batch_get_csr_sizes(fem_gpu_batch_t* b, size_t i, int64_t* n_rows, int64_t* nnz);
 int fem_gpu_batch_get_csr(fem_gpu_batch_t* b, size_t i, int64_t* row_ptr, int32_t* col_idx, double* values);
-/* apply a configuration read back from that table (sum_block, 128, 256 or 512,
- * is recorded in the table only: the node-row reduction has one shape) */
+/* apply a configuration read back from that table */
 int fem_gpu_batch_configure(fem_gpu_batch_t* b, int persistent, int block, int ctas_per_sm, int tile_truss,
                             int tile_beam, int tile_plate, int sum_block);
 

@@ -507,7 +507,8 @@ static double plate_gauss_g(void) { return sqrt((double)(1.0f / 3.0f)); }
  *       (quad.rs:252-338 and 380-446; ax.. are the sums of plate.rs:424-429)
  *   D  = det Jh = 16 det J,  q = 1 / D
  *   gx_i = D dh_i/dx,  gy_i = D dh_i/dy    (quad.rs:613-653)
- *   S..  = sum over IPs of q g_i g_j   ->  K_mem = (cm/16) T, K_bend = (cb/16) T
+ *   S..  = sum over IPs of (cm/16) q g_i g_j   ->  K_mem = T, K_bend = (t^2 / 12) T
+ *       (the membrane factor rides on the integration-point weights)
  *   shear: m^2 det w = Q / (4 D) with Q = |Jh row|^2 (plate.rs:443-447); the
  *   four rank-1 rows of each IP are grouped by tying line (rows at s = +-g share
  *   a direction, rows at r = +-g share a direction), coefficient c_s / 64.
@@ -541,6 +542,16 @@ static void plate_local_matrix(const double xl[4], const double yl[4], double yo
     q[2] = (D[3] * D01) * inv;
     q[3] = (D[2] * D01) * inv;
   }
+  /* material (plate.rs:532-548, :580-597, :629-636), one reciprocal: cm/16 = E t / (16 (1 - nu^2)) scales
+   * the membrane sums through the integration-point weights, bending = (t^2 / 12) x membrane, shear
+   * c_s/64 = E t k (1 - nu) / (128 (1 - nu^2)) */
+  double dinv = 1.0 / (1.0 - poisson * poisson);
+  double Et = young * thickness;
+  double cmq = (Et * dinv) * 0.0625;
+  double tb = (thickness * thickness) * 0x1.5555555555555p-4;
+  double omn = 1.0 - poisson;
+  double cq = ((Et * shear_factor) * omn) * (dinv * 0x1p-7);
+  double gam = omn * 0.5;
   double Sxx[16] = {0}, Syy[16] = {0}, Sxy[16] = {0};
   double Wr[4], Ws[4];
   for (int ip = 0; ip < 4; ++ip) {
@@ -550,10 +561,11 @@ static void plate_local_matrix(const double xl[4], const double yl[4], double yo
     double P3 = J01[ip] * rp, P4 = J01[ip] * rm, Q1 = J00[ip] * rp, Q2 = J00[ip] * rm;
     double gx[4] = {fma(J11[ip], sp, -P3), fma(-J11[ip], sp, -P4), fma(-J11[ip], sm, P4), fma(J11[ip], sm, P3)};
     double gy[4] = {fma(-J10[ip], sp, Q1), fma(J10[ip], sp, Q2), fma(J10[ip], sm, -Q2), fma(-J10[ip], sm, -Q1)};
+    double qm = cmq * q[ip];
     double a[4], bq[4];
     for (int i = 0; i < 4; ++i) {
-      a[i] = q[ip] * gx[i];
-      bq[i] = q[ip] * gy[i];
+      a[i] = qm * gx[i];
+      bq[i] = qm * gy[i];
     }
     for (int i = 0; i < 4; ++i)
       for (int j = i; j < 4; ++j) {
@@ -565,17 +577,8 @@ static void plate_local_matrix(const double xl[4], const double yl[4], double yo
     Wr[ip] = fma(J11[ip], J11[ip], J10[ip] * J10[ip]) * q[ip];
     Ws[ip] = fma(J01[ip], J01[ip], J00[ip] * J00[ip]) * q[ip];
   }
-  /* material (plate.rs:532-548, :580-597, :629-636), one reciprocal:
-   * cm/16, cb/16 = (cm/16) t^2 / 12, c_s/64 = E t k (1 - nu) / (128 (1 - nu^2)) */
-  double dinv = 1.0 / (1.0 - poisson * poisson);
-  double Et = young * thickness;
-  double cmq = (Et * dinv) * 0.0625;
-  double cbq = ((cmq * thickness) * thickness) * 0x1.5555555555555p-4;
-  double omn = 1.0 - poisson;
-  double cq = ((Et * shear_factor) * omn) * (dinv * 0x1p-7);
-  double gam = omn * 0.5;
 
-  /* membrane: (u_i,u_j) = cm T_uu, (v_i,v_j) = cm T_vv, (u_i,v_j) = cm T_uv(i,j) */
+  /* membrane: (u_i,u_j) = T_uu, (v_i,v_j) = T_vv, (u_i,v_j) = T_uv(i,j) (the sums carry cm/16) */
   double Tuu[16], Tvv[16], Tuv[16];
   for (int i = 0; i < 4; ++i)
     for (int j = 0; j < 4; ++j) {
@@ -587,16 +590,16 @@ static void plate_local_matrix(const double xl[4], const double yl[4], double yo
   for (int i = 0; i < 4; ++i)
     for (int j = i; j < 4; ++j) {
       int ri = 6 * i, cj = 6 * j;
-      double uu = cmq * Tuu[4 * i + j], vv = cmq * Tvv[4 * i + j];
+      double uu = Tuu[4 * i + j], vv = Tvv[4 * i + j];
       K[24 * (ri + 0) + cj + 0] = uu;
       K[24 * (cj + 0) + ri + 0] = uu;
       K[24 * (ri + 1) + cj + 1] = vv;
       K[24 * (cj + 1) + ri + 1] = vv;
-      double uv = cmq * Tuv[4 * i + j];
+      double uv = Tuv[4 * i + j];
       K[24 * (ri + 0) + cj + 1] = uv;
       K[24 * (cj + 1) + ri + 0] = uv;
       if (i != j) {
-        double vu = cmq * Tuv[4 * j + i]; /* (v_i, u_j) = (u_j, v_i) */
+        double vu = Tuv[4 * j + i]; /* (v_i, u_j) = (u_j, v_i) */
         K[24 * (ri + 1) + cj + 0] = vu;
         K[24 * (cj + 0) + ri + 1] = vu;
       }
@@ -664,12 +667,12 @@ static void plate_local_matrix(const double xl[4], const double yl[4], double yo
           double sh = fma(f, e, t1);
           double v = sh;
           if (a_ >= 1 && b_ >= 1) {
-            /* bending on (thx, thy): (thy,thy) = cb T_uu, (thx,thx) = cb T_vv,
-             * (thy_i, thx_j) = -cb T_uv(i,j), (thx_i, thy_j) = -cb T_uv(j,i) */
-            if (a_ == 2 && b_ == 2) v = fma(cbq, Tuu[4 * i + j], sh);
-            else if (a_ == 1 && b_ == 1) v = fma(cbq, Tvv[4 * i + j], sh);
-            else if (a_ == 2 && b_ == 1) v = fma(-cbq, Tuv[4 * i + j], sh);
-            else v = fma(-cbq, Tuv[4 * j + i], sh);
+            /* bending on (thx, thy): (thy,thy) = tb T_uu, (thx,thx) = tb T_vv,
+             * (thy_i, thx_j) = -tb T_uv(i,j), (thx_i, thy_j) = -tb T_uv(j,i) */
+            if (a_ == 2 && b_ == 2) v = fma(tb, Tuu[4 * i + j], sh);
+            else if (a_ == 1 && b_ == 1) v = fma(tb, Tvv[4 * i + j], sh);
+            else if (a_ == 2 && b_ == 1) v = fma(-tb, Tuv[4 * i + j], sh);
+            else v = fma(-tb, Tuv[4 * j + i], sh);
           }
           int r_ = 6 * i + 2 + a_, c_ = 6 * j + 2 + b_;
           K[24 * r_ + c_] = v;
