@@ -645,6 +645,30 @@ def run_results(args):
     g.close()
 
 
+def copy_ceiling(nbytes, reps=5):
+    """The link's copy rates on this machine: one cudaMemcpyAsync of `nbytes` between a device buffer and pinned
+    host memory each way (CUDA events, best of `reps`), in GB/s -- the ceiling of the e2e read-back."""
+    import torch
+
+    dev = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    out = {}
+    for name, dst, src in (("d2h_gbs", host, dev), ("h2d_gbs", dev, host)):
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[name] = nbytes / (best * 1e-3) / 1e9
+    out["bytes"] = int(nbytes)
+    del dev, host
+    return out
+
+
 def run_numeric(args):
     """The numeric pass of the plate, beam or truss workload (the line's value), its roofline, the CPU
     baseline and the e2e drop-in sequence.  Returns the result line."""
@@ -787,6 +811,8 @@ def run_numeric(args):
            "phases_ms": {"add_nodes": ph[0], "add_elements": ph[1], "assemble_to_host": ph[2]},
            "what": "create + add_nodes + add_* + assemble (symbolic + numeric) with the CSR read back to pinned "
                    "host buffers (fem_gpu_assemble_to_host: the pattern's read-back overlaps the numeric pass)"}
+    if args.e2e_steps:
+        e2e["copy_ceiling"] = copy_ceiling(d2h)
 
     cpu = None
     if rank == 0 and not args.no_cpu:

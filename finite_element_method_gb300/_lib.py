@@ -83,6 +83,7 @@ SIGNATURES = {
     "fem_gpu_batch_size": (c_int, [hp, szp]),
     "fem_gpu_batch_get_csr_sizes": (c_int, [hp, c_size_t, i64p, i64p]),
     "fem_gpu_batch_get_csr": (c_int, [hp, c_size_t, i64p, i32p, dp]),
+    "fem_gpu_debug_check": (c_int, [POINTER(c_int), POINTER(c_int), i64p, i64p]),
     "fem_gpu_assemble_dense_noalloc": (c_int, [c_uint32, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p,
                                                c_void_p, c_size_t, c_void_p, c_void_p, c_double, c_double, c_void_p,
                                                c_void_p]),
@@ -110,6 +111,30 @@ def library_path() -> str:
     return _build.LIB_PATH
 
 
+def _bind(lib):
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+_debug_lib = None
+
+
+def load_debug(build_if_missing: bool = True) -> ctypes.CDLL:
+    """libfem_gpu_debug.so: the same C ABI with the device-side index checks of the assembly path (its
+    fem_gpu_debug_check reports the first out-of-range index).  Loaded beside the release library."""
+    global _debug_lib
+    if _debug_lib is None:
+        if build_if_missing:
+            _build.build()
+        if not os.path.exists(_build.DEBUG_LIB_PATH):
+            raise RuntimeError(f"index-checked library not found at {_build.DEBUG_LIB_PATH}")
+        _debug_lib = _bind(ctypes.CDLL(_build.DEBUG_LIB_PATH))
+    return _debug_lib
+
+
 def load(build_if_missing: bool = True) -> ctypes.CDLL:
     """Load libfem_gpu.so (building it first when absent or stale)."""
     global _lib
@@ -120,13 +145,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         path = _build.build()
     if not os.path.exists(path):
         raise RuntimeError(f"CUDA assembly library not found at {path}; build it with finite_element_method_gb300.build")
-    lib = ctypes.CDLL(path)
-    for name, (res, args) in SIGNATURES.items():
-        f = getattr(lib, name)
-        f.restype = res
-        f.argtypes = args
-    _lib = lib
-    return lib
+    _lib = _bind(ctypes.CDLL(path))
+    return _lib
 
 
 def ptr(a, ct):

@@ -15,6 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libfem_gpu.so")
+# the same library with the device-side index checks of the assembly path (-DFEM_GPU_DEBUG)
+DEBUG_LIB_PATH = os.path.join(LIB_DIR, "libfem_gpu_debug.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -35,30 +37,37 @@ def _sources():
     return [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
 
 
-def _stale() -> bool:
-    if not os.path.exists(LIB_PATH):
+def _stale(path: str) -> bool:
+    if not os.path.exists(path):
         return True
-    t = os.path.getmtime(LIB_PATH)
+    t = os.path.getmtime(path)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+VARIANTS = {LIB_PATH: ("obj", []), DEBUG_LIB_PATH: ("obj_debug", ["-DFEM_GPU_DEBUG"])}
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile every translation unit in parallel and link libfem_gpu.so."""
-    if not force and not _stale():
+    """Compile every translation unit of both libraries (release and index-checked) in parallel and link
+    libfem_gpu.so and libfem_gpu_debug.so; returns the release library's path."""
+    todo = [path for path in VARIANTS if force or _stale(path)]
+    if not todo:
         return LIB_PATH
     nvcc = _nvcc()
-    obj_dir = os.path.join(LIB_DIR, "obj")
-    os.makedirs(obj_dir, exist_ok=True)
-    procs = []
-    objs = []
-    for src in _sources():
-        obj = os.path.join(obj_dir, os.path.splitext(src)[0] + ".o")
-        objs.append(obj)
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
-        if verbose:
-            cmd.insert(1, "-Xptxas=-v")
-        procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    procs, objs = [], {}
+    for path in todo:
+        sub, extra = VARIANTS[path]
+        obj_dir = os.path.join(LIB_DIR, sub)
+        os.makedirs(obj_dir, exist_ok=True)
+        objs[path] = []
+        for src in _sources():
+            obj = os.path.join(obj_dir, os.path.splitext(src)[0] + ".o")
+            objs[path].append(obj)
+            cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+            if verbose:
+                cmd.insert(1, "-Xptxas=-v")
+            procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
     failed = []
     for src, p in procs:
         out, _ = p.communicate()
@@ -68,9 +77,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
             print(out.decode(errors="replace"))
     if failed:
         raise RuntimeError("nvcc failed:\n" + "\n".join(failed))
-    tmp = LIB_PATH + ".tmp"
-    subprocess.run([nvcc, *ARCH, "-shared", "-o", tmp, *objs], check=True, capture_output=True)
-    os.replace(tmp, LIB_PATH)
+    for path in todo:
+        tmp = path + ".tmp"
+        subprocess.run([nvcc, *ARCH, "-shared", "-o", tmp, *objs[path]], check=True, capture_output=True)
+        os.replace(tmp, path)
     return LIB_PATH
 
 

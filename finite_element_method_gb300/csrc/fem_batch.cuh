@@ -91,6 +91,7 @@ struct BatchData {
   const uint2* desc = nullptr;      // block-sum descriptors (sums first, then the check-only ones)
   size_t n_desc = 0, n_sums = 0;
   unsigned long long vs_off = 0;    // S starts here in V
+  unsigned long long v_words = 0;   // packed element scratch (before S)
   const uint32_t* src_map = nullptr;
   double* values = nullptr;
 };
@@ -145,7 +146,7 @@ struct fem_gpu_batch {
     return fail(e == cudaErrorMemoryAllocation ? FEM_GPU_ERR_OUT_OF_MEMORY : FEM_GPU_ERR_CUDA, "CUDA error in %s: %s",
                 what, cudaGetErrorString(e));
   }
-  NodesView nodes() const { return NodesView{dx.p, dy.p, dz.p}; }
+  NodesView nodes() const { return NodesView{dx.p, dy.p, dz.p, n_nodes}; }
   TrussView trusses() const { return TrussView{t_n1.p, t_n2.p, t_E.p, t_A.p, t_A2.p}; }
   BeamView beams() const {
     return BeamView{b_n1.p, b_n2.p, b_E.p, b_nu.p, b_A.p, b_i11.p, b_i22.p, b_i12.p, b_it.p, b_ks.p, b_ax.p, b_ay.p, b_az.p};
@@ -189,9 +190,9 @@ int batch_enqueue(fem_gpu_batch* b) {
   cudaStream_t s = b->stream;
   BCK(cudaMemsetAsync(b->flag.p, 0, sizeof(int), s));
   const BatchData& d = b->d;
-  BlockSink st{nullptr, d.V, d.pk_t, b->flag.p};
-  BlockSink sb{nullptr, d.V, d.pk_b, b->flag.p};
-  BlockSink sp{nullptr, d.V, d.pk_p, b->flag.p};
+  BlockSink st{nullptr, d.V, d.pk_t, b->flag.p, d.v_words};
+  BlockSink sb{nullptr, d.V, d.pk_b, b->flag.p, d.v_words};
+  BlockSink sp{nullptr, d.V, d.pk_p, b->flag.p, d.v_words};
   if (b->cfg.persistent) {
     BCK(cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned int), s));
     const unsigned grid = (unsigned)std::max(1, b->sm_count * b->cfg.ctas_per_sm);
@@ -205,10 +206,11 @@ int batch_enqueue(fem_gpu_batch* b) {
   }
   const unsigned rb = (unsigned)b->cfg.sum_block;
   if (d.n_desc)
-    k_block_sums<<<grid_for(d.n_desc, rb), rb, 0, s>>>(d.n_desc, d.n_sums, d.desc, d.V, d.V + d.vs_off, b->flag.p);
+    k_block_sums<<<grid_for(d.n_desc, rb), rb, 0, s>>>(d.n_desc, d.n_sums, d.desc, d.V, d.V + d.vs_off, b->flag.p,
+                                                       d.v_words);
   if (b->nnz)
     k_gather_values<<<grid_for(((size_t)b->nnz + kGatherPerThread - 1) / kGatherPerThread, rb), rb, 0, s>>>(
-        (size_t)b->nnz, d.src_map, d.V, d.vs_off, d.values, b->flag.p);
+        (size_t)b->nnz, d.src_map, d.V, d.vs_off, d.values, b->flag.p, d.vs_off + d.n_sums);
   BCK(cudaGetLastError());
   return FEM_GPU_OK;
 }
@@ -429,6 +431,7 @@ extern "C" int fem_gpu_batch_create(fem_gpu_t* const* models, size_t n_models, f
   d.n_desc = b->n_desc;
   d.n_sums = b->n_sums;
   d.vs_off = b->vs_off;
+  d.v_words = b->vs_off;  // the models' scratch, end to end (S follows)
   d.src_map = b->src_map.p;
   d.values = b->values.p;
   BCK(cudaStreamSynchronize(s));

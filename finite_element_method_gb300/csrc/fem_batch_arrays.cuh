@@ -551,6 +551,7 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
   d.n_desc = h->n_desc;
   d.n_sums = h->s_words;
   d.vs_off = h->vs_off;
+  d.v_words = h->v_words;
   d.src_map = h->src_map.p;
   d.values = h->values.p;
   return batch_make_graph(b);

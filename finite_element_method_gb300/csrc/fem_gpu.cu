@@ -132,9 +132,56 @@ struct DevBuf {
 // ---------------------------------------------------------------------------
 // kernels: validation
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// debug builds: index checks on the assembly path
+// ---------------------------------------------------------------------------
+// Built with -DFEM_GPU_DEBUG (lib/libfem_gpu_debug.so), the assembly kernels
+// check every node index, scratch position, block-sum source, CSR source and
+// CSR / group position against the length of its array before the access.  An
+// index out of range skips the access and records the first failing site,
+// index and bound in g_dbg -- no trap, so the context stays usable and the host
+// reads the record with fem_gpu_debug_check.  Without the macro the checks
+// compile to nothing.
+struct DebugRecord {
+  int flag, site;
+  unsigned long long index, bound;
+};
+__device__ DebugRecord g_dbg;
+enum : int {
+  kDbgNode = 1,         // node index of an element (coordinate gather)
+  kDbgScratch = 2,      // packed block written by an element kernel
+  kDbgSumSource = 3,    // last contribution read by a block sum
+  kDbgGatherSource = 4, // scratch or sum slot read by the CSR gather
+  kDbgCsrEntry = 5,     // CSR position written by the row fill
+  kDbgGroup = 6,        // stiffness-group position written by the row fill
+  kDbgRowSource = 7     // value source the row fill records for a CSR entry
+};
+constexpr unsigned long long kNoBound = ~0ull;
+__device__ __forceinline__ bool dbg_in_range(unsigned long long i, unsigned long long n, int site) {
+#ifdef FEM_GPU_DEBUG
+  if (i < n) return true;
+  if (atomicCAS(&g_dbg.flag, 0, 1) == 0) {
+    g_dbg.site = site;
+    g_dbg.index = i;
+    g_dbg.bound = n;
+  }
+  return false;
+#else
+  (void)i;
+  (void)n;
+  (void)site;
+  return true;
+#endif
+}
+
 struct NodesView {
   const double *x, *y, *z;
+  unsigned long long n = kNoBound;  // nodes held (checked in debug builds)
   __device__ __forceinline__ void get(int i, double o[3]) const {
+    if (!dbg_in_range((unsigned long long)(unsigned)i, n, kDbgNode)) {
+      o[0] = o[1] = o[2] = 0.0;
+      return;
+    }
     o[0] = x[i];
     o[1] = y[i];
     o[2] = z[i];
@@ -330,6 +377,7 @@ struct BlockSink {
   double* V;                            // numeric mode
   const unsigned long long* pack;       // numeric mode: per (element, pair)
   int* flag;
+  unsigned long long v_words = kNoBound;  // numeric mode: doubles of V (checked in debug builds)
   __device__ __forceinline__ void put(size_t ep, bool transpose, const double blk[36]) const {
     if (mask) {
       uint64_t m = 0;
@@ -345,6 +393,8 @@ struct BlockSink {
     }
     const unsigned long long pk = pack[ep];
     const uint32_t lay = (uint32_t)(pk >> 62);
+    if (!dbg_in_range((pk & ((1ull << 62) - 1ull)) + (unsigned long long)lay_size(lay) - 1ull, v_words, kDbgScratch))
+      return;
     double* dst = V + (pk & ((1ull << 62) - 1ull));
     if (lay == kLayFull) {
 #pragma unroll
@@ -735,7 +785,8 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
                            const int64_t* __restrict__ row_ptr, const int64_t* __restrict__ gbase,
                            int32_t* __restrict__ col_idx, int32_t* __restrict__ nnz_group,
                            uint32_t* __restrict__ src_map, int32_t* __restrict__ g_row, int32_t* __restrict__ g_col,
-                           uint8_t* __restrict__ g_kind) {
+                           uint8_t* __restrict__ g_kind, unsigned long long nnz, unsigned long long n_groups,
+                           unsigned long long vs_end) {
   const size_t r = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) / kRowLanes;
   const int lane = (int)(threadIdx.x & (kRowLanes - 1));
   // every lane stays for the shuffles: a node past the end or without blocks has an empty range
@@ -776,9 +827,11 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
     for (int kd = 0; kd < 4; ++kd) {
       kg[kd] = -1;
       if (km & (1u << kd)) {
-        g_row[g] = (int32_t)r;
-        g_col[g] = (int32_t)J;
-        g_kind[g] = (uint8_t)kd;
+        if (dbg_in_range((unsigned long long)g, n_groups, kDbgGroup)) {
+          g_row[g] = (int32_t)r;
+          g_col[g] = (int32_t)J;
+          g_kind[g] = (uint8_t)kd;
+        }
         kg[kd] = (int32_t)g;
         ++g;
       }
@@ -794,9 +847,12 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
 #pragma unroll
       for (int c = 0; c < 6; ++c)
         if (rowbits & (1u << c)) {
-          col_idx[pos] = (int32_t)(6 * J + c);
-          nnz_group[pos] = kg[2 * (a / 3) + c / 3];
-          src_map[pos] = (uint32_t)(sb + (unsigned long long)packed_pos(lay, t ? 6 * c + a : 6 * a + c));
+          const unsigned long long src = sb + (unsigned long long)packed_pos(lay, t ? 6 * c + a : 6 * a + c);
+          if (dbg_in_range((unsigned long long)pos, nnz, kDbgCsrEntry) && dbg_in_range(src, vs_end, kDbgRowSource)) {
+            col_idx[pos] = (int32_t)(6 * J + c);
+            nnz_group[pos] = kg[2 * (a / 3) + c / 3];
+            src_map[pos] = (uint32_t)src;
+          }
           ++pos;
         }
       next[a] += __shfl_sync(0xffffffffu, inc, kRowLanes - 1, kRowLanes);
@@ -841,12 +897,14 @@ __global__ void k_slot_desc(size_t nb, const uint32_t* __restrict__ blk_count, c
 // a pattern slot whose contributions are all zero, raises kFlagPattern (the
 // exact-zero pattern changed).
 __global__ void __launch_bounds__(512) k_block_sums(size_t n_desc, size_t n_sums, const uint2* __restrict__ desc,
-                                                    const double* __restrict__ V, double* __restrict__ S, int* flag) {
+                                                    const double* __restrict__ V, double* __restrict__ S, int* flag,
+                                                    unsigned long long v_words) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i >= n_desc) return;
   const uint2 d = desc[i];
   const uint32_t n = d.y & 0xffffffu, stride = (d.y >> 24) & 0x7fu;
   const bool inpat = (d.y >> 31) != 0;
+  if (n == 0 || !dbg_in_range(d.x + (unsigned long long)(n - 1) * stride, v_words, kDbgSumSource)) return;
   const double* src = V + d.x;
   bool nz;
   double sum;
@@ -893,7 +951,8 @@ __global__ void __launch_bounds__(512) k_block_sums(size_t n_desc, size_t n_sums
 constexpr int kGatherPerThread = 8;
 __global__ void __launch_bounds__(512) k_gather_values(size_t nnz, const uint32_t* __restrict__ src_map,
                                                        const double* __restrict__ VS, unsigned long long vs_off,
-                                                       double* __restrict__ values, int* flag) {
+                                                       double* __restrict__ values, int* flag,
+                                                       unsigned long long vs_end) {
   const size_t k0 = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) * kGatherPerThread;
   if (k0 >= nnz) return;
   bool zero_direct = false;
@@ -904,7 +963,7 @@ __global__ void __launch_bounds__(512) k_gather_values(size_t nnz, const uint32_
     const uint32_t sx[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
     double a[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) a[q] = VS[sx[q]];
+    for (int q = 0; q < 8; ++q) a[q] = dbg_in_range(sx[q], vs_end, kDbgGatherSource) ? VS[sx[q]] : 0.0;
 #pragma unroll
     for (int q = 0; q < 8; ++q) zero_direct |= sx[q] < vs_off && !nonzero(a[q]);
     double2* out = reinterpret_cast<double2*>(values + k0);
@@ -915,7 +974,7 @@ __global__ void __launch_bounds__(512) k_gather_values(size_t nnz, const uint32_
   } else {
     for (size_t k = k0; k < nnz; ++k) {
       const uint32_t sx = src_map[k];
-      const double v = VS[sx];
+      const double v = dbg_in_range(sx, vs_end, kDbgGatherSource) ? VS[sx] : 0.0;
       zero_direct |= sx < vs_off && !nonzero(v);
       values[k] = v;
     }
@@ -1483,7 +1542,7 @@ struct fem_gpu {
     return fail(e == cudaErrorMemoryAllocation ? FEM_GPU_ERR_OUT_OF_MEMORY : FEM_GPU_ERR_CUDA, "CUDA error in %s: %s",
                 what, cudaGetErrorString(e));
   }
-  NodesView nodes() const { return NodesView{dx.p, dy.p, dz.p}; }
+  NodesView nodes() const { return NodesView{dx.p, dy.p, dz.p, dx.cap}; }
   BeamView beams() const {
     return BeamView{b_n1.p, b_n2.p, b_E.p, b_nu.p, b_A.p, b_i11.p, b_i22.p, b_i12.p, b_it.p, b_ks.p, b_ax.p, b_ay.p, b_az.p};
   }
@@ -2709,18 +2768,19 @@ int launch_elements(fem_gpu* h, BlockSink sink_t, BlockSink sink_b, BlockSink si
 int numeric_enqueue(fem_gpu* h) {
   CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->stream));
   CK(cudaEventRecordWithFlags(h->ev[0], h->stream, cudaEventRecordExternal));
-  BlockSink st{nullptr, h->V.p, h->off_t.p, h->flag.p};
-  BlockSink sb{nullptr, h->V.p, h->off_b.p, h->flag.p};
-  BlockSink sp{nullptr, h->V.p, h->off_p.p, h->flag.p};
+  BlockSink st{nullptr, h->V.p, h->off_t.p, h->flag.p, h->v_words};
+  BlockSink sb{nullptr, h->V.p, h->off_b.p, h->flag.p, h->v_words};
+  BlockSink sp{nullptr, h->V.p, h->off_p.p, h->flag.p, h->v_words};
   int r = launch_elements(h, st, sb, sp);
   if (r) return r;
   CK(cudaEventRecordWithFlags(h->ev[1], h->stream, cudaEventRecordExternal));
   if (h->n_blocks) {
     if (h->n_desc)
       k_block_sums<<<grid_for(h->n_desc, 256), 256, 0, h->stream>>>(h->n_desc, h->s_words, h->slot_desc.p, h->V.p,
-                                                                     h->V.p + h->vs_off, h->flag.p);
+                                                                     h->V.p + h->vs_off, h->flag.p, h->v_words);
     k_gather_values<<<grid_for(((size_t)h->nnz + kGatherPerThread - 1) / kGatherPerThread, 256), 256, 0,
-                      h->stream>>>((size_t)h->nnz, h->src_map.p, h->V.p, h->vs_off, h->values.p, h->flag.p);
+                      h->stream>>>((size_t)h->nnz, h->src_map.p, h->V.p, h->vs_off, h->values.p, h->flag.p,
+                                   h->vs_off + h->s_words);
   }
   CK(cudaGetLastError());
   CK(cudaEventRecordWithFlags(h->ev[2], h->stream, cudaEventRecordExternal));
@@ -2969,7 +3029,9 @@ int symbolic(fem_gpu* h) {
     k_row_fill<<<grid_for(nn * kRowLanes, 256), 256, 0, s>>>(nn, seg_b.p, seg_e.p, sakeys.p, kb, savals.p, h->blk_mask.p,
                                                     h->blk_maskT.p, h->blk_lay.p, h->blk_count.p, h->blk_voff.p, L,
                                                     h->row_ptr.p, gbase.p, h->col_idx.p, h->nnz_group.p,
-                                                    h->src_map.p, h->g_row.p, h->g_col.p, h->g_kind.p);
+                                                    h->src_map.p, h->g_row.p, h->g_col.p, h->g_kind.p,
+                                                             (unsigned long long)nnz, (unsigned long long)ng,
+                                                             h->vs_off + h->s_words);
     CK(cudaGetLastError());
     int too_many = 0;
     CK(cudaMemcpyAsync(&too_many, h->flag.p, sizeof too_many, cudaMemcpyDeviceToHost, s));
@@ -3070,6 +3132,30 @@ extern "C" int fem_gpu_assemble_numeric_async(fem_gpu_t* h) {
   if (!h) return FEM_GPU_ERR_ARGUMENT;
   if (!h->pattern_valid) return h->fail(FEM_GPU_ERR_STATE, "no valid pattern: call fem_gpu_assemble first");
   return numeric_launch(h);
+}
+
+extern "C" int fem_gpu_debug_check(int* checked, int* site, int64_t* index, int64_t* bound) {
+#ifdef FEM_GPU_DEBUG
+  if (checked) *checked = 1;
+#else
+  if (checked) *checked = 0;
+#endif
+  DebugRecord r = {};
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(&r, g_dbg, sizeof r);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return FEM_GPU_ERR_CUDA;
+  }
+  if (site) *site = r.flag ? r.site : 0;
+  if (index) *index = (int64_t)r.index;
+  if (bound) *bound = (int64_t)r.bound;
+  if (r.flag) {
+    const DebugRecord zero = {};
+    e = cudaMemcpyToSymbol(g_dbg, &zero, sizeof zero);
+    if (e != cudaSuccess) return FEM_GPU_ERR_CUDA;
+  }
+  return FEM_GPU_OK;
 }
 
 extern "C" int fem_gpu_check_pattern(fem_gpu_t* h) {

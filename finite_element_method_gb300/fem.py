@@ -53,8 +53,10 @@ def _u32(v, shape):
 class FEM:
     """FEM::create(rel_tol, abs_tol, nodes_number) with the GPU assembly behind it."""
 
-    def __init__(self, rel_tol: float, abs_tol: float, nodes_number: int):
-        self._L = _lib.load()
+    def __init__(self, rel_tol: float, abs_tol: float, nodes_number: int, library=None):
+        """`library`: the loaded C library to use (default the release build; `_lib.load_debug()` gives the
+        build with device-side index checks)."""
+        self._L = library if library is not None else _lib.load()
         h = c_void_p()
         self._check(self._L.fem_gpu_create(rel_tol, abs_tol, nodes_number, ctypes.byref(h)), None)
         self._h = h
@@ -609,14 +611,14 @@ class Batch:
             raise FEMError(st, msg)
 
     @classmethod
-    def from_meshes(cls, meshes, rel_tol: float, abs_tol: float, nodes_number=None) -> "Batch":
+    def from_meshes(cls, meshes, rel_tol: float, abs_tol: float, nodes_number=None, library=None) -> "Batch":
         """One batch standing for `FEM(rel_tol, abs_tol, n)` + add_nodes + add_trusses + add_beams +
         add_plates + assemble per mesh (fem_gpu_batch_create_from_arrays): the checks of every mesh run in
         bulk on the GPU, one symbolic phase covers all meshes and one graph launch assembles them.
         `nodes_number` (per mesh) defaults to each mesh's node count.  A failing mesh raises its first
         failing call's error, the message prefixed by "structure i: "."""
         self = cls.__new__(cls)
-        self._L = _lib.load()
+        self._L = library if library is not None else _lib.load()
         self.models = None
         S = len(meshes)
         keep = []

@@ -155,6 +155,18 @@ int fem_gpu_get_element_counts(fem_gpu_t* h, int64_t* n_truss, int64_t* n_beam, 
 int fem_gpu_get_stream(fem_gpu_t* h, void** stream);
 int fem_gpu_numeric_launch_count(fem_gpu_t* h, int* n_launches);
 
+/* Device-side index checks (no counterpart in the reference).  The library
+ * built with -DFEM_GPU_DEBUG (lib/libfem_gpu_debug.so) checks every node
+ * index, packed-scratch position, block-sum source, CSR source and CSR /
+ * stiffness-group position of the assembly kernels against its array's length
+ * and skips an out-of-range access instead of making it.  This waits for the
+ * current device, sets *checked (1 in that build, 0 in the release build) and
+ * the first failing access since the last call: *site 0 when none, else 1 node
+ * index, 2 scratch write, 3 block-sum read, 4 gather read, 5 CSR entry,
+ * 6 stiffness group, 7 CSR value source; *index and *bound the offending index
+ * and its array's length.  Reading clears the record.  Any pointer may be NULL. */
+int fem_gpu_debug_check(int* checked, int* site, int64_t* index, int64_t* bound);
+
 /* Sizes of the stored pattern: global node-pair blocks, element node-pair
  * contributions, doubles of packed element-block scratch one numeric pass
  * writes and reads, and packed block-sum slots the CSR values are gathered from. */

@@ -79,6 +79,7 @@ unsafe extern "C" {
     pub fn fem_gpu_get_element_counts(h: *mut FemGpu, n_truss: *mut i64, n_beam: *mut i64, n_plate: *mut i64) -> c_int;
     pub fn fem_gpu_get_stream(h: *mut FemGpu, stream: *mut *mut c_void) -> c_int;
     pub fn fem_gpu_numeric_launch_count(h: *mut FemGpu, n_launches: *mut c_int) -> c_int;
+    pub fn fem_gpu_debug_check(checked: *mut c_int, site: *mut c_int, index: *mut i64, bound: *mut i64) -> c_int;
     pub fn fem_gpu_get_pattern_stats(h: *mut FemGpu, n_blocks: *mut i64, n_contributions: *mut i64, scratch_doubles: *mut i64, sum_slots: *mut i64) -> c_int;
     pub fn fem_gpu_last_numeric_timing(h: *mut FemGpu, element_ms: *mut f32, reduce_ms: *mut f32) -> c_int;
     pub fn fem_gpu_vjp(h: *mut FemGpu, u: *const f64, lam: *const f64, npairs: c_int, g_truss: *mut f64, g_beam: *mut f64, g_plate: *mut f64, g_xyz: *mut f64) -> c_int;
