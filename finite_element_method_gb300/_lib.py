@@ -81,6 +81,7 @@ SIGNATURES = {
                                                     POINTER(c_void_p)]),
     "fem_gpu_batch_create_from_arrays": (c_int, [c_double, c_double, c_void_p, POINTER(c_void_p)]),
     "fem_gpu_batch_size": (c_int, [hp, szp]),
+    "fem_gpu_batch_build_ms": (c_int, [hp, dp, c_size_t]),
     "fem_gpu_batch_get_csr_sizes": (c_int, [hp, c_size_t, i64p, i64p]),
     "fem_gpu_batch_get_csr": (c_int, [hp, c_size_t, i64p, i32p, dp]),
     "fem_gpu_debug_check": (c_int, [POINTER(c_int), POINTER(c_int), i64p, i64p]),

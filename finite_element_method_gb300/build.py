@@ -48,6 +48,12 @@ def _stale(path: str) -> bool:
 VARIANTS = {LIB_PATH: ("obj", []), DEBUG_LIB_PATH: ("obj_debug", ["-DFEM_GPU_DEBUG"])}
 
 
+def _extra_flags():
+    """tuning flags from the environment (for instance FEM_GPU_NVCC_EXTRA="-DFEM_PLATE_MAXNREG=168
+    -DFEM_PLATE_BLOCK=128"); rebuild with force=True after changing them"""
+    return os.environ.get("FEM_GPU_NVCC_EXTRA", "").split()
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     """Compile every translation unit of both libraries (release and index-checked) in parallel and link
     libfem_gpu.so and libfem_gpu_debug.so; returns the release library's path."""
@@ -64,7 +70,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         for src in _sources():
             obj = os.path.join(obj_dir, os.path.splitext(src)[0] + ".o")
             objs[path].append(obj)
-            cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+            cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, *_extra_flags(), "-I", INCLUDE, "-c", os.path.join(CSRC, src),
+                   "-o", obj]
             if verbose:
                 cmd.insert(1, "-Xptxas=-v")
             procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))

@@ -276,6 +276,10 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
   *out = nullptr;
   fem_gpu_batch* b = new fem_gpu_batch();
   *out = b;
+  const auto t_start = std::chrono::steady_clock::now();
+  auto mark = [&](int k) {
+    b->build_ms[k] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+  };
   const size_t S = in->n_structures;
   if (S == 0 || S >= (1ull << 31) || !in->nodes_number || !in->node_off || !ba_offsets_ok(in->node_off, S) ||
       !ba_offsets_ok(in->truss_off, S) || !ba_offsets_ok(in->beam_off, S) || !ba_offsets_ok(in->plate_off, S))
@@ -496,6 +500,7 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
   }
   BAK(cudaMemcpyAsync(fail.data(), d_fail.p, S * sizeof(int), cudaMemcpyDeviceToHost, s));
   BAK(cudaStreamSynchronize(s));
+  mark(0);
   for (size_t q = 0; q < S; ++q) {
     if (!fail[q]) continue;
     std::string msg;
@@ -511,8 +516,10 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
   h->append_run(kTruss, 0, NT);
   h->append_run(kBeam, 0, NB);
   h->append_run(kPlate, 0, NP);
+  mark(1);
   st = fem_gpu_assemble(h);
   if (st) return b->fail(st, "%s", h->err.c_str());
+  mark(2);
   // per structure: entry offsets, local columns and row starts
   std::vector<int64_t> zoff(S + 1);
   DevBuf<int64_t> d_zoff;
@@ -554,7 +561,16 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
   d.v_words = h->v_words;
   d.src_map = h->src_map.p;
   d.values = h->values.p;
-  return batch_make_graph(b);
+  mark(3);
+  st = batch_make_graph(b);
+  mark(4);
+  return st;
+}
+
+extern "C" int fem_gpu_batch_build_ms(const fem_gpu_batch_t* b, double* ms, size_t n) {
+  if (!b || (n && !ms)) return FEM_GPU_ERR_ARGUMENT;
+  for (size_t k = 0; k < n && k < 5; ++k) ms[k] = b->build_ms[k];
+  return FEM_GPU_OK;
 }
 
 extern "C" int fem_gpu_batch_size(const fem_gpu_batch_t* b, size_t* n_structures) {

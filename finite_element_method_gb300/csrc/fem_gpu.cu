@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -553,7 +554,18 @@ __device__ __forceinline__ void plate_element(size_t e, NodesView nd, const Plat
   plate_pair<3, 3>(C, R, ident, nidx, ep + 9, sink);
 }
 
-__global__ void __launch_bounds__(256) k_plate(NodesView nd, PlateView pl, double abs_tol, size_t count,
+// Launch shape of the plate kernel.  FEM_PLATE_BLOCK threads per CTA (64 by default: at 254 registers a
+// thread an SM holds 8 warps either way, in finer pieces than 128); FEM_PLATE_MAXNREG, when defined, caps
+// its registers (more warps per SM, more spills: the measured caps of 232, 200, 168 and 128 were slower).
+#ifndef FEM_PLATE_BLOCK
+#define FEM_PLATE_BLOCK 64
+#endif
+#ifdef FEM_PLATE_MAXNREG
+__global__ void __maxnreg__(FEM_PLATE_MAXNREG)
+#else
+__global__ void __launch_bounds__(256)
+#endif
+k_plate(NodesView nd, PlateView pl, double abs_tol, size_t count,
                                                BlockSink sink) {
   size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (e >= count) return;
@@ -2759,7 +2771,9 @@ int launch_elements(fem_gpu* h, BlockSink sink_t, BlockSink sink_b, BlockSink si
     k_truss<<<grid_for(h->nt, 128), 128, 0, h->stream>>>(nd, h->trusses(), h->abs_tol, h->nt, sink_t);
   if (h->nbm)
     k_beam<<<grid_for(h->nbm, 128), 128, 0, h->stream>>>(nd, h->beams(), h->rel_tol, h->abs_tol, h->nbm, sink_b);
-  if (h->np) k_plate<<<grid_for(h->np, 128), 128, 0, h->stream>>>(nd, h->plates(), h->abs_tol, h->np, sink_p);
+  if (h->np)
+    k_plate<<<grid_for(h->np, FEM_PLATE_BLOCK), FEM_PLATE_BLOCK, 0, h->stream>>>(nd, h->plates(), h->abs_tol, h->np,
+                                                                              sink_p);
   CK(cudaGetLastError());
   return FEM_GPU_OK;
 }

@@ -617,9 +617,28 @@ class Batch:
         bulk on the GPU, one symbolic phase covers all meshes and one graph launch assembles them.
         `nodes_number` (per mesh) defaults to each mesh's node count.  A failing mesh raises its first
         failing call's error, the message prefixed by "structure i: "."""
+        return cls.from_structures(cls.structures(meshes, nodes_number), rel_tol, abs_tol, library)
+
+    @classmethod
+    def from_structures(cls, structures, rel_tol: float, abs_tol: float, library=None) -> "Batch":
+        """The batch of `Batch.structures(...)` (the arrays of many meshes laid out one after another)."""
+        st, _keep = structures
         self = cls.__new__(cls)
         self._L = library if library is not None else _lib.load()
         self.models = None
+        h = c_void_p()
+        code = self._L.fem_gpu_batch_create_from_arrays(rel_tol, abs_tol, ctypes.byref(st), ctypes.byref(h))
+        self._h = h
+        if code:
+            msg = self._L.fem_gpu_batch_last_error(h).decode() if h else f"status {code}"
+            self.close()
+            raise FEMError(code, msg)
+        return self
+
+    @staticmethod
+    def structures(meshes, nodes_number=None):
+        """The host arrays of many meshes laid out one after another, as fem_gpu_structures_t: returns the
+        ctypes structure and the arrays it points into (keep both alive while it is used)."""
         S = len(meshes)
         keep = []
 
@@ -700,15 +719,14 @@ class Batch:
             for field, key in (("plate_young", "young"), ("plate_poisson", "poisson"),
                                ("plate_thickness", "thickness"), ("plate_shear_factor", "shear_factor")):
                 setattr(st, field, ptr(col("plates", key), c_double))
-        h = c_void_p()
-        code = self._L.fem_gpu_batch_create_from_arrays(rel_tol, abs_tol, ctypes.byref(st), ctypes.byref(h))
-        self._h = h
-        del keep
-        if code:
-            msg = self._L.fem_gpu_batch_last_error(h).decode() if h else f"status {code}"
-            self.close()
-            raise FEMError(code, msg)
-        return self
+        return st, keep
+
+    def build_ms(self):
+        """host times (ms from the start) at the end of the phases of a batch built from arrays: uploads and
+        checks, union laid out, symbolic + first numeric pass, per-structure CSR offsets, graph captured"""
+        out = np.zeros(5)
+        self._check(self._L.fem_gpu_batch_build_ms(self._h, ptr(out, c_double), 5))
+        return out
 
     def __len__(self) -> int:
         n = ctypes.c_size_t(0)

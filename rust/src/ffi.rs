@@ -95,6 +95,7 @@ unsafe extern "C" {
     pub fn fem_gpu_batch_last_ms(b: *mut FemGpuBatch, ms: *mut f32) -> c_int;
     pub fn fem_gpu_batch_autotune(b: *mut FemGpuBatch, reps: c_int, cache_path: *const c_char, summary: *mut c_char, cap: usize) -> c_int;
     pub fn fem_gpu_batch_create_from_arrays(rel_tol: f64, abs_tol: f64, structures: *const FemGpuStructures, out: *mut *mut FemGpuBatch) -> c_int;
+    pub fn fem_gpu_batch_build_ms(b: *const FemGpuBatch, ms: *mut f64, n: usize) -> c_int;
     pub fn fem_gpu_batch_size(b: *const FemGpuBatch, n_structures: *mut usize) -> c_int;
     pub fn fem_gpu_batch_get_csr_sizes(b: *mut FemGpuBatch, i: usize, n_rows: *mut i64, nnz: *mut i64) -> c_int;
     pub fn fem_gpu_batch_get_csr(b: *mut FemGpuBatch, i: usize, row_ptr: *mut i64, col_idx: *mut i32, values: *mut f64) -> c_int;
