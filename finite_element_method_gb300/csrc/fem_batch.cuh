@@ -103,7 +103,7 @@ struct fem_gpu_batch {
   fem_gpu* un = nullptr;
   std::vector<size_t> cap_off, cap_n;
   DevBuf<int64_t> row_local;
-  double build_ms[5] = {0, 0, 0, 0, 0};  // fem_gpu_batch_create_from_arrays phase ends, ms from its start
+  double build_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // fem_gpu_batch_create_from_arrays phase ends, ms from its start
   BatchData d;
   cudaStream_t stream = nullptr;
   std::string err;

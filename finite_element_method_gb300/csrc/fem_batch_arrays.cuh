@@ -389,6 +389,8 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
     BAK(cudaMemcpyAsync(nidx.p, sidx.p, NN * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
   }
   BAK(cudaGetLastError());
+  BAK(cudaStreamSynchronize(s));
+  mark(0);
   // elements, kind by kind: numbers, nodes, properties, repeated numbers and node pairs / sets, validation
   const BaKind kinds[3] = {{kTruss, 2, in->truss_off, in->truss_numbers, in->truss_nodes},
                            {kBeam, 2, in->beam_off, in->beam_numbers, in->beam_nodes},
@@ -497,10 +499,11 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
     k_ba_status<<<grid_for(n, 256), 256, 0, s>>>(n, status.p, esid.p, d_fail.p);
     BAK(cudaGetLastError());
     BAK(cudaStreamSynchronize(s));  // the host offsets above are on this frame
+    mark(1 + k.kind);
   }
   BAK(cudaMemcpyAsync(fail.data(), d_fail.p, S * sizeof(int), cudaMemcpyDeviceToHost, s));
   BAK(cudaStreamSynchronize(s));
-  mark(0);
+  mark(4);
   for (size_t q = 0; q < S; ++q) {
     if (!fail[q]) continue;
     std::string msg;
@@ -516,10 +519,9 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
   h->append_run(kTruss, 0, NT);
   h->append_run(kBeam, 0, NB);
   h->append_run(kPlate, 0, NP);
-  mark(1);
   st = fem_gpu_assemble(h);
   if (st) return b->fail(st, "%s", h->err.c_str());
-  mark(2);
+  mark(5);
   // per structure: entry offsets, local columns and row starts
   std::vector<int64_t> zoff(S + 1);
   DevBuf<int64_t> d_zoff;
@@ -561,15 +563,15 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
   d.v_words = h->v_words;
   d.src_map = h->src_map.p;
   d.values = h->values.p;
-  mark(3);
+  mark(6);
   st = batch_make_graph(b);
-  mark(4);
+  mark(7);
   return st;
 }
 
 extern "C" int fem_gpu_batch_build_ms(const fem_gpu_batch_t* b, double* ms, size_t n) {
   if (!b || (n && !ms)) return FEM_GPU_ERR_ARGUMENT;
-  for (size_t k = 0; k < n && k < 5; ++k) ms[k] = b->build_ms[k];
+  for (size_t k = 0; k < n && k < 8; ++k) ms[k] = b->build_ms[k];
   return FEM_GPU_OK;
 }
 

@@ -722,10 +722,11 @@ class Batch:
         return st, keep
 
     def build_ms(self):
-        """host times (ms from the start) at the end of the phases of a batch built from arrays: uploads and
-        checks, union laid out, symbolic + first numeric pass, per-structure CSR offsets, graph captured"""
-        out = np.zeros(5)
-        self._check(self._L.fem_gpu_batch_build_ms(self._h, ptr(out, c_double), 5))
+        """host times (ms from the start) at the end of the phases of a batch built from arrays: nodes,
+        trusses, beams, plates uploaded and checked, checks read, symbolic + first numeric pass,
+        per-structure CSR offsets, graph captured"""
+        out = np.zeros(8)
+        self._check(self._L.fem_gpu_batch_build_ms(self._h, ptr(out, c_double), 8))
         return out
 
     def __len__(self) -> int:

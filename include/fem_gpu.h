@@ -267,9 +267,9 @@ typedef struct fem_gpu_structures {
 int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, const fem_gpu_structures_t* structures,
                                      fem_gpu_batch_t** out);
 /* Host times of the phases of fem_gpu_batch_create_from_arrays, ms from its start at the end of each:
- * [0] uploads and the bulk checks of every structure, [1] the union model laid out, [2] its symbolic phase
- * and first numeric pass, [3] per-structure columns and row starts, [4] the numeric pass captured as a
- * graph (all 0 for a batch of models).  At most n values. */
+ * [0] nodes uploaded and checked, [1] trusses, [2] beams, [3] plates uploaded and checked, [4] the checks'
+ * result read, [5] the union's symbolic phase and first numeric pass, [6] per-structure columns and row
+ * starts, [7] the numeric pass captured as a graph (all 0 for a batch of models).  At most n values. */
 int fem_gpu_batch_build_ms(const fem_gpu_batch_t* b, double* ms, size_t n);
 /* structures (or models) in the batch, and structure i's CSR: sizes, then host copies (any may be NULL) */
 int fem_gpu_batch_size(const fem_gpu_batch_t* b, size_t* n_structures);
