@@ -201,7 +201,7 @@ int batch_enqueue(fem_gpu_batch* b) {
                                                b->n_tiles, b->counter.p);
   } else {
     const unsigned bs = (unsigned)b->cfg.block;
-    if (b->np) k_plate<<<grid_for(b->np, bs), bs, 0, s>>>(d.nd, d.pv, b->abs_tol, b->np, sp);
+    if (b->np) k_plate<<<grid_for(b->np, bs), bs, plate_smem(sp, bs), s>>>(d.nd, d.pv, b->abs_tol, b->np, sp);
     if (b->nbm) k_beam<<<grid_for(b->nbm, bs), bs, 0, s>>>(d.nd, d.bv, b->rel_tol, b->abs_tol, b->nbm, sb);
     if (b->nt) k_truss<<<grid_for(b->nt, bs), bs, 0, s>>>(d.nd, d.tv, b->abs_tol, b->nt, st);
   }

@@ -392,7 +392,10 @@ struct BlockSink {
       mask[ep] = m;
       return;
     }
-    const unsigned long long pk = pack[ep];
+    put_pk(pack[ep], transpose, blk);
+  }
+  // numeric mode, the pair's scratch position and layout word already read
+  __device__ __forceinline__ void put_pk(unsigned long long pk, bool transpose, const double blk[36]) const {
     const uint32_t lay = (uint32_t)(pk >> 62);
     if (!dbg_in_range((pk & ((1ull << 62) - 1ull)) + (unsigned long long)lay_size(lay) - 1ull, v_words, kDbgScratch))
       return;
@@ -513,9 +516,12 @@ __global__ void __launch_bounds__(256) k_beam(NodesView nd, BeamView b, double r
   beam_element(e, nd, b, rel_tol, abs_tol, sink);
 }
 
-template <int I, int J>
+// node pair P = (I, J) of the plate; its scratch word comes from spk[P * spk_stride] when the caller staged the
+// plate's words in shared memory, else from the sink's array
+template <int I, int J, int P>
 __device__ __forceinline__ void plate_pair(const PlateCore& C, const double R[9], bool ident, const int nidx[4],
-                                           size_t ep, const BlockSink& sink) {
+                                           size_t e, const BlockSink& sink, const unsigned long long* spk,
+                                           unsigned spk_stride) {
   double blk[36];
   plate_block_ct<I, J>(C, blk);
   if (!ident) {
@@ -524,11 +530,25 @@ __device__ __forceinline__ void plate_pair(const PlateCore& C, const double R[9]
 #pragma unroll
     for (int k = 0; k < 36; ++k) blk[k] = o[k];
   }
-  sink.put(ep, I != J && nidx[I] > nidx[J], blk);
+  const bool transpose = I != J && nidx[I] > nidx[J];
+  if (spk)
+    sink.put_pk(spk[P * spk_stride], transpose, blk);
+  else
+    sink.put(e * kPairs4 + P, transpose, blk);
 }
 
+// 8-byte asynchronous copy global -> shared (each thread copies only words it reads itself, so waiting for its
+// own copies is enough: no barrier)
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 __device__ __forceinline__ void plate_element(size_t e, NodesView nd, const PlateView& pl, double abs_tol,
-                                              const BlockSink& sink) {
+                                              const BlockSink& sink, const unsigned long long* spk = nullptr,
+                                              unsigned spk_stride = 0) {
   int nidx[4] = {pl.n1[e], pl.n2[e], pl.n3[e], pl.n4[e]};
   double X[4][3];
 #pragma unroll
@@ -540,18 +560,18 @@ __device__ __forceinline__ void plate_element(size_t e, NodesView nd, const Plat
   plate_local_xy(X, R, ident, xl, yl);
   PlateCore C;
   plate_core(xl, yl, pl.E[e], pl.nu[e], pl.t[e], pl.ks[e], C);
-  const size_t ep = e * kPairs4;
+  if (spk) cp_async_wait_all();
   // node pairs in the order of pair_nodes4
-  plate_pair<0, 0>(C, R, ident, nidx, ep + 0, sink);
-  plate_pair<0, 1>(C, R, ident, nidx, ep + 1, sink);
-  plate_pair<0, 2>(C, R, ident, nidx, ep + 2, sink);
-  plate_pair<0, 3>(C, R, ident, nidx, ep + 3, sink);
-  plate_pair<1, 1>(C, R, ident, nidx, ep + 4, sink);
-  plate_pair<1, 2>(C, R, ident, nidx, ep + 5, sink);
-  plate_pair<1, 3>(C, R, ident, nidx, ep + 6, sink);
-  plate_pair<2, 2>(C, R, ident, nidx, ep + 7, sink);
-  plate_pair<2, 3>(C, R, ident, nidx, ep + 8, sink);
-  plate_pair<3, 3>(C, R, ident, nidx, ep + 9, sink);
+  plate_pair<0, 0, 0>(C, R, ident, nidx, e, sink, spk, spk_stride);
+  plate_pair<0, 1, 1>(C, R, ident, nidx, e, sink, spk, spk_stride);
+  plate_pair<0, 2, 2>(C, R, ident, nidx, e, sink, spk, spk_stride);
+  plate_pair<0, 3, 3>(C, R, ident, nidx, e, sink, spk, spk_stride);
+  plate_pair<1, 1, 4>(C, R, ident, nidx, e, sink, spk, spk_stride);
+  plate_pair<1, 2, 5>(C, R, ident, nidx, e, sink, spk, spk_stride);
+  plate_pair<1, 3, 6>(C, R, ident, nidx, e, sink, spk, spk_stride);
+  plate_pair<2, 2, 7>(C, R, ident, nidx, e, sink, spk, spk_stride);
+  plate_pair<2, 3, 8>(C, R, ident, nidx, e, sink, spk, spk_stride);
+  plate_pair<3, 3, 9>(C, R, ident, nidx, e, sink, spk, spk_stride);
 }
 
 // Launch shape of the plate kernel.  FEM_PLATE_BLOCK threads per CTA (64 by default: at 254 registers a
@@ -567,9 +587,23 @@ __global__ void __launch_bounds__(256)
 #endif
 k_plate(NodesView nd, PlateView pl, double abs_tol, size_t count,
                                                BlockSink sink) {
+  // numeric mode: the plate's ten scratch words are copied to shared memory ([pair][thread], dynamic, sized
+  // kPairs4 x blockDim.x by plate_smem) while the element arithmetic runs, instead of being loaded at each store
+  extern __shared__ unsigned long long s_pack[];
   size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (e >= count) return;
-  plate_element(e, nd, pl, abs_tol, sink);
+  const unsigned long long* spk = nullptr;
+  if (sink.pack) {
+#pragma unroll
+    for (int p = 0; p < kPairs4; ++p) cp_async8(&s_pack[p * blockDim.x + threadIdx.x], sink.pack + e * kPairs4 + p);
+    cp_async_commit();
+    spk = &s_pack[threadIdx.x];
+  }
+  plate_element(e, nd, pl, abs_tol, sink, spk, blockDim.x);
+}
+// dynamic shared memory of a k_plate launch of `block` threads
+size_t plate_smem(const BlockSink& sink, unsigned block) {
+  return sink.pack ? (size_t)kPairs4 * block * sizeof(unsigned long long) : 0;
 }
 
 // sorted position k: record the element pair's slot and its mask
@@ -2772,8 +2806,8 @@ int launch_elements(fem_gpu* h, BlockSink sink_t, BlockSink sink_b, BlockSink si
   if (h->nbm)
     k_beam<<<grid_for(h->nbm, 128), 128, 0, h->stream>>>(nd, h->beams(), h->rel_tol, h->abs_tol, h->nbm, sink_b);
   if (h->np)
-    k_plate<<<grid_for(h->np, FEM_PLATE_BLOCK), FEM_PLATE_BLOCK, 0, h->stream>>>(nd, h->plates(), h->abs_tol, h->np,
-                                                                              sink_p);
+    k_plate<<<grid_for(h->np, FEM_PLATE_BLOCK), FEM_PLATE_BLOCK, plate_smem(sink_p, FEM_PLATE_BLOCK), h->stream>>>(
+        nd, h->plates(), h->abs_tol, h->np, sink_p);
   CK(cudaGetLastError());
   return FEM_GPU_OK;
 }
