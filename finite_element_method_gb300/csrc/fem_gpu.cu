@@ -364,6 +364,10 @@ constexpr uint64_t kSetOff13 = (1ull << 0) | (1ull << 1) | (1ull << 6) | (1ull <
                                (1ull << 27) | (1ull << 28);
 constexpr uint64_t kSetDiag14 = kSetOff13 | (1ull << 35);
 __host__ __device__ constexpr int lay_size(uint32_t lay) { return lay == kLayFull ? 36 : lay == kLayDiag14 ? 14 : 13; }
+// doubles one contribution occupies: the 13-entry packing is padded to 14 (its 14th word holds the block's
+// entry 35, which is zero for such a block), so every contribution starts on a 16-byte boundary and is
+// written with 16-byte stores
+__host__ __device__ constexpr int lay_stride(uint32_t lay) { return lay == kLayFull ? 36 : 14; }
 
 // a 6x6 block in element orientation -> destination, transposed (to the
 // block's (lower node, higher node) orientation) when the element's first node
@@ -397,12 +401,17 @@ struct BlockSink {
   // numeric mode, the pair's scratch position and layout word already read
   __device__ __forceinline__ void put_pk(unsigned long long pk, bool transpose, const double blk[36]) const {
     const uint32_t lay = (uint32_t)(pk >> 62);
-    if (!dbg_in_range((pk & ((1ull << 62) - 1ull)) + (unsigned long long)lay_size(lay) - 1ull, v_words, kDbgScratch))
+    if (!dbg_in_range((pk & ((1ull << 62) - 1ull)) + (unsigned long long)lay_stride(lay) - 1ull, v_words, kDbgScratch))
       return;
-    double* dst = V + (pk & ((1ull << 62) - 1ull));
+    // 16-byte aligned: V is, and every contribution's offset is even
+    double2* dst = reinterpret_cast<double2*>(V + (pk & ((1ull << 62) - 1ull)));
     if (lay == kLayFull) {
 #pragma unroll
-      for (int en = 0; en < 36; ++en) dst[en] = transpose ? blk[6 * (en % 6) + en / 6] : blk[en];
+      for (int q = 0; q < 18; ++q) {
+        const int e0 = 2 * q, e1 = 2 * q + 1;
+        dst[q] = transpose ? make_double2(blk[6 * (e0 % 6) + e0 / 6], blk[6 * (e1 % 6) + e1 / 6])
+                           : make_double2(blk[e0], blk[e1]);
+      }
       return;
     }
     // structural packings: the set is symmetric, so a transposed block packs its
@@ -414,13 +423,15 @@ struct BlockSink {
       bool in = (kSetOff13 >> en) & 1ull;
       if (!in && en != 35) outside |= nonzero(blk[en]);
     }
+    double w[14];
 #pragma unroll
-    for (int j = 0; j < 13; ++j) {
+    for (int j = 0; j < 14; ++j) {
       const int en = order[j];
-      dst[j] = transpose ? blk[6 * (en % 6) + en / 6] : blk[en];
+      w[j] = transpose ? blk[6 * (en % 6) + en / 6] : blk[en];
     }
-    if (lay == kLayDiag14) dst[13] = blk[35];
-    else outside |= nonzero(blk[35]);
+#pragma unroll
+    for (int q = 0; q < 7; ++q) dst[q] = make_double2(w[2 * q], w[2 * q + 1]);
+    if (lay != kLayDiag14) outside |= nonzero(blk[35]);
     if (outside) atomicOr(flag, 1);
   }
 };
@@ -517,14 +528,15 @@ __global__ void __launch_bounds__(256) k_beam(NodesView nd, BeamView b, double r
 }
 
 // node pair P = (I, J) of the plate; its scratch word comes from spk[P * spk_stride] when the caller staged the
-// plate's words in shared memory, else from the sink's array
-template <int I, int J, int P>
-__device__ __forceinline__ void plate_pair(const PlateCore& C, const double R[9], bool ident, const int nidx[4],
-                                           size_t e, const BlockSink& sink, const unsigned long long* spk,
-                                           unsigned spk_stride) {
+// plate's words in shared memory, else from the sink's array.  IDENT (R = I) is a template argument so that the
+// identity path keeps the local block's structural zeros as compile-time zeros (no rotation, no merge with the
+// rotated values, no run-time tests of entries known to be zero).
+template <int I, int J, int P, bool IDENT>
+__device__ __forceinline__ void plate_pair(const PlateCore& C, const double R[9], const int nidx[4], size_t e,
+                                           const BlockSink& sink, const unsigned long long* spk, unsigned spk_stride) {
   double blk[36];
   plate_block_ct<I, J>(C, blk);
-  if (!ident) {
+  if constexpr (!IDENT) {
     double o[36];
     plate_rotate_block_ct<I == J>(R, blk, o);
 #pragma unroll
@@ -535,6 +547,22 @@ __device__ __forceinline__ void plate_pair(const PlateCore& C, const double R[9]
     sink.put_pk(spk[P * spk_stride], transpose, blk);
   else
     sink.put(e * kPairs4 + P, transpose, blk);
+}
+
+// the ten node pairs in the order of pair_nodes4
+template <bool IDENT>
+__device__ __forceinline__ void plate_pairs(const PlateCore& C, const double R[9], const int nidx[4], size_t e,
+                                            const BlockSink& sink, const unsigned long long* spk, unsigned stride) {
+  plate_pair<0, 0, 0, IDENT>(C, R, nidx, e, sink, spk, stride);
+  plate_pair<0, 1, 1, IDENT>(C, R, nidx, e, sink, spk, stride);
+  plate_pair<0, 2, 2, IDENT>(C, R, nidx, e, sink, spk, stride);
+  plate_pair<0, 3, 3, IDENT>(C, R, nidx, e, sink, spk, stride);
+  plate_pair<1, 1, 4, IDENT>(C, R, nidx, e, sink, spk, stride);
+  plate_pair<1, 2, 5, IDENT>(C, R, nidx, e, sink, spk, stride);
+  plate_pair<1, 3, 6, IDENT>(C, R, nidx, e, sink, spk, stride);
+  plate_pair<2, 2, 7, IDENT>(C, R, nidx, e, sink, spk, stride);
+  plate_pair<2, 3, 8, IDENT>(C, R, nidx, e, sink, spk, stride);
+  plate_pair<3, 3, 9, IDENT>(C, R, nidx, e, sink, spk, stride);
 }
 
 // 8-byte asynchronous copy global -> shared (each thread copies only words it reads itself, so waiting for its
@@ -561,17 +589,10 @@ __device__ __forceinline__ void plate_element(size_t e, NodesView nd, const Plat
   PlateCore C;
   plate_core(xl, yl, pl.E[e], pl.nu[e], pl.t[e], pl.ks[e], C);
   if (spk) cp_async_wait_all();
-  // node pairs in the order of pair_nodes4
-  plate_pair<0, 0, 0>(C, R, ident, nidx, e, sink, spk, spk_stride);
-  plate_pair<0, 1, 1>(C, R, ident, nidx, e, sink, spk, spk_stride);
-  plate_pair<0, 2, 2>(C, R, ident, nidx, e, sink, spk, spk_stride);
-  plate_pair<0, 3, 3>(C, R, ident, nidx, e, sink, spk, spk_stride);
-  plate_pair<1, 1, 4>(C, R, ident, nidx, e, sink, spk, spk_stride);
-  plate_pair<1, 2, 5>(C, R, ident, nidx, e, sink, spk, spk_stride);
-  plate_pair<1, 3, 6>(C, R, ident, nidx, e, sink, spk, spk_stride);
-  plate_pair<2, 2, 7>(C, R, ident, nidx, e, sink, spk, spk_stride);
-  plate_pair<2, 3, 8>(C, R, ident, nidx, e, sink, spk, spk_stride);
-  plate_pair<3, 3, 9>(C, R, ident, nidx, e, sink, spk, spk_stride);
+  if (ident)
+    plate_pairs<true>(C, R, nidx, e, sink, spk, spk_stride);
+  else
+    plate_pairs<false>(C, R, nidx, e, sink, spk, spk_stride);
 }
 
 // Launch shape of the plate kernel.  FEM_PLATE_BLOCK threads per CTA (64 by default: at 254 registers a
@@ -716,28 +737,41 @@ __global__ void k_row_counts(size_t n_nodes, const int32_t* __restrict__ seg_beg
 // ---------------------------------------------------------------------------
 // compacted scratch layout
 // ---------------------------------------------------------------------------
-// Block b stores count_b contributions of c_b = popcount(mask_b) doubles each,
+// Block b stores count_b contributions of lay_stride(layout_b) doubles each,
 // contiguous and in element order, at blk_voff[b] (an exclusive scan of
-// count_b * c_b).
+// count_b * lay_stride).
 __global__ void k_block_sizes(size_t nb, const uint32_t* __restrict__ blk_count, const uint64_t* __restrict__ blk_mask,
                               const int32_t* __restrict__ blk_I, const int32_t* __restrict__ blk_J, uint8_t* blk_lay,
-                              uint64_t* blk_pmask, unsigned long long* sizes) {
-  size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (b >= nb) return;
-  const uint64_t m = blk_mask[b];
-  uint32_t lay = kLayFull;
-  if (blk_I[b] == blk_J[b]) {
-    if ((m & ~kSetDiag14) == 0) lay = kLayDiag14;
-  } else if ((m & ~kSetOff13) == 0) {
-    lay = kLayOff13;
+                              uint64_t* blk_pmask, unsigned long long* sizes, unsigned long long* pad_words) {
+  const size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  unsigned pad = 0;
+  if (b < nb) {
+    const uint64_t m = blk_mask[b];
+    uint32_t lay = kLayFull;
+    if (blk_I[b] == blk_J[b]) {
+      if ((m & ~kSetDiag14) == 0) lay = kLayDiag14;
+    } else if ((m & ~kSetOff13) == 0) {
+      lay = kLayOff13;
+    }
+    blk_lay[b] = (uint8_t)lay;
+    // the pattern over packed positions: bit j set when packed entry j is a pattern entry
+    uint64_t pm = 0;
+    for (int j = 0; j < lay_size(lay); ++j)
+      if ((m >> c_lay_en[lay][j]) & 1ull) pm |= 1ull << j;
+    blk_pmask[b] = pm;
+    sizes[b] = (unsigned long long)blk_count[b] * (unsigned long long)lay_stride(lay);
+    pad = (unsigned)(lay_stride(lay) - lay_size(lay)) * blk_count[b];
   }
-  blk_lay[b] = (uint8_t)lay;
-  // the pattern over packed positions: bit j set when packed entry j is a pattern entry
-  uint64_t pm = 0;
-  for (int j = 0; j < lay_size(lay); ++j)
-    if ((m >> c_lay_en[lay][j]) & 1ull) pm |= 1ull << j;
-  blk_pmask[b] = pm;
-  sizes[b] = (unsigned long long)blk_count[b] * (unsigned long long)lay_size(lay);
+  // padding words of the CTA's blocks, one atomic per CTA (blockDim.x = 256)
+  __shared__ unsigned long long warp_pad[8];
+  const unsigned wsum = __reduce_add_sync(0xffffffffu, pad);
+  if ((threadIdx.x & 31) == 0) warp_pad[threadIdx.x >> 5] = wsum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += warp_pad[w];
+    if (t) atomicAdd(pad_words, t);
+  }
 }
 
 // per element pair: its packed offset in V (low 62 bits) and the block's packing (top 2 bits)
@@ -751,7 +785,7 @@ __global__ void k_pair_offsets(const uint32_t* __restrict__ svals, const uint32_
   uint32_t kind = v >> 30, idx = v & 0x3fffffffu;
   uint32_t b = incl[k] - 1;
   const uint32_t lay = blk_lay[b];
-  unsigned long long off = blk_voff[b] + (unsigned long long)(k - blk_start[b]) * (unsigned long long)lay_size(lay);
+  unsigned long long off = blk_voff[b] + (unsigned long long)(k - blk_start[b]) * (unsigned long long)lay_stride(lay);
   off |= (unsigned long long)lay << 62;
   if (kind == kTruss) pk_t[idx] = off;
   else if (kind == kBeam) pk_b[idx] = off;
@@ -907,8 +941,8 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
 }
 
 // Symbolic, once per pattern: the descriptors -- the scratch position of the
-// first contribution, the number of contributions (bits 0-23), the packed
-// block size, i.e. the stride between contributions (bits 24-30), and whether
+// first contribution, the number of contributions (bits 0-23), the stride
+// between contributions (bits 24-30: lay_stride), and whether
 // the entry is a pattern entry (bit 31).
 __global__ void k_slot_desc(size_t nb, const uint32_t* __restrict__ blk_count, const uint64_t* __restrict__ blk_pmask,
                             const uint8_t* __restrict__ blk_lay, const unsigned long long* __restrict__ blk_voff,
@@ -921,7 +955,7 @@ __global__ void k_slot_desc(size_t nb, const uint32_t* __restrict__ blk_count, c
   const uint64_t pm = blk_pmask[b];
   const int cat = slot_cat(cnt);
   const unsigned long long voff = blk_voff[b];
-  const uint32_t hi = (cnt & 0xffffffu) | ((uint32_t)c << 24);
+  const uint32_t hi = (cnt & 0xffffffu) | ((uint32_t)lay_stride(blk_lay[b]) << 24);
   if (cat == 0) {
     // one contribution: pattern entries are gathered straight from the scratch; the others get a check
     unsigned long long at = L.off[0] + L.base[b];
@@ -1539,6 +1573,7 @@ struct fem_gpu {
   DevBuf<uint2> slot_desc;           // per slot: scratch start, count | stride << 24 | in-pattern << 31
   size_t s_words = 0;
   size_t v_words = 0;
+  size_t v_pad = 0;    // of which padding words (never read: one per contribution of a 13-entry block)
   DevBuf<double> V;
   DevBuf<uint32_t> blk_start, blk_count;
   DevBuf<uint64_t> blk_mask, blk_maskT;
@@ -2957,19 +2992,20 @@ int symbolic(fem_gpu* h) {
   // compacted scratch: block offsets and, per element pair, its offset and mask
   {
     DevBuf<unsigned long long> sizes;
-    CK(sizes.reserve(nb + 1, s));
+    CK(sizes.reserve(nb + 2, s));
     CK(h->blk_voff.reserve(nb + 1, s));
     CK(h->blk_lay.reserve(nb + 1, s));
-    CK(cudaMemsetAsync(sizes.p + nb, 0, sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(sizes.p + nb, 0, 2 * sizeof(unsigned long long), s));  // the scan's tail, the padding count
     CK(h->blk_pmask.reserve(nb + 1, s));
     k_block_sizes<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_mask.p, h->blk_I.p, h->blk_J.p,
-                                                    h->blk_lay.p, h->blk_pmask.p, sizes.p);
+                                                    h->blk_lay.p, h->blk_pmask.p, sizes.p, sizes.p + nb + 1);
     st = cub_call(h, [&](void* tmp, size_t& bytes) {
       return cub::DeviceScan::ExclusiveSum(tmp, bytes, sizes.p, h->blk_voff.p, (int64_t)(nb + 1), s);
     });
     if (st) return st;
-    unsigned long long total = 0;
+    unsigned long long total = 0, pads = 0;
     CK(cudaMemcpyAsync(&total, h->blk_voff.p + nb, sizeof total, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&pads, sizes.p + nb + 1, sizeof pads, cudaMemcpyDeviceToHost, s));
     CK(h->off_t.reserve(h->nt * kPairs2 + 1, s));
     CK(h->off_b.reserve(h->nbm * kPairs2 + 1, s));
     CK(h->off_p.reserve(h->np * kPairs4 + 1, s));
@@ -2978,6 +3014,7 @@ int symbolic(fem_gpu* h) {
     CK(cudaStreamSynchronize(s));
     sizes.release();
     h->v_words = (size_t)total;
+    h->v_pad = (size_t)pads;
   }
   uint32_t last_off = 0, last_n = 0;
   CK(cudaMemcpyAsync(&last_off, adj_off.p + nb - 1, sizeof last_off, cudaMemcpyDeviceToHost, s));
@@ -3381,7 +3418,7 @@ extern "C" int fem_gpu_get_pattern_stats(fem_gpu_t* h, int64_t* n_blocks, int64_
   if (!h->pattern_valid) return h->fail(FEM_GPU_ERR_STATE, "call fem_gpu_assemble first");
   if (n_blocks) *n_blocks = (int64_t)h->n_blocks;
   if (n_contributions) *n_contributions = (int64_t)h->n_pairs;
-  if (scratch_doubles) *scratch_doubles = (int64_t)h->v_words;
+  if (scratch_doubles) *scratch_doubles = (int64_t)(h->v_words - h->v_pad);
   if (sum_slots) *sum_slots = (int64_t)h->s_words;
   return FEM_GPU_OK;
 }

@@ -168,8 +168,10 @@ int fem_gpu_numeric_launch_count(fem_gpu_t* h, int* n_launches);
 int fem_gpu_debug_check(int* checked, int* site, int64_t* index, int64_t* bound);
 
 /* Sizes of the stored pattern: global node-pair blocks, element node-pair
- * contributions, doubles of packed element-block scratch one numeric pass
- * writes and reads, and packed block-sum slots the CSR values are gathered from. */
+ * contributions, packed element-block entries one numeric pass writes and reads
+ * (the scratch also holds one padding word per contribution of a 13-entry
+ * block, written with it and never read), and packed block-sum slots the CSR
+ * values are gathered from. */
 int fem_gpu_get_pattern_stats(fem_gpu_t* h, int64_t* n_blocks, int64_t* n_contributions, int64_t* scratch_doubles,
                               int64_t* sum_slots);
 
