@@ -1026,37 +1026,36 @@ __global__ void __launch_bounds__(512) k_block_sums(size_t n_desc, size_t n_sums
 
 // Numeric pass, part 2: CSR values in storage order, each read from its source
 // (the scratch for one-contribution entries, S otherwise; S starts at vs_off of
-// the same buffer); eight consecutive entries per thread so their loads
-// overlap.  A one-contribution pattern entry that reads zero raises kFlagPattern.
+// the same buffer).  A warp takes 32 x kGatherPerThread consecutive entries and
+// lane t entries t, t + 32, ...: every load of the source map and every store of
+// the values is one contiguous warp access, and neighbouring entries of a row
+// (neighbouring sources) sit in neighbouring lanes.  A one-contribution pattern
+// entry that reads zero raises kFlagPattern.
 constexpr int kGatherPerThread = 8;
 __global__ void __launch_bounds__(512) k_gather_values(size_t nnz, const uint32_t* __restrict__ src_map,
                                                        const double* __restrict__ VS, unsigned long long vs_off,
                                                        double* __restrict__ values, int* flag,
                                                        unsigned long long vs_end) {
-  const size_t k0 = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) * kGatherPerThread;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t k0 = (t >> 5) * (32 * kGatherPerThread) + (t & 31);
   if (k0 >= nnz) return;
   bool zero_direct = false;
-  if (k0 + kGatherPerThread <= nnz) {
-    // src_map and values are 256-byte aligned and k0 % 8 == 0
-    const uint4 s0 = reinterpret_cast<const uint4*>(src_map + k0)[0];
-    const uint4 s1 = reinterpret_cast<const uint4*>(src_map + k0)[1];
-    const uint32_t sx[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
-    double a[8];
+  uint32_t sx[kGatherPerThread];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) a[q] = dbg_in_range(sx[q], vs_end, kDbgGatherSource) ? VS[sx[q]] : 0.0;
+  for (int q = 0; q < kGatherPerThread; ++q) {
+    const size_t k = k0 + 32 * (size_t)q;
+    sx[q] = k < nnz ? src_map[k] : 0u;
+  }
+  double a[kGatherPerThread];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) zero_direct |= sx[q] < vs_off && !nonzero(a[q]);
-    double2* out = reinterpret_cast<double2*>(values + k0);
-    out[0] = make_double2(a[0], a[1]);
-    out[1] = make_double2(a[2], a[3]);
-    out[2] = make_double2(a[4], a[5]);
-    out[3] = make_double2(a[6], a[7]);
-  } else {
-    for (size_t k = k0; k < nnz; ++k) {
-      const uint32_t sx = src_map[k];
-      const double v = dbg_in_range(sx, vs_end, kDbgGatherSource) ? VS[sx] : 0.0;
-      zero_direct |= sx < vs_off && !nonzero(v);
-      values[k] = v;
+  for (int q = 0; q < kGatherPerThread; ++q)
+    a[q] = (k0 + 32 * (size_t)q < nnz && dbg_in_range(sx[q], vs_end, kDbgGatherSource)) ? VS[sx[q]] : 0.0;
+#pragma unroll
+  for (int q = 0; q < kGatherPerThread; ++q) {
+    const size_t k = k0 + 32 * (size_t)q;
+    if (k < nnz) {
+      zero_direct |= sx[q] < vs_off && !nonzero(a[q]);
+      values[k] = a[q];
     }
   }
   if (zero_direct) atomicOr(flag, kFlagPattern);
