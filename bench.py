@@ -72,9 +72,9 @@ def element_flops(workload, mesh):
 # bytes per element read by the element kernel (connectivity, coordinates of its nodes, properties)
 IN_BYTES = {"plate": 4 * 4 + 4 * 24 + 4 * 8, "beam": 2 * 4 + 2 * 24 + 11 * 8, "truss": 2 * 4 + 2 * 24 + 3 * 8}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per element of one launch of the element kernel,
-# from an ncu capture of k_plate on the 500 x 500 plate mesh (250,000 plates: 55.7 MB read + 242.3 MB written),
+# from an ncu capture of k_plate on the 500 x 500 plate mesh (250,000 plates: 46.4 MB read + 230.4 MB written),
 # scaled by the element count (the kernel's traffic is per element: its inputs and its packed blocks)
-TRAFFIC_PER_ELEMENT = {"plate": (55675392 + 242335232) / 250000}
+TRAFFIC_PER_ELEMENT = {"plate": (46394368 + 230444800) / 250000}
 
 
 def measured_peaks():
