@@ -1593,9 +1593,11 @@ struct fem_gpu {
   // a second stream for pattern read-backs that overlap the numeric pass (fem_gpu_assemble_to_host)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t copy_ev = nullptr;
+  bool num_eager_done = false;  // the first numeric pass since the graph was dropped has run (uncaptured)
   void drop_numeric_graph() {
     if (num_graph) cudaGraphExecDestroy(num_graph);
     num_graph = nullptr;
+    num_eager_done = false;
   }
   // vector-Jacobian product
   bool vjp_inc_valid = false;
@@ -2847,15 +2849,19 @@ int launch_elements(fem_gpu* h, BlockSink sink_t, BlockSink sink_b, BlockSink si
 }
 
 // the numeric pass's operations (captured into the handle's graph); the phase events are graph nodes
-int numeric_enqueue(fem_gpu* h) {
+int numeric_enqueue(fem_gpu* h, bool captured) {
+  // phase events: graph nodes when captured, plain records otherwise
+  auto mark = [&](cudaEvent_t ev) {
+    return captured ? cudaEventRecordWithFlags(ev, h->stream, cudaEventRecordExternal) : cudaEventRecord(ev, h->stream);
+  };
   CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), h->stream));
-  CK(cudaEventRecordWithFlags(h->ev[0], h->stream, cudaEventRecordExternal));
+  CK(mark(h->ev[0]));
   BlockSink st{nullptr, h->V.p, h->off_t.p, h->flag.p, h->v_words};
   BlockSink sb{nullptr, h->V.p, h->off_b.p, h->flag.p, h->v_words};
   BlockSink sp{nullptr, h->V.p, h->off_p.p, h->flag.p, h->v_words};
   int r = launch_elements(h, st, sb, sp);
   if (r) return r;
-  CK(cudaEventRecordWithFlags(h->ev[1], h->stream, cudaEventRecordExternal));
+  CK(mark(h->ev[1]));
   if (h->n_blocks) {
     if (h->n_desc)
       k_block_sums<<<grid_for(h->n_desc, 256), 256, 0, h->stream>>>(h->n_desc, h->s_words, h->slot_desc.p, h->V.p,
@@ -2865,18 +2871,28 @@ int numeric_enqueue(fem_gpu* h) {
                                    h->vs_off + h->s_words);
   }
   CK(cudaGetLastError());
-  CK(cudaEventRecordWithFlags(h->ev[2], h->stream, cudaEventRecordExternal));
+  CK(mark(h->ev[2]));
   return FEM_GPU_OK;
 }
 
-// One numeric pass: a single graph launch (the pass's arrays keep their addresses until the next
+// One numeric pass: the first after a symbolic phase runs its kernels directly, later ones are a single graph
+// launch (the pass's arrays keep their addresses until the next
 // symbolic phase, which drops the graph)
 int numeric_launch(fem_gpu* h) {
   h->sep_valid = false;  // a separation describes the stiffness it was taken from
   h->sell_valid = false;
+  if (!h->num_graph && !h->num_eager_done) {
+    // the first pass after a symbolic phase runs its kernels directly: capturing and instantiating the
+    // graph costs host time the single assemble of a new model would wait for; the next pass captures it
+    h->num_eager_done = true;
+    const int r = numeric_enqueue(h, false);
+    if (r) return r;
+    h->numeric_done = true;
+    return FEM_GPU_OK;
+  }
   if (!h->num_graph) {
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    const int r = numeric_enqueue(h);
+    const int r = numeric_enqueue(h, true);
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     if (r) {
