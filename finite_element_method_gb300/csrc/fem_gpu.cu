@@ -857,7 +857,7 @@ __device__ __forceinline__ int seg_inclusive_sum(int v) {
 // block-sum slot in S -- both in one buffer, S starting at vs_off).  A block
 // stored with the row node second (t = 1) is read transposed.  The node's
 // groups are placed the same way.
-__global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin, const int32_t* __restrict__ seg_end,
+__global__ void k_row_fill(size_t node0, size_t n_nodes, const int32_t* __restrict__ seg_begin, const int32_t* __restrict__ seg_end,
                            const uint64_t* __restrict__ akeys, int kb, const uint32_t* __restrict__ avals,
                            const uint64_t* __restrict__ blk_mask, const uint64_t* __restrict__ blk_maskT,
                            const uint8_t* __restrict__ blk_lay, const uint32_t* __restrict__ blk_count,
@@ -867,7 +867,7 @@ __global__ void k_row_fill(size_t n_nodes, const int32_t* __restrict__ seg_begin
                            uint32_t* __restrict__ src_map, int32_t* __restrict__ g_row, int32_t* __restrict__ g_col,
                            uint8_t* __restrict__ g_kind, unsigned long long nnz, unsigned long long n_groups,
                            unsigned long long vs_end) {
-  const size_t r = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) / kRowLanes;
+  const size_t r = node0 + (blockIdx.x * (size_t)blockDim.x + threadIdx.x) / kRowLanes;
   const int lane = (int)(threadIdx.x & (kRowLanes - 1));
   // every lane stays for the shuffles: a node past the end or without blocks has an empty range
   int32_t s = 0, e = 0;
@@ -1593,6 +1593,7 @@ struct fem_gpu {
   // a second stream for pattern read-backs that overlap the numeric pass (fem_gpu_assemble_to_host)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t copy_ev = nullptr;
+  cudaEvent_t fill_ev[4] = {};  // the row fill's node chunks done (their columns can go back)
   bool num_eager_done = false;  // the first numeric pass since the graph was dropped has run (uncaptured)
   void drop_numeric_graph() {
     if (num_graph) cudaGraphExecDestroy(num_graph);
@@ -1881,7 +1882,7 @@ int ensure_ready(fem_gpu* h) {
   CK(h->dx.reserve(nn, h->stream));
   CK(h->dy.reserve(nn, h->stream));
   CK(h->dz.reserve(nn, h->stream));
-  CK(h->flag.reserve(1, h->stream));
+  CK(h->flag.reserve(2, h->stream));  // [0] numeric pass, [1] symbolic phase
   return FEM_GPU_OK;
 }
 
@@ -1977,6 +1978,8 @@ extern "C" int fem_gpu_destroy(fem_gpu_t* h) {
   h->res_buf.release();
   h->drop_numeric_graph();
   if (h->copy_ev) cudaEventDestroy(h->copy_ev);
+  for (auto& ev : h->fill_ev)
+    if (ev) cudaEventDestroy(ev);
   if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   for (auto& ev : h->ev)
     if (ev) cudaEventDestroy(ev);
@@ -2913,7 +2916,19 @@ int numeric_launch(fem_gpu* h) {
 }
 
 
-int symbolic(fem_gpu* h) {
+// Host buffers a caller wants the pattern read back into (fem_gpu_assemble_to_host): the symbolic phase sends
+// row_ptr back once the rows are counted and the columns in node chunks as the row fill finishes each, on the
+// copy stream, so the host link starts on the pattern before the phase ends.
+struct PatternCopy {
+  int64_t* row_ptr;
+  int32_t* col_idx;
+  int64_t capacity;     // entries col_idx has room for (nothing is sent when the pattern is larger)
+  bool issued = false;  // set when the copies were enqueued
+};
+constexpr int kFillChunks = 4;
+const char* const kTooManyMsg = "a node pair is shared by 2^24 or more elements";
+
+int symbolic(fem_gpu* h, PatternCopy* pc = nullptr) {
   h->drop_numeric_graph();
   cudaStream_t s = h->stream;
   size_t np = h->n_pairs;
@@ -3075,9 +3090,20 @@ int symbolic(fem_gpu* h) {
   int64_t nnz = 0, ng = 0;
   CK(cudaMemcpyAsync(&nnz, h->row_ptr.p + nrows, sizeof nnz, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(&ng, gbase.p + nn, sizeof ng, cudaMemcpyDeviceToHost, s));
+  // node chunks of the row fill and their first entries
+  size_t fill_node[kFillChunks + 1];
+  int64_t fill_entry[kFillChunks + 1];
+  for (int c = 0; c <= kFillChunks; ++c) {
+    fill_node[c] = nn * (size_t)c / kFillChunks;
+    fill_entry[c] = 0;
+    if (pc && c > 0 && c < kFillChunks)
+      CK(cudaMemcpyAsync(&fill_entry[c], h->row_ptr.p + 6 * fill_node[c], sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  }
   CK(cudaStreamSynchronize(s));
   h->nnz = nnz;
   h->n_groups = ng;
+  fill_entry[kFillChunks] = nnz;
+  const bool early = pc && h->copy_stream && nnz <= pc->capacity;
   CK(h->col_idx.reserve(nnz + 1, s));
   CK(h->values.reserve(nnz + 1, s));
   CK(h->nnz_group.reserve(nnz + 1, s));
@@ -3123,23 +3149,49 @@ int symbolic(fem_gpu* h) {
     for (int g = 0; g < kSlotCats; ++g) L.off[g] = h->slot_off[g];
     L.vs_off = h->vs_off;
     CK(h->slot_desc.reserve(h->n_desc + 1, s));
-    CK(cudaMemsetAsync(h->flag.p, 0, sizeof(int), s));
+    CK(cudaMemsetAsync(h->flag.p + 1, 0, sizeof(int), s));
+    if (early) {
+      // row_ptr is final: it goes back while the slots and columns are made.  From here on the phase makes no
+      // device-to-host read on its own stream (one would queue behind these copies on the copy engine).
+      CK(cudaEventRecord(h->copy_ev, s));
+      CK(cudaStreamWaitEvent(h->copy_stream, h->copy_ev, 0));
+      CK(cudaMemcpyAsync(pc->row_ptr, h->row_ptr.p, (nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                         h->copy_stream));
+    }
     k_slot_desc<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_count.p, h->blk_pmask.p, h->blk_lay.p, h->blk_voff.p, L,
-                                                  h->slot_desc.p, h->flag.p);
-    k_row_fill<<<grid_for(nn * kRowLanes, 256), 256, 0, s>>>(nn, seg_b.p, seg_e.p, sakeys.p, kb, savals.p, h->blk_mask.p,
-                                                    h->blk_maskT.p, h->blk_lay.p, h->blk_count.p, h->blk_voff.p, L,
-                                                    h->row_ptr.p, gbase.p, h->col_idx.p, h->nnz_group.p,
-                                                    h->src_map.p, h->g_row.p, h->g_col.p, h->g_kind.p,
-                                                             (unsigned long long)nnz, (unsigned long long)ng,
-                                                             h->vs_off + h->s_words);
+                                                  h->slot_desc.p, h->flag.p + 1);
+    // the rows in node chunks when the columns go back early (each chunk's columns follow it on the copy
+    // stream), else in one launch
+    const int chunks = early ? kFillChunks : 1;
+    for (int c = 0; c < chunks; ++c) {
+      const size_t n0 = early ? fill_node[c] : 0, n1 = early ? fill_node[c + 1] : nn;
+      if (n1 > n0)
+        k_row_fill<<<grid_for((n1 - n0) * kRowLanes, 256), 256, 0, s>>>(
+            n0, n1, seg_b.p, seg_e.p, sakeys.p, kb, savals.p, h->blk_mask.p, h->blk_maskT.p, h->blk_lay.p,
+            h->blk_count.p, h->blk_voff.p, L, h->row_ptr.p, gbase.p, h->col_idx.p, h->nnz_group.p, h->src_map.p,
+            h->g_row.p, h->g_col.p, h->g_kind.p, (unsigned long long)nnz, (unsigned long long)ng,
+            h->vs_off + h->s_words);
+      if (early && fill_entry[c + 1] > fill_entry[c]) {
+        if (!h->fill_ev[c]) CK(cudaEventCreateWithFlags(&h->fill_ev[c], cudaEventDisableTiming));
+        CK(cudaEventRecord(h->fill_ev[c], s));
+        CK(cudaStreamWaitEvent(h->copy_stream, h->fill_ev[c], 0));
+        CK(cudaMemcpyAsync(pc->col_idx + fill_entry[c], h->col_idx.p + fill_entry[c],
+                           (size_t)(fill_entry[c + 1] - fill_entry[c]) * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                           h->copy_stream));
+      }
+    }
     CK(cudaGetLastError());
-    int too_many = 0;
-    CK(cudaMemcpyAsync(&too_many, h->flag.p, sizeof too_many, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (too_many) return h->fail(FEM_GPU_ERR_ARGUMENT, "a node pair is shared by 2^24 or more elements");
+    if (early) {
+      pc->issued = true;  // the caller reads flag[1] (a node pair shared by 2^24 or more elements) after its pass
+    } else {
+      int too_many = 0;
+      CK(cudaMemcpyAsync(&too_many, h->flag.p + 1, sizeof too_many, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if (too_many) return h->fail(FEM_GPU_ERR_ARGUMENT, kTooManyMsg);
+    }
     sz.release();
   }
-  CK(cudaStreamSynchronize(s));
+  if (!early) CK(cudaStreamSynchronize(s));
   // temporaries
   keys.release();
   skeys.release();
@@ -3197,32 +3249,48 @@ extern "C" int fem_gpu_assemble_to_host(fem_gpu_t* h, int64_t* row_ptr, int32_t*
   }
   const size_t nrows = (size_t)h->nodes_number * 6;
   for (int attempt = 0; attempt < 2; ++attempt) {
+    PatternCopy pc{row_ptr, col_idx, nnz_capacity};
     if (!h->pattern_valid) {
-      st = symbolic(h);
-      if (st) return st;
+      st = symbolic(h, &pc);
+      if (st) {
+        cudaStreamSynchronize(h->copy_stream);  // no copy into the caller's buffers outlives the call
+        return st;
+      }
     }
     if (nnz) *nnz = h->nnz;
     if (h->nnz > nnz_capacity)
       return h->fail(FEM_GPU_ERR_ARGUMENT, "the CSR has %lld entries, the buffers room for %lld",
                      (long long)h->nnz, (long long)nnz_capacity);
-    // the pattern goes back on the copy stream while the numeric pass runs (it writes only the values)
-    CK(cudaEventRecord(h->copy_ev, h->stream));
-    CK(cudaStreamWaitEvent(h->copy_stream, h->copy_ev, 0));
+    if (!pc.issued) {
+      // the pattern goes back on the copy stream while the numeric pass runs (it writes only the values)
+      CK(cudaEventRecord(h->copy_ev, h->stream));
+      CK(cudaStreamWaitEvent(h->copy_stream, h->copy_ev, 0));
+    }
     st = numeric_launch(h);
-    if (st) return st;
-    CK(cudaMemcpyAsync(row_ptr, h->row_ptr.p, (nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, h->copy_stream));
-    if (h->nnz)
-      CK(cudaMemcpyAsync(col_idx, h->col_idx.p, (size_t)h->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost,
+    if (st) {
+      cudaStreamSynchronize(h->copy_stream);
+      return st;
+    }
+    if (!pc.issued) {
+      CK(cudaMemcpyAsync(row_ptr, h->row_ptr.p, (nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost,
                          h->copy_stream));
-    int flag = 0;
-    CK(cudaMemcpyAsync(&flag, h->flag.p, sizeof flag, cudaMemcpyDeviceToHost, h->stream));
+      if (h->nnz)
+        CK(cudaMemcpyAsync(col_idx, h->col_idx.p, (size_t)h->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                           h->copy_stream));
+    }
+    int flag[2] = {0, 0};
+    CK(cudaMemcpyAsync(flag, h->flag.p, (pc.issued ? 2 : 1) * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     if (h->nnz)
       CK(cudaMemcpyAsync(values, h->values.p, (size_t)h->nnz * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaStreamSynchronize(h->copy_stream));
+    if (flag[1]) {
+      h->pattern_valid = false;
+      return h->fail(FEM_GPU_ERR_ARGUMENT, kTooManyMsg);
+    }
     CK(cudaEventElapsedTime(&h->t_elem_ms, h->ev[0], h->ev[1]));
     CK(cudaEventElapsedTime(&h->t_reduce_ms, h->ev[1], h->ev[2]));
-    if (!flag) return FEM_GPU_OK;
+    if (!flag[0]) return FEM_GPU_OK;
     h->pattern_valid = false;  // a coordinate/property update changed the exact-zero pattern
   }
   return h->fail(FEM_GPU_ERR_PATTERN_CHANGED, "pattern changed twice in one assemble");

@@ -318,6 +318,32 @@ def test_batch_matches_each_model():
     b.close()
 
 
+@pytest.mark.parametrize("name", ["plate", "frame_slab", "truss", "tiny"])
+def test_assemble_to_host_fresh_pattern(name):
+    """A first assemble_to_host on a new model: row_ptr goes back once the rows are counted and the
+    columns in node chunks as the row fill finishes each, during the symbolic phase; the host arrays
+    hold the CSR of assemble() + stiffness_csr() and nothing past nnz is written."""
+    m = {"plate": lambda: meshes.plate_mesh(60, 45, size=5.0),
+         "frame_slab": lambda: meshes.adjoint_model(frame=(5, 4, 3), slab=(40, 30)),
+         "truss": lambda: meshes.truss_lattice(5),
+         "tiny": lambda: meshes.plate_mesh(1, 1, size=1.0)}[name]()
+    g, _ = build_pair(m)
+    rp0, ci0, va0 = g.stiffness_csr()
+    g.close()
+    g2 = FEM(1e-12, 1e-12, m.nodes_number)
+    meshes.load(g2, m)
+    rp = np.full(6 * m.nodes_number + 1, -1, np.int64)
+    ci = np.full(len(ci0) + 3, -1, np.int32)
+    va = np.full(len(va0) + 3, np.nan)
+    nnz = g2.assemble_to_host(rp, ci, va)
+    assert nnz == len(ci0)
+    np.testing.assert_array_equal(rp, rp0)
+    np.testing.assert_array_equal(ci[:nnz], ci0)
+    np.testing.assert_array_equal(va[:nnz].view(np.uint64), va0.view(np.uint64))
+    assert (ci[nnz:] == -1).all() and np.isnan(va[nnz:]).all()
+    g2.close()
+
+
 def test_assemble_to_host_matches_assemble():
     m = meshes.plate_mesh(50, 40, size=5.0)
     g, o = build_pair(m)
