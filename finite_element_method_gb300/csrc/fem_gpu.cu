@@ -665,7 +665,7 @@ __device__ __forceinline__ uint64_t transpose36(uint64_t m) {
 __global__ void k_block_meta(const uint32_t* __restrict__ blk_start, size_t nb, size_t n_pairs,
                              const uint64_t* __restrict__ keys, int kb, const uint64_t* __restrict__ sorted_mask,
                              uint32_t* blk_count, uint64_t* blk_mask, uint64_t* blk_maskT, int32_t* blk_I,
-                             int32_t* blk_J, uint32_t* adj_n) {
+                             int32_t* blk_J) {
   size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (b >= nb) return;
   uint32_t s = blk_start[b];
@@ -679,30 +679,75 @@ __global__ void k_block_meta(const uint32_t* __restrict__ blk_start, size_t nb, 
   int32_t I = (int32_t)(key >> kb), J = (int32_t)(key & ((1ull << kb) - 1ull));
   blk_I[b] = I;
   blk_J[b] = J;
-  adj_n[b] = I == J ? 1u : 2u;
 }
 
-__global__ void k_adjacency(const uint32_t* __restrict__ adj_off, size_t nb, const int32_t* __restrict__ blk_I,
-                            const int32_t* __restrict__ blk_J, int kb, uint64_t* akeys, uint32_t* avals) {
-  size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+// Row-node adjacency from the blocks, which are in (I, J) order with I <= J: row r lists the blocks (I, r),
+// I <= r, in I order (a stable sort of the blocks by J) and then the blocks (r, J), J > r, in J order (a
+// range of the block order) -- the (row node, column node) order without sorting on both nodes.
+__global__ void k_block_cols(size_t nb, const int32_t* __restrict__ blk_J, uint32_t* col, uint32_t* idx) {
+  const size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (b >= nb) return;
-  uint32_t o = adj_off[b];
-  uint32_t I = (uint32_t)blk_I[b], J = (uint32_t)blk_J[b];
-  akeys[o] = ((uint64_t)I << kb) | J;
-  avals[o] = (uint32_t)(b << 1);
-  if (I != J) {
-    akeys[o + 1] = ((uint64_t)J << kb) | I;
-    avals[o + 1] = (uint32_t)((b << 1) | 1u);
+  col[b] = (uint32_t)blk_J[b];
+  idx[b] = (uint32_t)b;
+}
+// first and end position of every key's run in a sorted array (untouched for keys absent)
+template <class K>
+__global__ void k_runs(const K* __restrict__ keys, size_t n, int32_t* first, int32_t* end) {
+  const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t r = (uint32_t)keys[k];
+  if (k == 0 || (uint32_t)keys[k - 1] != r) first[r] = (int32_t)k;
+  if (k + 1 == n || (uint32_t)keys[k + 1] != r) end[r] = (int32_t)(k + 1);
+}
+// entries of row r: its column run (blocks (I, r)) and its row run past the diagonal (blocks (r, J), J > r)
+__device__ __forceinline__ void adj_parts(size_t r, const int32_t* jf, const int32_t* je, const int32_t* i_f,
+                                          const int32_t* ie, const int32_t* __restrict__ blk_J, int32_t& n_low,
+                                          int32_t& up_first, int32_t& n_up) {
+  n_low = jf[r] >= 0 ? je[r] - jf[r] : 0;
+  up_first = i_f[r];
+  n_up = 0;
+  if (up_first >= 0) {
+    n_up = ie[r] - up_first;
+    if (blk_J[up_first] == (int32_t)r) {  // the diagonal block leads the row run; it is in the column run
+      ++up_first;
+      --n_up;
+    }
   }
 }
-
-__global__ void k_row_segments(const uint64_t* __restrict__ akeys, size_t na, int kb, int32_t* seg_begin,
-                               int32_t* seg_end) {
-  size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (k >= na) return;
-  uint32_t r = (uint32_t)(akeys[k] >> kb);
-  if (k == 0 || (uint32_t)(akeys[k - 1] >> kb) != r) seg_begin[r] = (int32_t)k;
-  if (k + 1 == na || (uint32_t)(akeys[k + 1] >> kb) != r) seg_end[r] = (int32_t)(k + 1);
+__global__ void k_adj_lens(size_t nn, const int32_t* jf, const int32_t* je, const int32_t* i_f, const int32_t* ie,
+                           const int32_t* __restrict__ blk_J, uint32_t* len) {
+  const size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (r > nn) return;
+  if (r == nn) {
+    len[r] = 0;
+    return;
+  }
+  int32_t n_low, up_first, n_up;
+  adj_parts(r, jf, je, i_f, ie, blk_J, n_low, up_first, n_up);
+  len[r] = (uint32_t)(n_low + n_up);
+}
+__global__ void k_adj_fill(size_t nn, const int32_t* jf, const int32_t* je, const int32_t* i_f, const int32_t* ie,
+                           const int32_t* __restrict__ blk_I, const int32_t* __restrict__ blk_J,
+                           const uint32_t* __restrict__ by_col, const uint32_t* __restrict__ off, int kb,
+                           uint64_t* akeys, uint32_t* avals, int32_t* seg_begin, int32_t* seg_end) {
+  const size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (r >= nn) return;
+  int32_t n_low, up_first, n_up;
+  adj_parts(r, jf, je, i_f, ie, blk_J, n_low, up_first, n_up);
+  const uint32_t o = off[r];
+  seg_begin[r] = n_low + n_up > 0 ? (int32_t)o : -1;
+  seg_end[r] = n_low + n_up > 0 ? (int32_t)(o + n_low + n_up) : -1;
+  for (int32_t k = 0; k < n_low; ++k) {
+    const uint32_t b = by_col[jf[r] + k];
+    const uint32_t I = (uint32_t)blk_I[b];
+    akeys[o + k] = ((uint64_t)r << kb) | I;
+    avals[o + k] = (b << 1) | (I != (uint32_t)r ? 1u : 0u);
+  }
+  for (int32_t k = 0; k < n_up; ++k) {
+    const uint32_t b = (uint32_t)(up_first + k);
+    akeys[o + n_low + k] = ((uint64_t)r << kb) | (uint32_t)blk_J[b];
+    avals[o + n_low + k] = b << 1;
+  }
 }
 
 __device__ __forceinline__ uint32_t kinds_of(uint64_t m) {
@@ -3010,15 +3055,8 @@ int symbolic(fem_gpu* h, PatternCopy* pc = nullptr) {
   CK(h->blk_I.reserve(nb, s));
   CK(h->blk_J.reserve(nb, s));
   k_block_starts<<<grid_for(np, 256), 256, 0, s>>>(incl.p, np, h->blk_start.p);
-  DevBuf<uint32_t> adj_n, adj_off;
-  CK(adj_n.reserve(nb, s));
-  CK(adj_off.reserve(nb, s));
   k_block_meta<<<grid_for(nb, 256), 256, 0, s>>>(h->blk_start.p, nb, np, skeys.p, kb, smask.p, h->blk_count.p,
-                                                 h->blk_mask.p, h->blk_maskT.p, h->blk_I.p, h->blk_J.p, adj_n.p);
-  st = cub_call(h, [&](void* tmp, size_t& bytes) {
-    return cub::DeviceScan::ExclusiveSum(tmp, bytes, adj_n.p, adj_off.p, (int64_t)nb, s);
-  });
-  if (st) return st;
+                                                 h->blk_mask.p, h->blk_maskT.p, h->blk_I.p, h->blk_J.p);
   // compacted scratch: block offsets and, per element pair, its offset and mask
   {
     DevBuf<unsigned long long> sizes;
@@ -3046,25 +3084,42 @@ int symbolic(fem_gpu* h, PatternCopy* pc = nullptr) {
     h->v_words = (size_t)total;
     h->v_pad = (size_t)pads;
   }
-  uint32_t last_off = 0, last_n = 0;
-  CK(cudaMemcpyAsync(&last_off, adj_off.p + nb - 1, sizeof last_off, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&last_n, adj_n.p + nb - 1, sizeof last_n, cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  size_t na = (size_t)last_off + last_n;
-  // 6. row-node adjacency sorted by (row node, col node)
-  DevBuf<uint64_t> akeys, sakeys;
-  DevBuf<uint32_t> avals, savals;
-  CK(akeys.reserve(na, s));
-  CK(sakeys.reserve(na, s));
-  CK(avals.reserve(na, s));
-  CK(savals.reserve(na, s));
-  k_adjacency<<<grid_for(nb, 256), 256, 0, s>>>(adj_off.p, nb, h->blk_I.p, h->blk_J.p, kb, akeys.p, avals.p);
+  // 6. row-node adjacency in (row node, column node) order: a stable sort of the blocks by their column node
+  // J (kb bits) gives every row its blocks (I, r), I <= r, in I order; the block order gives its (r, J), J > r
+  size_t nn = h->nodes_number;
+  DevBuf<uint32_t> jcol, sjcol, jidx, by_col, alen, aoff;
+  CK(jcol.reserve(nb, s));
+  CK(sjcol.reserve(nb, s));
+  CK(jidx.reserve(nb, s));
+  CK(by_col.reserve(nb, s));
+  k_block_cols<<<grid_for(nb, 256), 256, 0, s>>>(nb, h->blk_J.p, jcol.p, jidx.p);
   st = cub_call(h, [&](void* tmp, size_t& bytes) {
-    return cub::DeviceRadixSort::SortPairs(tmp, bytes, akeys.p, sakeys.p, avals.p, savals.p, (int64_t)na, 0, 2 * kb,
-                                           s);
+    return cub::DeviceRadixSort::SortPairs(tmp, bytes, jcol.p, sjcol.p, jidx.p, by_col.p, (int64_t)nb, 0, kb, s);
   });
   if (st) return st;
-  size_t nn = h->nodes_number;
+  DevBuf<int32_t> jf, je, i_f, ie;
+  CK(jf.reserve(nn, s));
+  CK(je.reserve(nn, s));
+  CK(i_f.reserve(nn, s));
+  CK(ie.reserve(nn, s));
+  CK(cudaMemsetAsync(jf.p, 0xff, nn * sizeof(int32_t), s));
+  CK(cudaMemsetAsync(je.p, 0xff, nn * sizeof(int32_t), s));
+  CK(cudaMemsetAsync(i_f.p, 0xff, nn * sizeof(int32_t), s));
+  CK(cudaMemsetAsync(ie.p, 0xff, nn * sizeof(int32_t), s));
+  k_runs<<<grid_for(nb, 256), 256, 0, s>>>(sjcol.p, nb, jf.p, je.p);
+  k_runs<<<grid_for(nb, 256), 256, 0, s>>>(h->blk_I.p, nb, i_f.p, ie.p);
+  CK(alen.reserve(nn + 1, s));
+  CK(aoff.reserve(nn + 1, s));
+  k_adj_lens<<<grid_for(nn + 1, 256), 256, 0, s>>>(nn, jf.p, je.p, i_f.p, ie.p, h->blk_J.p, alen.p);
+  st = cub_call(h, [&](void* tmp, size_t& bytes) {
+    return cub::DeviceScan::ExclusiveSum(tmp, bytes, alen.p, aoff.p, (int64_t)(nn + 1), s);
+  });
+  if (st) return st;
+  const size_t na = 2 * nb;  // at most: every block once in its row, the off-diagonal ones once more
+  DevBuf<uint64_t> sakeys;
+  DevBuf<uint32_t> savals;
+  CK(sakeys.reserve(na, s));
+  CK(savals.reserve(na, s));
   DevBuf<int32_t> seg_b, seg_e;
   DevBuf<int64_t> row_nnz, gcount, gbase;
   CK(seg_b.reserve(nn, s));
@@ -3072,11 +3127,10 @@ int symbolic(fem_gpu* h, PatternCopy* pc = nullptr) {
   CK(row_nnz.reserve(nrows + 1, s));
   CK(gcount.reserve(nn + 1, s));
   CK(gbase.reserve(nn + 1, s));
-  CK(cudaMemsetAsync(seg_b.p, 0xff, nn * sizeof(int32_t), s));
-  CK(cudaMemsetAsync(seg_e.p, 0xff, nn * sizeof(int32_t), s));
   CK(cudaMemsetAsync(row_nnz.p, 0, (nrows + 1) * sizeof(int64_t), s));
   CK(cudaMemsetAsync(gcount.p, 0, (nn + 1) * sizeof(int64_t), s));
-  k_row_segments<<<grid_for(na, 256), 256, 0, s>>>(sakeys.p, na, kb, seg_b.p, seg_e.p);
+  k_adj_fill<<<grid_for(nn, 128), 128, 0, s>>>(nn, jf.p, je.p, i_f.p, ie.p, h->blk_I.p, h->blk_J.p, by_col.p, aoff.p,
+                                               kb, sakeys.p, savals.p, seg_b.p, seg_e.p);
   k_row_counts<<<grid_for(nn, 128), 128, 0, s>>>(nn, seg_b.p, seg_e.p, savals.p, h->blk_mask.p, h->blk_maskT.p,
                                                  row_nnz.p, gcount.p);
   st = cub_call(h, [&](void* tmp, size_t& bytes) {
@@ -3200,11 +3254,17 @@ int symbolic(fem_gpu* h, PatternCopy* pc = nullptr) {
   smask.release();
   head.release();
   incl.release();
-  adj_n.release();
-  adj_off.release();
-  akeys.release();
+  jcol.release();
+  sjcol.release();
+  jidx.release();
+  by_col.release();
+  alen.release();
+  aoff.release();
+  jf.release();
+  je.release();
+  i_f.release();
+  ie.release();
   sakeys.release();
-  avals.release();
   savals.release();
   seg_b.release();
   seg_e.release();
