@@ -207,7 +207,7 @@ int batch_enqueue(fem_gpu_batch* b) {
   }
   const unsigned rb = (unsigned)b->cfg.sum_block;
   if (d.n_desc)
-    k_block_sums<<<grid_for(d.n_desc, rb), rb, 0, s>>>(d.n_desc, d.n_sums, d.desc, d.V, d.V + d.vs_off, b->flag.p,
+    k_block_sums<<<block_sums_grid(d.n_desc, rb), rb, 0, s>>>(d.n_desc, d.n_sums, d.desc, d.V, d.V + d.vs_off, b->flag.p,
                                                        d.v_words);
   if (b->nnz)
     k_gather_values<<<grid_for(((size_t)b->nnz + kGatherPerThread - 1) / kGatherPerThread, rb), rb, 0, s>>>(

@@ -1021,22 +1021,17 @@ __global__ void k_slot_desc(size_t nb, const uint32_t* __restrict__ blk_count, c
 // their entry.  No atomics on values.  A non-pattern entry with a non-zero, or
 // a pattern slot whose contributions are all zero, raises kFlagPattern (the
 // exact-zero pattern changed).
-__global__ void __launch_bounds__(512) k_block_sums(size_t n_desc, size_t n_sums, const uint2* __restrict__ desc,
-                                                    const double* __restrict__ V, double* __restrict__ S, int* flag,
-                                                    unsigned long long v_words) {
-  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i >= n_desc) return;
-  const uint2 d = desc[i];
+__device__ __forceinline__ bool block_sum_one(size_t i, uint2 d, size_t n_sums, const double* __restrict__ V,
+                                              double* __restrict__ S, unsigned long long v_words) {
   const uint32_t n = d.y & 0xffffffu, stride = (d.y >> 24) & 0x7fu;
   const bool inpat = (d.y >> 31) != 0;
-  if (n == 0 || !dbg_in_range(d.x + (unsigned long long)(n - 1) * stride, v_words, kDbgSumSource)) return;
+  if (n == 0 || !dbg_in_range(d.x + (unsigned long long)(n - 1) * stride, v_words, kDbgSumSource)) return false;
   const double* src = V + d.x;
   bool nz;
   double sum;
   switch (n) {
     case 1:
-      if (nonzero(src[0])) atomicOr(flag, kFlagPattern);
-      return;
+      return nonzero(src[0]);
     case 2: {
       const double a = src[0], b = src[stride];
       nz = nonzero(a) | nonzero(b);
@@ -1066,7 +1061,36 @@ __global__ void __launch_bounds__(512) k_block_sums(size_t n_desc, size_t n_sums
     }
   }
   if (i < n_sums) S[i] = sum;
-  if (nz != inpat) atomicOr(flag, kFlagPattern);
+  return nz != inpat;
+}
+
+// grid-stride over the descriptors, the next descriptor loaded while the current one's contributions are read
+__global__ void __launch_bounds__(512) k_block_sums(size_t n_desc, size_t n_sums, const uint2* __restrict__ desc,
+                                                    const double* __restrict__ V, double* __restrict__ S, int* flag,
+                                                    unsigned long long v_words) {
+  const size_t step = (size_t)gridDim.x * blockDim.x;
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n_desc) return;
+  uint2 d = desc[i];
+  bool bad = false;
+  for (;;) {
+    const size_t inext = i + step;
+    const uint2 dn = inext < n_desc ? desc[inext] : make_uint2(0u, 0u);
+    bad |= block_sum_one(i, d, n_sums, V, S, v_words);
+    if (inext >= n_desc) break;
+    i = inext;
+    d = dn;
+  }
+  if (bad) atomicOr(flag, kFlagPattern);
+}
+// CTAs of a block-sum launch: enough to fill the SMs a few times over, each looping over its share
+unsigned block_sums_grid(size_t n_desc, unsigned block) {
+  static int sms[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms[dev] = 1;
+  const size_t want = (n_desc + block - 1) / block, cap = (size_t)sms[dev] * (2048 / block) * 2;
+  return (unsigned)std::max<size_t>(1, std::min(want, cap));
 }
 
 // Numeric pass, part 2: CSR values in storage order, each read from its source
@@ -2912,7 +2936,7 @@ int numeric_enqueue(fem_gpu* h, bool captured) {
   CK(mark(h->ev[1]));
   if (h->n_blocks) {
     if (h->n_desc)
-      k_block_sums<<<grid_for(h->n_desc, 256), 256, 0, h->stream>>>(h->n_desc, h->s_words, h->slot_desc.p, h->V.p,
+      k_block_sums<<<block_sums_grid(h->n_desc, 256), 256, 0, h->stream>>>(h->n_desc, h->s_words, h->slot_desc.p, h->V.p,
                                                                      h->V.p + h->vs_off, h->flag.p, h->v_words);
     k_gather_values<<<grid_for(((size_t)h->nnz + kGatherPerThread - 1) / kGatherPerThread, 256), 256, 0,
                       h->stream>>>((size_t)h->nnz, h->src_map.p, h->V.p, h->vs_off, h->values.p, h->flag.p,

@@ -106,9 +106,11 @@ int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const uint32_t* no
  * Synchronous; returns after the CSR is complete on the device. */
 int fem_gpu_assemble(fem_gpu_t* h);
 /* fem_gpu_assemble with the CSR read back into host arrays (row_ptr 6 * nodes_number + 1, col_idx and
- * values room for nnz_capacity entries): the pattern goes back on a second stream while the numeric pass
- * runs, the values after it.  *nnz gets the entry count; FEM_GPU_ERR_ARGUMENT when it exceeds
- * nnz_capacity (fem_gpu_get_csr_sizes tells it after a fem_gpu_assemble). */
+ * values room for nnz_capacity entries; page-locked arrays copy fastest).  The pattern goes back on a
+ * second stream -- during a symbolic phase row_ptr as soon as the rows are counted and col_idx in node
+ * chunks as they are filled, otherwise while the numeric pass runs -- and the values after the pass.
+ * Every copy has landed when the call returns.  *nnz gets the entry count; FEM_GPU_ERR_ARGUMENT when it
+ * exceeds nnz_capacity (fem_gpu_get_csr_sizes tells it after a fem_gpu_assemble). */
 int fem_gpu_assemble_to_host(fem_gpu_t* h, int64_t* row_ptr, int32_t* col_idx, double* values,
                              int64_t nnz_capacity, int64_t* nnz);
 
