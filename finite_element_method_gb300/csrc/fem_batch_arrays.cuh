@@ -252,6 +252,41 @@ int ba_replay(double rel_tol, double abs_tol, const fem_gpu_structures_t* in, si
 }
 
 // the element kinds of the input, in call order
+// A caller's host array to the device.  Where the GPU reads pageable host memory itself
+// (cudaDevAttrPageableMemoryAccess: address translation over the host link, as on Grace systems), a
+// kernel reads it at the link's rate; a pageable cudaMemcpyAsync goes through the driver's staging, which
+// took anywhere from 1.6 to 72 ms for the same 120 MB of coordinates between one call and the next.
+// Small, unaligned or unreadable-in-place arrays take cudaMemcpyAsync.  Asynchronous either way: the
+// caller's array must stay valid until the stream has passed the copy.
+__global__ void k_read_host(const uint4* __restrict__ src, uint4* __restrict__ dst, size_t n16) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+constexpr size_t kDirectReadBytes = 1u << 20;
+cudaError_t host_to_device(void* dst, const void* src, size_t bytes, cudaStream_t s, int sm_count) {
+  static int direct[64];
+  static bool known[64];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < 64 && !known[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) v = 0;
+    direct[dev] = v;
+    known[dev] = true;
+  }
+  const bool use = dev >= 0 && dev < 64 && direct[dev] && bytes >= kDirectReadBytes &&
+                   ((uintptr_t)src % 16) == 0 && ((uintptr_t)dst % 16) == 0;
+  if (!use) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+  const size_t n16 = bytes / 16, tail = bytes - n16 * 16;
+  k_read_host<<<(unsigned)std::max(1, sm_count * 4), 256, 0, s>>>(static_cast<const uint4*>(src),
+                                                                  static_cast<uint4*>(dst), n16);
+  e = cudaGetLastError();
+  if (e != cudaSuccess || !tail) return e;
+  return cudaMemcpyAsync(static_cast<char*>(dst) + n16 * 16, static_cast<const char*>(src) + n16 * 16, tail,
+                         cudaMemcpyHostToDevice, s);
+}
+
 struct BaKind {
   int kind;
   int per_el;                   // nodes per element
@@ -360,8 +395,8 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
   BAK(u32.reserve(most + 1, s));
   BAK(h->stage.reserve(3 * NN + 1, s));
   if (NN) {
-    BAK(cudaMemcpyAsync(u32.p, in->node_numbers, NN * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    BAK(cudaMemcpyAsync(h->stage.p, in->xyz, 3 * NN * sizeof(double), cudaMemcpyHostToDevice, s));
+    BAK(host_to_device(u32.p, in->node_numbers, NN * sizeof(uint32_t), s, b->sm_count));
+    BAK(host_to_device(h->stage.p, in->xyz, 3 * NN * sizeof(double), s, b->sm_count));
     k_ba_sid<<<grid_for(NN, 256), 256, 0, s>>>(d_nodeoff.p, (uint32_t)S, NN, nsid.p);
     k_ba_coord_keys<<<grid_for(NN, 256), 256, 0, s>>>(NN, nsid.p, h->stage.p, key.p, idx.p);
     st = sort_pairs(NN, 64);
@@ -408,13 +443,13 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
     BAK(esid.reserve(n + 1, s));
     k_ba_sid<<<grid_for(n, 256), 256, 0, s>>>(d_eloff.p, (uint32_t)S, n, esid.p);
     // element numbers repeated inside a structure
-    BAK(cudaMemcpyAsync(u32.p, k.numbers, n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    BAK(host_to_device(u32.p, k.numbers, n * sizeof(uint32_t), s, b->sm_count));
     k_ba_num_keys<<<grid_for(n, 256), 256, 0, s>>>(n, esid.p, u32.p, key.p, idx.p);
     st = sort_pairs(n, 32 + sbits);
     if (st) return cerr(st);
     k_ba_equal_keys<<<grid_for(n, 256), 256, 0, s>>>(n, skey.p, sidx.p, esid.p, d_fail.p);
     // node numbers -> node slots
-    BAK(cudaMemcpyAsync(u32.p, k.nodes, (size_t)k.per_el * n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    BAK(host_to_device(u32.p, k.nodes, (size_t)k.per_el * n * sizeof(uint32_t), s, b->sm_count));
     int32_t* o[4] = {nullptr, nullptr, nullptr, nullptr};
     if (k.kind == kTruss) {
       BAK(h->t_n1.reserve(n + 1, s));
@@ -447,7 +482,7 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
     // properties
     auto up = [&](DevBuf<double>& d, const double* src) -> int {
       BAK(d.reserve(n + 1, s));
-      BAK(cudaMemcpyAsync(d.p, src, n * sizeof(double), cudaMemcpyHostToDevice, s));
+      BAK(host_to_device(d.p, src, n * sizeof(double), s, b->sm_count));
       return FEM_GPU_OK;
     };
     int r = 0;
@@ -465,7 +500,7 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
           (r = up(h->b_it, in->beam_it)) || (r = up(h->b_ks, in->beam_shear_factor)))
         return r;
       BAK(v3.reserve(3 * n + 1, s));
-      BAK(cudaMemcpyAsync(v3.p, in->beam_local_axis, 3 * n * sizeof(double), cudaMemcpyHostToDevice, s));
+      BAK(host_to_device(v3.p, in->beam_local_axis, 3 * n * sizeof(double), s, b->sm_count));
       for (DevBuf<double>* d : {&h->b_ax, &h->b_ay, &h->b_az}) BAK(d->reserve(n + 1, s));
       k_ba_split3<<<grid_for(n, 256), 256, 0, s>>>(n, v3.p, h->b_ax.p, h->b_ay.p, h->b_az.p);
     } else {
