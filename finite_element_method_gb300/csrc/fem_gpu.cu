@@ -595,17 +595,17 @@ __device__ __forceinline__ void plate_element(size_t e, NodesView nd, const Plat
     plate_pairs<false>(C, R, nidx, e, sink, spk, spk_stride);
 }
 
-// Launch shape of the plate kernel.  FEM_PLATE_BLOCK threads per CTA (64 by default: at 254 registers a
-// thread an SM holds 8 warps either way, in finer pieces than 128); FEM_PLATE_MAXNREG, when defined, caps
-// its registers (more warps per SM, more spills: the measured caps of 232, 200, 168 and 128 were slower).
+// Launch shape of the plate kernel.  FEM_PLATE_BLOCK threads per CTA (64 by default) and at most
+// FEM_PLATE_MAXNREG registers a thread (200 by default: five 64-thread CTAs, 10 warps, an SM instead of
+// four at the 254 the kernel takes uncapped; the 160 bytes a thread spills cost less than the two warps
+// win -- 1.0185 against 1.0226 ms on the 1M-plate mesh; caps of 168 and 128 were no better or slower).
 #ifndef FEM_PLATE_BLOCK
 #define FEM_PLATE_BLOCK 64
 #endif
-#ifdef FEM_PLATE_MAXNREG
-__global__ void __maxnreg__(FEM_PLATE_MAXNREG)
-#else
-__global__ void __launch_bounds__(256)
+#ifndef FEM_PLATE_MAXNREG
+#define FEM_PLATE_MAXNREG 200
 #endif
+__global__ void __maxnreg__(FEM_PLATE_MAXNREG)
 k_plate(NodesView nd, PlateView pl, double abs_tol, size_t count,
                                                BlockSink sink) {
   // numeric mode: the plate's ten scratch words are copied to shared memory ([pair][thread], dynamic, sized
