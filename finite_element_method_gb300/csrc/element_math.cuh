@@ -927,7 +927,7 @@ __device__ __forceinline__ bool quad_on_line(const double* P0, const double* P1,
     sub3(P[pairs[k][1]], P[pairs[k][0]], u);
     sub3(P[pairs[k][2]], P[pairs[k][0]], v);
     cross3(u, v, c);
-    if (norm3(c) == 0.0) return true;
+    if (dot3(c, c) == 0.0) return true;  // |c| == 0 exactly when |c|^2 == 0 (no square root needed)
   }
   return false;
 }
