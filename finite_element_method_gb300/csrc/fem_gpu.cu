@@ -1914,29 +1914,44 @@ __global__ void k_pair_dups(size_t n, const unsigned long long* __restrict__ ske
 }
 
 // The first of the items [0, count) that the validation kernel launch(status, first) rejects, with its error code
-// (*first_bad = count when none).
-template <class Launch, class Host>
-int first_failure(fem_gpu* h, size_t count, Launch launch, Host host, size_t* first_bad, int* code) {
-  *first_bad = count;
-  *code = 0;
-  if (!count) return FEM_GPU_OK;
-  CK(h->vstatus.reserve(count, h->stream));
+// (*first_bad = count when none).  validate_start enqueues the kernel over `launched` items; validate_finish
+// waits and reports the first rejected item below `count` (<= launched): a bulk call can start the kernel
+// before its host checks have settled how many items get that far.
+template <class Launch>
+int validate_start(fem_gpu* h, size_t launched, Launch launch) {
+  if (!launched) return FEM_GPU_OK;
+  CK(h->vstatus.reserve(launched, h->stream));
   CK(h->vfirst.reserve(1, h->stream));
   unsigned long long init = ~0ull;
   CK(cudaMemcpyAsync(h->vfirst.p, &init, sizeof init, cudaMemcpyHostToDevice, h->stream));
   launch(h->vstatus.p, h->vfirst.p);
   CK(cudaGetLastError());
-  host();  // host work that does not wait for the result runs while the GPU validates
+  return FEM_GPU_OK;
+}
+int validate_finish(fem_gpu* h, size_t count, size_t* first_bad, int* code) {
+  *first_bad = count;
+  *code = 0;
+  if (!count) return FEM_GPU_OK;
   unsigned long long first = 0;
   CK(cudaMemcpyAsync(&first, h->vfirst.p, sizeof first, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  if (first != ~0ull) {
+  if (first != ~0ull && first < count) {
     int c = 0;
     CK(cudaMemcpy(&c, h->vstatus.p + first, sizeof c, cudaMemcpyDeviceToHost));
     *first_bad = (size_t)first;
     *code = c;
   }
   return FEM_GPU_OK;
+}
+template <class Launch, class Host>
+int first_failure(fem_gpu* h, size_t count, Launch launch, Host host, size_t* first_bad, int* code) {
+  *first_bad = count;
+  *code = 0;
+  if (!count) return FEM_GPU_OK;
+  int st = validate_start(h, count, launch);
+  if (st) return st;
+  host();  // host work that does not wait for the result runs while the GPU validates
+  return validate_finish(h, count, first_bad, code);
 }
 
 int ensure_ready(fem_gpu* h) {
@@ -2434,8 +2449,10 @@ int two_node_checks(fem_gpu* h, const char* kind, NumberMap& by_num, DevBuf<int3
 // The same for plates: the four nodes exist, the number is new, the node set is new.  Returns -1
 // (nothing changed) when an item before the first missing node repeats a node number: those take
 // the sequential loop's subset test.
+// (props: young, poisson, thickness, shear factor of the call's plates; *validated gets the number of items
+// whose validation kernel was started here -- it runs on the GPU while the host checks the numbers)
 int plate_checks(fem_gpu* h, const uint32_t* numbers, const uint32_t* nodes, size_t n, HostVec<int32_t>* id,
-                 size_t* passed) {
+                 size_t* passed, const double* const props[4], size_t* validated) {
   const unsigned T = add_threads();
   const size_t base = h->np;
   for (int q = 0; q < 4; ++q) id[q].resize(n);
@@ -2467,6 +2484,21 @@ int plate_checks(fem_gpu* h, const uint32_t* numbers, const uint32_t* nodes, siz
   for (int c = 0; c < 4; ++c) {
     DevBuf<int32_t>& dst = c == 0 ? h->p_n1 : c == 1 ? h->p_n2 : c == 2 ? h->p_n3 : h->p_n4;
     CK(upload(dst, base, id[c].data(), limit, h->stream));
+  }
+  // their properties too, and the validation of these items starts now (it needs no host check)
+  CK(upload(h->p_E, base, props[0], limit, h->stream));
+  CK(upload(h->p_nu, base, props[1], limit, h->stream));
+  CK(upload(h->p_t, base, props[2], limit, h->stream));
+  CK(upload(h->p_ks, base, props[3], limit, h->stream));
+  {
+    const NodesView nd = h->nodes();
+    const PlateView pv = h->plates();
+    const double abs_tol = h->abs_tol;
+    int vs = validate_start(h, limit, [&](int* s_, unsigned long long* f_) {
+      k_validate_plate<<<grid_for(limit, 128), 128, 0, h->stream>>>(nd, pv, abs_tol, base, limit, s_, f_);
+    });
+    if (vs) return vs;
+    *validated = limit;
   }
   const size_t total = base + limit;
   const int32_t *n1 = h->p_n1.p, *n2 = h->p_n2.p, *n3 = h->p_n3.p, *n4 = h->p_n4.p;
@@ -2784,8 +2816,10 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
   h->p_nodes.reserve(4 * (h->np + n));
   h->p_num.reserve(h->np + n);
   bool sequential = n < kParallelAdd;
+  size_t validated = 0;  // items whose validation the bulk checks started
   if (!sequential) {
-    host_code = plate_checks(h, numbers, nodes, n, id, &k);
+    const double* const props[4] = {young, poisson, thickness, shear_factor};
+    host_code = plate_checks(h, numbers, nodes, n, id, &k, props, &validated);
     if (host_code < 0) {  // repeated node numbers: the sequential loop's subset test
       host_code = FEM_GPU_OK;
       sequential = true;
@@ -2852,25 +2886,31 @@ extern "C" int fem_gpu_add_plates(fem_gpu_t* h, const uint32_t* numbers, const u
     CK(upload(h->p_n3, base, id[2].data(), m, h->stream));
     CK(upload(h->p_n4, base, id[3].data(), m, h->stream));
   }
-  CK(upload(h->p_E, base, young, m, h->stream));
-  CK(upload(h->p_nu, base, poisson, m, h->stream));
-  CK(upload(h->p_t, base, thickness, m, h->stream));
-  CK(upload(h->p_ks, base, shear_factor, m, h->stream));
   size_t bad;
   int code;
-  NodesView nd = h->nodes();
-  PlateView pv = h->plates();
-  double abs_tol = h->abs_tol;
-  st = first_failure(
-      h, m,
-      [&](int* s, unsigned long long* f) {
-        k_validate_plate<<<grid_for(m, 128), 128, 0, h->stream>>>(nd, pv, abs_tol, base, m, s, f);
-      },
-      [&] {  // the host arrays take every item now and drop the rejected ones after the result
-        append_host(h->p_num, numbers, m);
-        append_host(h->p_nodes, nodes, 4 * m);
-      },
-      &bad, &code);
+  if (validated >= m) {  // the bulk checks started the validation of these items already
+    append_host(h->p_num, numbers, m);  // the host arrays take every item now and drop the rejected ones after
+    append_host(h->p_nodes, nodes, 4 * m);
+    st = validate_finish(h, m, &bad, &code);
+  } else {
+    CK(upload(h->p_E, base, young, m, h->stream));
+    CK(upload(h->p_nu, base, poisson, m, h->stream));
+    CK(upload(h->p_t, base, thickness, m, h->stream));
+    CK(upload(h->p_ks, base, shear_factor, m, h->stream));
+    NodesView nd = h->nodes();
+    PlateView pv = h->plates();
+    double abs_tol = h->abs_tol;
+    st = first_failure(
+        h, m,
+        [&](int* s, unsigned long long* f) {
+          k_validate_plate<<<grid_for(m, 128), 128, 0, h->stream>>>(nd, pv, abs_tol, base, m, s, f);
+        },
+        [&] {  // the host arrays take every item now and drop the rejected ones after the result
+          append_host(h->p_num, numbers, m);
+          append_host(h->p_nodes, nodes, 4 * m);
+        },
+        &bad, &code);
+  }
   size_t accepted = st ? 0 : std::min(m, bad);
   h->p_num.resize(base + accepted);
   h->p_nodes.resize(4 * (base + accepted));

@@ -118,26 +118,48 @@ def test_bulk_two_node_elements(kind, case):
         np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
 
 
-@pytest.mark.parametrize("case", ["number", "same_nodes", "missing_node", "repeated_node_numbers"])
+@pytest.mark.parametrize("case", ["number", "same_nodes", "missing_node", "repeated_node_numbers",
+                                  "young_before_number", "number_before_young", "line_before_number",
+                                  "young_before_missing_node", "young_after_missing_node"])
 def test_bulk_plates(case):
+    """Bulk calls stop where the sequential calls would: the validation of a bulk call runs on the GPU while
+    the host checks the numbers, over the items before the first missing node, and the first failure in
+    item order wins (a number or node-set failure before an invalid plate, and the reverse)."""
     numbers, xyz, quads, _ = grid()
     quads = quads.copy()
     m = len(quads)
     pnums = np.arange(1, m + 1, dtype=np.uint32)
+    young = np.full(m, 70e9)
     if case == "number":
         pnums[35000] = pnums[100]
     elif case == "same_nodes":
         quads[35000] = quads[100][[2, 3, 0, 1]]
     elif case == "missing_node":
         quads[35000, 2] = 10 ** 7
-    else:  # a plate whose node list repeats a number (the subset rule): the sequential path decides
+    elif case == "repeated_node_numbers":  # a plate whose node list repeats a number: the sequential path decides
         quads[20000] = [quads[5][0], quads[5][1], quads[5][1], quads[5][2]]
+    elif case == "young_before_number":
+        young[20000] = 0.0
+        pnums[35000] = pnums[100]
+    elif case == "number_before_young":
+        pnums[20000] = pnums[100]
+        young[35000] = -1.0
+    elif case == "line_before_number":  # the third node moved onto the line of the first two (an inner plate)
+        a, b = int(quads[20050, 0]), int(quads[20050, 1])
+        quads[20050, 2] = b + (b - a)
+        pnums[35000] = pnums[100]
+    elif case == "young_before_missing_node":
+        young[20000] = 0.0
+        quads[35000, 2] = 10 ** 7
+    else:  # young_after_missing_node
+        quads[30000, 2] = 10 ** 7
+        young[35000] = 0.0
     g, o = both(len(numbers))
     g.add_nodes(numbers, xyz)
     o.add_nodes(numbers, xyz)
-    E, nu, t, ks = 70e9, 0.3, 0.02, 5 / 6
-    expect_same_failure(lambda: g.add_plates(pnums, quads, E, nu, t, ks),
-                        lambda: o.add_plates(pnums, quads, E, nu, t, ks))
+    nu, t, ks = 0.3, 0.02, 5 / 6
+    expect_same_failure(lambda: g.add_plates(pnums, quads, young, nu, t, ks),
+                        lambda: o.add_plates(pnums, quads, young, nu, t, ks))
     g.assemble()
     for a, b in zip(g.stiffness_csr(), o.csr()):
         np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
