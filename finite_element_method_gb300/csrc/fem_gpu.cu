@@ -2123,21 +2123,47 @@ size_t registry_pass(unsigned T, size_t limit, const uint8_t* own_a, const uint8
                      PB pb, int* role) {
   std::vector<size_t> first(T, limit);
   std::vector<int> which(T, 0);
-  const size_t ahead = 8 * (size_t)T;  // about 8 own items ahead
+  // every thread's checks as a list in item order (k << 1 | role B), made by a counting pass over T chunks, so
+  // that a thread walks its own items only rather than all of them
+  std::vector<size_t> cnt((size_t)T * T, 0), at((size_t)T * T, 0), len(T, 0);
+  parallel_chunks(T, limit, [&](unsigned c, size_t b, size_t e) {
+    size_t* n = &cnt[(size_t)c * T];
+    for (size_t k = b; k < e; ++k) {
+      if (own_a[k] < T) ++n[own_a[k]];
+      if (own_b[k] < T) ++n[own_b[k]];
+    }
+  });
+  for (unsigned t = 0; t < T; ++t) {
+    size_t run = 0;
+    for (unsigned c = 0; c < T; ++c) {
+      at[(size_t)c * T + t] = run;
+      run += cnt[(size_t)c * T + t];
+    }
+    len[t] = run;
+  }
+  std::vector<HostVec<uint64_t>> list(T);
+  run_threads(T, [&](unsigned t) { list[t].resize(len[t]); });
+  parallel_chunks(T, limit, [&](unsigned c, size_t b, size_t e) {
+    size_t* pos = &at[(size_t)c * T];
+    for (size_t k = b; k < e; ++k) {
+      if (own_a[k] < T) list[own_a[k]][pos[own_a[k]]++] = (uint64_t)k << 1;
+      if (own_b[k] < T) list[own_b[k]][pos[own_b[k]]++] = ((uint64_t)k << 1) | 1u;
+    }
+  });
   run_threads(T, [&](unsigned t) {
-    for (size_t k = 0; k < limit; ++k) {
-      if (k + ahead < limit) {
-        if (own_a[k + ahead] == t) pa(k + ahead);
-        if (own_b[k + ahead] == t) pb(k + ahead);
+    const HostVec<uint64_t>& my = list[t];
+    const size_t m = my.size(), ahead = 8;
+    for (size_t q = 0; q < m; ++q) {
+      if (q + ahead < m) {
+        const uint64_t w = my[q + ahead];
+        if (w & 1u) pb((size_t)(w >> 1));
+        else pa((size_t)(w >> 1));
       }
-      if (own_a[k] == t && !fa(k)) {
+      const uint64_t w = my[q];
+      const size_t k = (size_t)(w >> 1);
+      if (!(w & 1u) ? !fa(k) : !fb(k)) {
         first[t] = k;
-        which[t] = 1;
-        return;
-      }
-      if (own_b[k] == t && !fb(k)) {
-        first[t] = k;
-        which[t] = 2;
+        which[t] = (w & 1u) ? 2 : 1;
         return;
       }
     }
