@@ -267,7 +267,7 @@ def run_batch(args):
     plain_sequences(False)
     _, b = batch_build()
     b.close()
-    reps = max(1, min(3, args.e2e_steps))
+    reps = max(1, min(5, args.e2e_steps))
     t_plain = []
     for _ in range(reps - 1):
         t_plain.append(plain_sequences(False)[0])
@@ -930,7 +930,7 @@ def aux_results(args):
                                                                        "kernel")},
                          "clocks": beam["clocks"]}
     a = copy.copy(args)
-    a.e2e_steps = 3
+    a.e2e_steps = 5
     batch = run_batch(a)
     out["batch"] = {"workload": batch["config"]["workload"], "value": batch["value"], "unit": batch["unit"],
                     "from_arrays": batch["batch"]["from_arrays"], "numeric": batch["batch"]["numeric"],
