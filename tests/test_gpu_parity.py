@@ -344,6 +344,32 @@ def test_assemble_to_host_fresh_pattern(name):
     g2.close()
 
 
+def test_assemble_to_host_after_pattern_change():
+    """Nodes moved so that the exact-zero pattern changes (a flat mesh turned off the global planes): the
+    kept pattern's pass finds it changed, the symbolic phase runs again inside the same call and sends
+    the new pattern back while it runs; the host arrays hold the oracle's CSR of the moved mesh."""
+    q, _ = np.linalg.qr(np.random.default_rng(11).normal(size=(3, 3)))
+    flat = meshes.plate_mesh(30, 20, size=4.0)
+    tilted = meshes.plate_mesh(30, 20, size=4.0, rotation=q)
+    g = FEM(1e-12, 1e-12, flat.nodes_number)
+    meshes.load(g, flat)
+    o = OracleFEM(1e-12, 1e-12, tilted.nodes_number)
+    meshes.load(o, tilted)
+    rp0, ci0, va0 = o.csr()
+    rp = np.zeros(6 * flat.nodes_number + 1, np.int64)
+    ci = np.zeros(len(ci0) + 7, np.int32)
+    va = np.zeros(len(va0) + 7, np.float64)
+    nnz_flat = g.assemble_to_host(rp, ci, va)
+    assert nnz_flat < len(ci0)  # packed blocks in the plane
+    g.set_node_coordinates(tilted.xyz)
+    nnz = g.assemble_to_host(rp, ci, va)
+    assert nnz == len(ci0)
+    np.testing.assert_array_equal(rp, rp0)
+    np.testing.assert_array_equal(ci[:nnz], ci0)
+    np.testing.assert_array_equal(va[:nnz].view(np.uint64), va0.view(np.uint64))
+    g.close()
+
+
 def test_assemble_to_host_matches_assemble():
     m = meshes.plate_mesh(50, 40, size=5.0)
     g, o = build_pair(m)
