@@ -208,7 +208,9 @@ class FEM:
     def assemble_to_host(self, row_ptr, col_idx, values) -> int:
         """assemble() with the CSR read back into the given host arrays (row_ptr of 6 * nodes_number + 1
         int64, col_idx int32 and values float64 with room for the entries; page-locked arrays copy fastest):
-        the pattern travels back while the numeric pass runs.  Returns nnz."""
+        during a symbolic phase row_ptr travels back once the rows are counted and col_idx as the rows are
+        filled, otherwise the pattern travels back while the numeric pass runs; the values follow the pass.
+        Returns nnz."""
         rp = np.asarray(row_ptr)
         ci = np.asarray(col_idx)
         va = np.asarray(values)
