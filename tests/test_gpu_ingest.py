@@ -83,13 +83,26 @@ def test_bulk_nodes_then_continue_and_assemble():
 
 
 @pytest.mark.parametrize("kind", ["truss", "beam"])
-@pytest.mark.parametrize("case", ["number", "pair", "reversed_pair", "missing_node", "order"])
+@pytest.mark.parametrize("case", ["number", "pair", "reversed_pair", "missing_node", "order",
+                                  "young_before_number", "number_before_young", "young_after_missing_node"])
 def test_bulk_two_node_elements(kind, case):
+    """Bulk calls stop where the sequential calls would (the validation runs on the GPU while the host
+    checks the numbers, over the items before the first missing node)."""
     numbers, xyz, _, bars = grid()
     bars = bars.copy()
     m = len(bars)
     enums = np.arange(1, m + 1, dtype=np.uint32)
-    if case == "number":
+    young = np.full(m, 200e9 if kind == "truss" else 210e9)
+    if case == "young_before_number":
+        young[40000] = 0.0
+        enums[45000] = enums[3]
+    elif case == "number_before_young":
+        enums[40000] = enums[3]
+        young[45000] = -1.0
+    elif case == "young_after_missing_node":
+        bars[40000, 1] = 10 ** 7
+        young[45000] = 0.0
+    elif case == "number":
         enums[40000] = enums[3]
     elif case == "pair":
         bars[40000] = bars[77]
@@ -104,12 +117,12 @@ def test_bulk_two_node_elements(kind, case):
     g.add_nodes(numbers, xyz)
     o.add_nodes(numbers, xyz)
     if kind == "truss":
-        add_g = lambda: g.add_trusses(enums, bars, 200e9, 3e-4)
-        add_o = lambda: o.add_trusses(enums, bars, 200e9, 3e-4)
+        add_g = lambda: g.add_trusses(enums, bars, young, 3e-4)
+        add_o = lambda: o.add_trusses(enums, bars, young, 3e-4)
     else:
-        args = (210e9, 0.3, 1e-2, 3e-5, 8e-5, 0.0, 2e-5, 5 / 6, [0.0, 0.0, 1.0])
-        add_g = lambda: g.add_beams(enums, bars, *args)
-        add_o = lambda: o.add_beams(enums, bars, *args)
+        args = (0.3, 1e-2, 3e-5, 8e-5, 0.0, 2e-5, 5 / 6, [0.0, 0.0, 1.0])
+        add_g = lambda: g.add_beams(enums, bars, young, *args)
+        add_o = lambda: o.add_beams(enums, bars, young, *args)
     expect_same_failure(add_g, add_o)
     counts = g.element_counts()
     assert counts[0 if kind == "truss" else 1] == (50000 if case == "order" else 40000)
