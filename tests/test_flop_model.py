@@ -1,0 +1,53 @@
+"""The bench's algorithmic FP64 work per plate (bench.PLATE_FLOPS, the roofline's numerator) against an
+operation count of the device arithmetic itself: tests/flops/count_plate_ops.cpp compiles
+element_math.cuh on the host with a counting number type (adds, multiplications, divisions and square
+roots one flop, a fused multiply-add two) and runs the plate's rotation and local coordinates, its
+element core and its ten node-pair blocks, for a plate in a global plane (R = I) and one off the planes."""
+import os
+import re
+import shutil
+import subprocess
+import sys
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, ROOT)
+
+
+def counts(tmp_path):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    exe = str(tmp_path / "count_plate_ops")
+    subprocess.run([cxx, "-std=c++17", "-O1", "-o", exe, os.path.join(HERE, "flops", "count_plate_ops.cpp")],
+                   check=True, capture_output=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    res, case = {}, None
+    for line in out.splitlines():
+        m = re.match(r"(\w+) identity=(\d)", line)
+        if m:
+            case = m.group(1)
+            res[case] = {"identity": m.group(2) == "1"}
+            continue
+        m = re.match(r"\s+(\w+) add=(\d+) mul=(\d+) fma=(\d+) div=(\d+) sqrt=(\d+) flops=(\d+)", line)
+        if m:
+            res[case][m.group(1)] = dict(zip(("add", "mul", "fma", "div", "sqrt", "flops"), map(int, m.groups()[1:])))
+            continue
+        m = re.match(r"\s+total=(\d+)", line)
+        if m:
+            res[case]["total"] = int(m.group(1))
+    return res
+
+
+def test_plate_flop_model_matches_the_device_arithmetic(tmp_path):
+    import bench
+
+    c = counts(tmp_path)
+    assert c["flat"]["identity"] and not c["tilted"]["identity"]
+    assert c["flat"]["total"] == bench.PLATE_FLOPS["flat"] == 932
+    assert c["tilted"]["total"] == bench.PLATE_FLOPS["tilted"] == 2480
+    # the element core is the same on both paths; only the rotation and the blocks differ
+    assert c["flat"]["core"] == c["tilted"]["core"]
+    assert c["flat"]["core"]["flops"] == 583
