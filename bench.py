@@ -44,9 +44,10 @@ FP64_PEAK_FLOPS = 2 * 152 * 2070e6 * 2
 #   plate off the global planes (general R): rotation and local coordinates 30 add + 39 mul + 21 fma + 3 div +
 #   3 sqrt, core as above, 10 blocks with their rotation R^T K R on the structural entries 548 mul + 616 fma
 #   = 2480
-#   beam, I12 != 0: 57 add + 213 mul + 201 fma + 19 div + 7 sqrt (trig as polynomial fma chains) = 698;
+#   beam, I12 != 0: 57 add + 213 mul + 201 fma + 19 div + 7 sqrt (trig as polynomial fma chains) = 698 when
+#   I11 >= I22, 897 when I11 < I22 (one more turn of the principal-axes loop: arctangent, sine and cosine);
 #   I12 == 0 (principal axes along the section axes, no arctangent and series): 515 when I11 >= I22, and
-#   714 when I11 < I22 (one turn of the principal-axes loop: arctangent, sine and cosine)
+#   714 when I11 < I22 (one turn of the loop)
 #   truss: 20 add + 46 mul + 9 fma + 4 div + 4 sqrt
 PLATE_FLOPS = {"flat": (15 + 6) + (20 + 145 + 2 * 208 + 2) + (20 + 2 * 154),
                "tilted": (30 + 39 + 2 * 21 + 3 + 3) + (20 + 145 + 2 * 208 + 2) + (548 + 2 * 616)}
@@ -55,7 +56,7 @@ WORK = {
     "beam": dict(elem_flops=57 + 213 + 2 * 201 + 19 + 7, pairs=3),
     "truss": dict(elem_flops=20 + 46 + 2 * 9 + 4 + 4, pairs=3),
 }
-BEAM_FLOPS = {"general": 698, "aligned": 515, "aligned_turn": 714}
+BEAM_FLOPS = {"general": 698, "general_turn": 897, "aligned": 515, "aligned_turn": 714}
 
 
 def element_flops(workload, mesh):
@@ -66,9 +67,9 @@ def element_flops(workload, mesh):
         return WORK[workload]["elem_flops"] * mesh.n_elements
     b = mesh.beams
     aligned = np.asarray(b["i12"]) == 0.0
-    turn = aligned & (np.asarray(b["i11"]) < np.asarray(b["i22"]))
-    return (BEAM_FLOPS["general"] * int((~aligned).sum()) + BEAM_FLOPS["aligned"] * int((aligned & ~turn).sum())
-            + BEAM_FLOPS["aligned_turn"] * int(turn.sum()))
+    turn = np.asarray(b["i11"]) < np.asarray(b["i22"])
+    return (BEAM_FLOPS["general"] * int((~aligned & ~turn).sum()) + BEAM_FLOPS["general_turn"] * int((~aligned & turn).sum())
+            + BEAM_FLOPS["aligned"] * int((aligned & ~turn).sum()) + BEAM_FLOPS["aligned_turn"] * int((aligned & turn).sum()))
 # bytes per element read by the element kernel (connectivity, coordinates of its nodes, properties)
 IN_BYTES = {"plate": 4 * 4 + 4 * 24 + 4 * 8, "beam": 2 * 4 + 2 * 24 + 11 * 8, "truss": 2 * 4 + 2 * 24 + 3 * 8}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per element of one launch of the element kernel,

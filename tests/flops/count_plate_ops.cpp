@@ -1,10 +1,13 @@
-// Floating-point operations of the plate element arithmetic, counted by compiling the device header
+// Floating-point operations of the plate and beam element arithmetic, counted by compiling the device header
 // element_math.cuh on the host with an operation-counting number type: the algorithmic work the bench's
 // roofline divides by (adds and subtractions, multiplications, divisions and square roots one flop each,
 // a fused multiply-add two).  Prints, for a plate in a global plane (R = I: the identity fast path) and a
 // plate off the planes (general rotation), the operation counts of the rotation and local coordinates, of
-// the element core and of the ten node-pair blocks.  Test infrastructure: tests/test_flop_model.py builds
-// and runs it.
+// the element core and of the ten node-pair blocks; and for a beam the counts of its blocks for sections
+// with I12 != 0 and with I12 = 0, each with I11 > I22 and with I11 < I22 (one more turn of the
+// principal-axes loop).  The header's transcendentals are double-only; their Cnt versions below add the operations of
+// the double code (the same argument reduction and series).  Test infrastructure:
+// tests/test_flop_model.py builds and runs it.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -78,6 +81,31 @@ inline bool bits_positive(Cnt v) { return v.v > 0.0; }
 
 using namespace femgpu;
 
+// the header's transcendentals for Cnt: the value of the double code, with its operations counted
+// (reduce_pio2: one multiplication and three fmas; sincos_reduced, both series: r^2 and r r^2, nine fmas
+// for the sine's polynomial and one to finish it, ten for the cosine's and one to finish it; the
+// arctangent: see datan)
+inline Cnt dsin(Cnt x) {
+  g_ops.mul += 1 + 2;
+  g_ops.fma += 3 + 9 + 1 + 10 + 1;
+  return Cnt(femgpu::dsin(x.v));
+}
+inline Cnt dcos(Cnt x) {
+  g_ops.mul += 1 + 2;
+  g_ops.fma += 3 + 9 + 1 + 10 + 1;
+  return Cnt(femgpu::dcos(x.v));
+}
+inline Cnt datan(Cnt t) {
+  const double a = std::fabs(t.v);
+  const bool inv = a > 1.0;
+  g_ops.div += inv ? 2 : 1;  // 1 / a; (a - c) / (1 + a c)
+  g_ops.mul += 4;            // a 8, k / 8, u u, u u^2
+  g_ops.add += inv ? 4 : 2;  // a - c, the table value + the series; pi/2 - res + its low part
+  g_ops.fma += 9;            // 1 + a c, seven series terms, u + u^3 p
+  return Cnt(femgpu::datan(t.v));
+}
+inline Cnt dacos(Cnt x) { return 2.0 * datan(sqrt((1.0 - x) / (1.0 + x))); }
+
 template <int I, int J, bool ROT>
 static void pair(const PlateCoreT<Cnt>& C, const Cnt R[9]) {
   Cnt blk[36];
@@ -136,6 +164,17 @@ static void count(const char* name, const double P[4][3]) {
   std::printf("  total=%ld\n", geo.flops() + core.flops() + blk.flops());
 }
 
+static void count_beam(const char* name, double i11, double i22, double i12) {
+  const Cnt x1[3] = {Cnt(0.03), Cnt(-0.02), Cnt(0.01)}, x2[3] = {Cnt(2.98), Cnt(0.05), Cnt(-0.04)};
+  const Cnt axis[3] = {Cnt(0.0), Cnt(0.0), Cnt(1.0)};
+  g_ops = Ops();
+  BeamBlocksT<Cnt> B;
+  const bool ok = beam_blocks(x1, x2, Cnt(210e9), Cnt(0.3), Cnt(1e-2), Cnt(i11), Cnt(i22), Cnt(i12), Cnt(2e-5),
+                              Cnt(5.0 / 6.0), axis, 1e-6, 1e-12, B);
+  std::printf("beam_%s ok=%d\n", name, ok ? 1 : 0);
+  report("  blocks", g_ops);
+}
+
 int main() {
   // a distorted quadrilateral in z = 0, counter-clockwise
   const double flat[4][3] = {{1.1, 1.05, 0.0}, {0.02, 0.97, 0.0}, {-0.03, 0.01, 0.0}, {1.04, -0.02, 0.0}};
@@ -151,5 +190,9 @@ int main() {
   }
   count("flat", flat);
   count("tilted", tilted);
+  count_beam("general", 8e-5, 3e-5, 2e-5);
+  count_beam("general_turn", 3e-5, 8e-5, 2e-5);
+  count_beam("aligned", 8e-5, 3e-5, 0.0);
+  count_beam("aligned_turn", 3e-5, 8e-5, 0.0);
   return 0;
 }

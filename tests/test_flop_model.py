@@ -2,7 +2,9 @@
 operation count of the device arithmetic itself: tests/flops/count_plate_ops.cpp compiles
 element_math.cuh on the host with a counting number type (adds, multiplications, divisions and square
 roots one flop, a fused multiply-add two) and runs the plate's rotation and local coordinates, its
-element core and its ten node-pair blocks, for a plate in a global plane (R = I) and one off the planes."""
+element core and its ten node-pair blocks, for a plate in a global plane (R = I) and one off the planes;
+and the beam's blocks (bench.BEAM_FLOPS) for the four section cases: I12 != 0 or I12 = 0, each with
+I11 >= I22 or I11 < I22."""
 import os
 import re
 import shutil
@@ -26,10 +28,10 @@ def counts(tmp_path):
     out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
     res, case = {}, None
     for line in out.splitlines():
-        m = re.match(r"(\w+) identity=(\d)", line)
+        m = re.match(r"(\w+) (identity|ok)=(\d)", line)
         if m:
             case = m.group(1)
-            res[case] = {"identity": m.group(2) == "1"}
+            res[case] = {m.group(2): m.group(3) == "1"}
             continue
         m = re.match(r"\s+(\w+) add=(\d+) mul=(\d+) fma=(\d+) div=(\d+) sqrt=(\d+) flops=(\d+)", line)
         if m:
@@ -51,3 +53,13 @@ def test_plate_flop_model_matches_the_device_arithmetic(tmp_path):
     # the element core is the same on both paths; only the rotation and the blocks differ
     assert c["flat"]["core"] == c["tilted"]["core"]
     assert c["flat"]["core"]["flops"] == 583
+
+
+def test_beam_flop_model_matches_the_device_arithmetic(tmp_path):
+    import bench
+
+    c = counts(tmp_path)
+    for case in ("general", "general_turn", "aligned", "aligned_turn"):
+        assert c["beam_" + case]["ok"]
+        assert c["beam_" + case]["blocks"]["flops"] == bench.BEAM_FLOPS[case], case
+    assert bench.WORK["beam"]["elem_flops"] == bench.BEAM_FLOPS["general"]
