@@ -251,7 +251,6 @@ int ba_replay(double rel_tol, double abs_tol, const fem_gpu_structures_t* in, si
   return st;
 }
 
-// the element kinds of the input, in call order
 // A caller's host array to the device.  Where the GPU reads pageable host memory itself
 // (cudaDevAttrPageableMemoryAccess: address translation over the host link, as on Grace systems), a
 // kernel reads it at the link's rate; a pageable cudaMemcpyAsync goes through the driver's staging, which
@@ -287,6 +286,7 @@ cudaError_t host_to_device(void* dst, const void* src, size_t bytes, cudaStream_
                          cudaMemcpyHostToDevice, s);
 }
 
+// the element kinds of the input, in call order
 struct BaKind {
   int kind;
   int per_el;                   // nodes per element
