@@ -263,19 +263,22 @@ __global__ void k_read_host(const uint4* __restrict__ src, uint4* __restrict__ d
 }
 constexpr size_t kDirectReadBytes = 1u << 20;
 cudaError_t host_to_device(void* dst, const void* src, size_t bytes, cudaStream_t s, int sm_count) {
-  static int direct[64];
-  static bool known[64];
+  static std::atomic<int> direct[64];  // per device: 0 = not asked yet, 1 = reads in place, 2 = copies
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev >= 0 && dev < 64 && !known[dev]) {
-    int v = 0;
-    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) v = 0;
-    direct[dev] = v;
-    known[dev] = true;
+  int mode = 2;
+  if (dev >= 0 && dev < 64) {
+    mode = direct[dev].load(std::memory_order_relaxed);
+    if (!mode) {
+      int v = 0;
+      if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) v = 0;
+      mode = v ? 1 : 2;
+      direct[dev].store(mode, std::memory_order_relaxed);
+    }
   }
-  const bool use = dev >= 0 && dev < 64 && direct[dev] && bytes >= kDirectReadBytes &&
-                   ((uintptr_t)src % 16) == 0 && ((uintptr_t)dst % 16) == 0;
+  const bool use = mode == 1 && bytes >= kDirectReadBytes && ((uintptr_t)src % 16) == 0 &&
+                   ((uintptr_t)dst % 16) == 0;
   if (!use) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
   const size_t n16 = bytes / 16, tail = bytes - n16 * 16;
   k_read_host<<<(unsigned)std::max(1, sm_count * 4), 256, 0, s>>>(static_cast<const uint4*>(src),

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -1085,11 +1086,15 @@ __global__ void __launch_bounds__(512) k_block_sums(size_t n_desc, size_t n_sums
 }
 // CTAs of a block-sum launch: enough to fill the SMs a few times over, each looping over its share
 unsigned block_sums_grid(size_t n_desc, unsigned block) {
-  static int sms[64] = {};
+  static std::atomic<int> sms[64];  // per device, 0 = not asked yet (calls may come from several threads)
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
-  if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms[dev] = 1;
-  const size_t want = (n_desc + block - 1) / block, cap = (size_t)sms[dev] * (2048 / block) * 2;
+  int n = sms[dev].load(std::memory_order_relaxed);
+  if (!n) {
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
+    sms[dev].store(n, std::memory_order_relaxed);
+  }
+  const size_t want = (n_desc + block - 1) / block, cap = (size_t)n * (2048 / block) * 2;
   return (unsigned)std::max<size_t>(1, std::min(want, cap));
 }
 
