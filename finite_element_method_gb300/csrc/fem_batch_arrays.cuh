@@ -363,6 +363,15 @@ extern "C" int fem_gpu_batch_create_from_arrays(double rel_tol, double abs_tol, 
   st = ensure_ready(h);
   if (st) return b->fail(st, "%s", h->err.c_str());
   cudaStream_t s = h->stream;
+  // Kernels on s read the caller's arrays in place (host_to_device); every return from here on, a failure
+  // included, waits for s, so that nothing still reads them once the call is back.
+  struct DrainOnReturn {
+    cudaStream_t s;
+    ~DrainOnReturn() {
+      cudaStreamCaptureStatus c = cudaStreamCaptureStatusNone;
+      if (cudaStreamIsCapturing(s, &c) == cudaSuccess && c == cudaStreamCaptureStatusNone) cudaStreamSynchronize(s);
+    }
+  } drain_on_return{s};
   auto cerr = [&](int code) { return b->fail(code, "%s", h->err.c_str()); };
 #define BAK(call)                                     \
   do {                                                \

@@ -235,7 +235,8 @@ int fem_gpu_batch_autotune(fem_gpu_batch_t* b, int reps, const char* cache_path,
  * status and message are those of the structure's first failing call, the
  * message prefixed by "structure i: ".  Structure i's CSR (fem_gpu_batch_get_csr)
  * is bit-identical to its plain assembly.  truss_area2 may be NULL (no second
- * area); a NULL offset array means no element of that kind. */
+ * area); a NULL offset array means no element of that kind.  The call is
+ * synchronous, failures included: no array is read after it returns. */
 typedef struct fem_gpu_structures {
   size_t n_structures;
   const uint32_t* nodes_number; /* per structure: the nodes_number of its fem_gpu_create */
