@@ -3402,15 +3402,17 @@ extern "C" int fem_gpu_assemble_to_host(fem_gpu_t* h, int64_t* row_ptr, int32_t*
     CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&h->copy_ev, cudaEventDisableTiming));
   }
+  // no copy into the caller's buffers outlives the call, whichever way it returns
+  struct DrainOnReturn {
+    cudaStream_t s;
+    ~DrainOnReturn() { cudaStreamSynchronize(s); }
+  } drain_on_return{h->copy_stream};
   const size_t nrows = (size_t)h->nodes_number * 6;
   for (int attempt = 0; attempt < 2; ++attempt) {
     PatternCopy pc{row_ptr, col_idx, nnz_capacity};
     if (!h->pattern_valid) {
       st = symbolic(h, &pc);
-      if (st) {
-        cudaStreamSynchronize(h->copy_stream);  // no copy into the caller's buffers outlives the call
-        return st;
-      }
+      if (st) return st;
     }
     if (nnz) *nnz = h->nnz;
     if (h->nnz > nnz_capacity)
@@ -3422,10 +3424,7 @@ extern "C" int fem_gpu_assemble_to_host(fem_gpu_t* h, int64_t* row_ptr, int32_t*
       CK(cudaStreamWaitEvent(h->copy_stream, h->copy_ev, 0));
     }
     st = numeric_launch(h);
-    if (st) {
-      cudaStreamSynchronize(h->copy_stream);
-      return st;
-    }
+    if (st) return st;
     if (!pc.issued) {
       CK(cudaMemcpyAsync(row_ptr, h->row_ptr.p, (nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost,
                          h->copy_stream));
