@@ -1,5 +1,5 @@
 """The bench's algorithmic FP64 work per plate (bench.PLATE_FLOPS, the roofline's numerator) against an
-operation count of the device arithmetic itself: tests/flops/count_plate_ops.cpp compiles
+operation count of the device arithmetic itself: tests/flops/count_element_ops.cpp compiles
 element_math.cuh on the host with a counting number type (adds, multiplications, divisions and square
 roots one flop, a fused multiply-add two) and runs the plate's rotation and local coordinates, its
 element core and its ten node-pair blocks, for a plate in a global plane (R = I) and one off the planes;
@@ -22,8 +22,8 @@ def counts(tmp_path):
     cxx = shutil.which("g++") or shutil.which("c++")
     if not cxx:
         pytest.skip("no C++ compiler")
-    exe = str(tmp_path / "count_plate_ops")
-    subprocess.run([cxx, "-std=c++17", "-O1", "-o", exe, os.path.join(HERE, "flops", "count_plate_ops.cpp")],
+    exe = str(tmp_path / "count_element_ops")
+    subprocess.run([cxx, "-std=c++17", "-O1", "-o", exe, os.path.join(HERE, "flops", "count_element_ops.cpp")],
                    check=True, capture_output=True)
     out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
     res, case = {}, None
