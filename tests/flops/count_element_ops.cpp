@@ -1,11 +1,12 @@
-// Floating-point operations of the plate and beam element arithmetic, counted by compiling the device header
+// Floating-point operations of the plate, beam and truss element arithmetic, counted by compiling the device header
 // element_math.cuh on the host with an operation-counting number type: the algorithmic work the bench's
 // roofline divides by (adds and subtractions, multiplications, divisions and square roots one flop each,
 // a fused multiply-add two).  Prints, for a plate in a global plane (R = I: the identity fast path) and a
 // plate off the planes (general rotation), the operation counts of the rotation and local coordinates, of
 // the element core and of the ten node-pair blocks; and for a beam the counts of its blocks for sections
 // with I12 != 0 and with I12 = 0, each with I11 > I22 and with I11 < I22 (one more turn of the
-// principal-axes loop).  The header's transcendentals are double-only; their Cnt versions below add the operations of
+// principal-axes loop); and for a truss the counts of its block for an oblique bar (without and with a
+// second area) and a bar along x.  The header's transcendentals are double-only; their Cnt versions below add the operations of
 // the double code (the same argument reduction and series).  Test infrastructure:
 // tests/test_flop_model.py builds and runs it.
 #include <cmath>
@@ -175,6 +176,16 @@ static void count_beam(const char* name, double i11, double i22, double i12) {
   report("  blocks", g_ops);
 }
 
+static void count_truss(const char* name, const double d[3], double area2) {
+  const Cnt x1[3] = {Cnt(0.02), Cnt(-0.01), Cnt(0.03)};
+  const Cnt x2[3] = {Cnt(0.02 + d[0]), Cnt(-0.01 + d[1]), Cnt(0.03 + d[2])};
+  g_ops = Ops();
+  Cnt g[9];
+  const bool ok = truss_block(x1, x2, Cnt(200e9), Cnt(3e-4), Cnt(area2), 1e-12, g);
+  std::printf("truss_%s ok=%d\n", name, ok ? 1 : 0);
+  report("  blocks", g_ops);
+}
+
 int main() {
   // a distorted quadrilateral in z = 0, counter-clockwise
   const double flat[4][3] = {{1.1, 1.05, 0.0}, {0.02, 0.97, 0.0}, {-0.03, 0.01, 0.0}, {1.04, -0.02, 0.0}};
@@ -194,5 +205,9 @@ int main() {
   count_beam("general_turn", 3e-5, 8e-5, 2e-5);
   count_beam("aligned", 8e-5, 3e-5, 0.0);
   count_beam("aligned_turn", 3e-5, 8e-5, 0.0);
+  const double oblique[3] = {0.97, 1.04, -0.03}, along_x[3] = {1.0, 0.0, 0.0};
+  count_truss("general", oblique, std::nan(""));
+  count_truss("general_area2", oblique, 5e-4);
+  count_truss("along_x", along_x, std::nan(""));
   return 0;
 }

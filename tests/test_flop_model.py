@@ -3,8 +3,8 @@ operation count of the device arithmetic itself: tests/flops/count_element_ops.c
 element_math.cuh on the host with a counting number type (adds, multiplications, divisions and square
 roots one flop, a fused multiply-add two) and runs the plate's rotation and local coordinates, its
 element core and its ten node-pair blocks, for a plate in a global plane (R = I) and one off the planes;
-and the beam's blocks (bench.BEAM_FLOPS) for the four section cases: I12 != 0 or I12 = 0, each with
-I11 >= I22 or I11 < I22."""
+the beam's blocks (bench.BEAM_FLOPS) for the four section cases: I12 != 0 or I12 = 0, each with
+I11 >= I22 or I11 < I22; and the truss block of an oblique bar (bench.WORK["truss"])."""
 import os
 import re
 import shutil
@@ -63,3 +63,14 @@ def test_beam_flop_model_matches_the_device_arithmetic(tmp_path):
         assert c["beam_" + case]["ok"]
         assert c["beam_" + case]["blocks"]["flops"] == bench.BEAM_FLOPS[case], case
     assert bench.WORK["beam"]["elem_flops"] == bench.BEAM_FLOPS["general"]
+
+
+def test_truss_flop_model_matches_the_device_arithmetic(tmp_path):
+    import bench
+
+    c = counts(tmp_path)
+    assert all(c["truss_" + k]["ok"] for k in ("general", "general_area2", "along_x"))
+    assert c["truss_general"]["blocks"]["flops"] == bench.WORK["truss"]["elem_flops"] == 92
+    # a second area adds its mean (one subtraction, one product, one addition); a bar along x has R = I
+    assert c["truss_general_area2"]["blocks"]["flops"] == 95
+    assert c["truss_along_x"]["blocks"]["flops"] == 69
