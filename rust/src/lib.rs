@@ -14,6 +14,15 @@
 //! | [`FEM::add_beam`] | `add_beam` (src/fem/methods_for_beam_data_handle.rs:49) |
 //! | [`FEM::add_plate`] | `add_plate` (src/fem/methods_for_plate_data_handle.rs:62) |
 //! | [`FEM::get_truss_rotation_matrix_elements`] and the beam / plate forms | src/fem/fem.rs:171-202 |
+//! | [`FEM::add_displacement`], [`FEM::add_concentrated_load`], [`FEM::add_uniformly_distributed_line_load`], [`FEM::add_uniformly_distributed_surface_load`] | src/fem/methods_for_bc_data_handle.rs:34-203 |
+//! | [`FEM::separate_stiffness_matrix_sparse_iterative`], [`FEM::compose_r_a_vector`], [`FEM::compose_u_b_vector`] | src/fem/methods_for_separate_stiffness_matrix.rs:217-342 |
+//! | [`FEM::find_ua_vector_iterative_pcg_jacobi_sparse`], [`FEM::find_ua_vector_iterative_pcg_block_jacobi_sparse`], [`FEM::find_r_r_vector_sparse`], [`FEM::compose_global_analysis_result`], [`FEM::extract_global_analysis_result`] | src/fem/methods_for_global_analysis.rs:189-387 |
+//! | [`FEM::extract_elements_analysis_result`] | src/fem/methods_for_element_analysis.rs:27-58 |
+//!
+//! The separation, the solution, the reactions and the element results run on the GPU; the crate's
+//! `Vector<V>` is a `Vec<f64>` here.  Where the crate walks a `HashMap` (the nodes in
+//! `extract_global_analysis_result`, the elements in `extract_elements_analysis_result`) the order here
+//! is insertion order.
 //!
 //! The reference assembles eagerly inside every `add_*`; here `add_*` checks the
 //! element exactly as the reference does (same checks, same order, same
@@ -31,6 +40,7 @@
 
 pub mod ffi;
 
+use std::collections::HashMap;
 use std::ffi::CStr;
 use std::os::raw::c_int;
 use std::ptr;
@@ -60,6 +70,14 @@ pub struct Vjp {
 pub struct FEM {
     h: *mut ffi::FemGpu,
     nodes_number: u32,
+    /// the reference's imposed_constraints: one flag per DOF (6 * nodes_number)
+    imposed: Vec<u8>,
+    /// the reference's displacements_vector: imposed values, then the solution once composed
+    displacements: Vec<f64>,
+    /// the forces vector with the reactions at the restrained DOFs, after compose_global_analysis_result
+    result_forces: Option<Vec<f64>>,
+    /// node number -> node index, for the nodes looked up so far (nodes are only ever appended)
+    node_index: HashMap<u32, usize>,
 }
 
 // The handle owns its device memory and one CUDA stream; it may move between
@@ -73,7 +91,15 @@ impl FEM {
         let mut h = ptr::null_mut();
         let st = unsafe { ffi::fem_gpu_create(rel_tol, abs_tol, nodes_number, &mut h) };
         assert!(st == 0 && !h.is_null(), "fem_gpu_create failed with status {st}");
-        FEM { h, nodes_number }
+        let ndof = 6 * nodes_number as usize;
+        FEM {
+            h,
+            nodes_number,
+            imposed: vec![0; ndof],
+            displacements: vec![0.0; ndof],
+            result_forces: None,
+            node_index: HashMap::new(),
+        }
     }
 
     fn check(&self, st: c_int) -> Result<(), String> {
@@ -331,6 +357,307 @@ impl FEM {
         };
         self.check(st).map(|_| out)
     }
+
+    // -- boundary conditions, loads, solution and results (the callers either side of the assembly) --
+
+    /// The node index of a node number (None: no such node).  Nodes are only appended, so the map is
+    /// extended with the nodes added since the last lookup.
+    fn node_index_of(&mut self, number: u32) -> Result<Option<usize>, String> {
+        let mut count = 0i64;
+        self.check(unsafe { ffi::fem_gpu_get_node_count(self.h, &mut count) })?;
+        let count = count as usize;
+        if self.node_index.len() < count {
+            let mut numbers = vec![0u32; count];
+            self.check(unsafe { ffi::fem_gpu_get_index_node_numbers(self.h, numbers.as_mut_ptr()) })?;
+            let known = self.node_index.len();
+            for (i, n) in numbers.iter().enumerate().skip(known) {
+                self.node_index.insert(*n, i);
+            }
+        }
+        Ok(self.node_index.get(&number).copied())
+    }
+
+    /// `add_displacement(node_number, dof_parameter, value)` (methods_for_bc_data_handle.rs:176-203):
+    /// imposes a displacement on one DOF; a DOF takes one imposed displacement.
+    pub fn add_displacement(&mut self, node_number: u32, dof_parameter: DOFParameter, value: f64) -> Result<(), String> {
+        let index = match self.node_index_of(node_number)? {
+            Some(i) => 6 * i + dof_parameter as usize,
+            None => return Err(format!("Node with number {node_number} does not exist!")),
+        };
+        if self.imposed[index] != 0 {
+            return Err(format!("Displacement {dof_parameter:?} already applied to node {node_number}!"));
+        }
+        self.imposed[index] = 1;
+        self.displacements[index] = value;
+        Ok(())
+    }
+
+    fn load(
+        &mut self,
+        f: unsafe extern "C" fn(*mut ffi::FemGpu, *const u32, *const u8, *const f64, usize, *mut usize) -> c_int,
+        number: u32,
+        dof_parameter: DOFParameter,
+        value: f64,
+    ) -> Result<(), String> {
+        let (dof, mut n) = (dof_parameter as u8, 0usize);
+        let st = unsafe { f(self.h, &number, &dof, &value, 1, &mut n) };
+        self.check(st)
+    }
+
+    /// `add_concentrated_load(node_number, dof_parameter, value)` (methods_for_bc_data_handle.rs:34-56).
+    pub fn add_concentrated_load(&mut self, node_number: u32, dof_parameter: DOFParameter, value: f64) -> Result<(), String> {
+        self.load(ffi::fem_gpu_add_concentrated_loads, node_number, dof_parameter, value)
+    }
+
+    /// `add_uniformly_distributed_line_load(beam_element_number, dof_parameter, value)`
+    /// (methods_for_bc_data_handle.rs:58-101): the beam's equivalent nodal loads, from its geometry now.
+    pub fn add_uniformly_distributed_line_load(
+        &mut self,
+        beam_element_number: u32,
+        dof_parameter: DOFParameter,
+        value: f64,
+    ) -> Result<(), String> {
+        self.load(ffi::fem_gpu_add_line_loads, beam_element_number, dof_parameter, value)
+    }
+
+    /// `add_uniformly_distributed_surface_load(plate_element_number, dof_parameter, value)`
+    /// (methods_for_bc_data_handle.rs:103-175).
+    pub fn add_uniformly_distributed_surface_load(
+        &mut self,
+        plate_element_number: u32,
+        dof_parameter: DOFParameter,
+        value: f64,
+    ) -> Result<(), String> {
+        self.load(ffi::fem_gpu_add_surface_loads, plate_element_number, dof_parameter, value)
+    }
+
+    /// The forces vector (6 * nodes_number, DOF order): every load's nodal contributions in call order.
+    pub fn forces_vector(&self) -> Result<Vec<f64>, String> {
+        let mut f = vec![0.0f64; 6 * self.nodes_number as usize];
+        self.check(unsafe { ffi::fem_gpu_get_forces(self.h, f.as_mut_ptr()) })?;
+        Ok(f)
+    }
+
+    /// `separate_stiffness_matrix_sparse_iterative()` (methods_for_separate_stiffness_matrix.rs:217-320) of
+    /// the assembled stiffness, on the GPU: K_aa, K_ab, K_ba, K_bb as triplets in (row, column) order.  The
+    /// blocks also stay with the model for the solution calls below, until its next assembly.
+    pub fn separate_stiffness_matrix_sparse_iterative(&self) -> Result<SeparatedStiffnessMatrixSparse, String> {
+        self.check(unsafe { ffi::fem_gpu_separate_sparse(self.h, self.imposed.as_ptr()) })?;
+        let (mut n_aa, mut n_bb, mut nnz) = (0i64, 0i64, [0i64; 4]);
+        self.check(unsafe { ffi::fem_gpu_get_separation_sizes(self.h, &mut n_aa, &mut n_bb, nnz.as_mut_ptr()) })?;
+        let (n_aa, n_bb) = (n_aa as usize, n_bb as usize);
+        let (mut aa, mut bb) = (vec![0i64; n_aa], vec![0i64; n_bb]);
+        self.check(unsafe { ffi::fem_gpu_get_separation_indexes(self.h, aa.as_mut_ptr(), bb.as_mut_ptr()) })?;
+        let mut blocks: Vec<Vec<(usize, usize, f64)>> = Vec::with_capacity(4);
+        for which in 0..4usize {
+            let rows = if which < 2 { n_aa } else { n_bb };
+            let mut row_ptr = vec![0i64; rows + 1];
+            let mut col_idx = vec![0i32; nnz[which] as usize];
+            let mut values = vec![0.0f64; nnz[which] as usize];
+            let st = unsafe {
+                ffi::fem_gpu_get_separation_block(
+                    self.h,
+                    which as c_int,
+                    row_ptr.as_mut_ptr(),
+                    col_idx.as_mut_ptr(),
+                    values.as_mut_ptr(),
+                )
+            };
+            self.check(st)?;
+            let mut t = Vec::with_capacity(values.len());
+            for r in 0..rows {
+                for k in row_ptr[r] as usize..row_ptr[r + 1] as usize {
+                    t.push((r, col_idx[k] as usize, values[k]));
+                }
+            }
+            blocks.push(t);
+        }
+        let k_bb_triplets = blocks.pop().unwrap_or_default();
+        let k_ba_triplets = blocks.pop().unwrap_or_default();
+        let k_ab_triplets = blocks.pop().unwrap_or_default();
+        let k_aa_triplets = blocks.pop().unwrap_or_default();
+        Ok(SeparatedStiffnessMatrixSparse {
+            k_aa_indexes: aa.iter().map(|&i| i as usize).collect(),
+            k_bb_indexes: bb.iter().map(|&i| i as usize).collect(),
+            k_aa_triplets,
+            k_ab_triplets,
+            k_ba_triplets,
+            k_bb_triplets,
+            n_aa,
+            n_bb,
+        })
+    }
+
+    /// `compose_r_a_vector(k_aa_indexes)` (methods_for_separate_stiffness_matrix.rs:322-331): the forces at
+    /// the free DOFs.
+    pub fn compose_r_a_vector(&self, k_aa_indexes: &Vec<usize>) -> Result<Vec<f64>, String> {
+        let f = self.forces_vector()?;
+        Ok(k_aa_indexes.iter().map(|&i| f[i]).collect())
+    }
+
+    /// `compose_u_b_vector(k_bb_indexes)` (methods_for_separate_stiffness_matrix.rs:333-342): the imposed
+    /// displacements at the restrained DOFs.
+    pub fn compose_u_b_vector(&self, k_bb_indexes: &Vec<usize>) -> Result<Vec<f64>, String> {
+        Ok(k_bb_indexes.iter().map(|&i| self.displacements[i]).collect())
+    }
+
+    fn pcg(
+        &self,
+        sep: &SeparatedStiffnessMatrixSparse,
+        r_a_vector: &Vec<f64>,
+        u_b_vector: &Vec<f64>,
+        max_iter: usize,
+        block_jacobi: bool,
+    ) -> Result<(Vec<f64>, usize), String> {
+        if r_a_vector.len() != sep.n_aa || u_b_vector.len() != sep.n_bb {
+            return Err("r_a / u_b vector sizes do not match the separation".to_string());
+        }
+        let mut u_a = vec![0.0f64; sep.n_aa];
+        let mut iterations: c_int = 0;
+        let st = unsafe {
+            ffi::fem_gpu_solve_pcg(
+                self.h,
+                r_a_vector.as_ptr(),
+                u_b_vector.as_ptr(),
+                block_jacobi as c_int,
+                max_iter.min(c_int::MAX as usize) as c_int,
+                u_a.as_mut_ptr(),
+                &mut iterations,
+            )
+        };
+        self.check(st).map(|_| (u_a, iterations as usize))
+    }
+
+    /// `find_ua_vector_iterative_pcg_jacobi_sparse(separated_stiffness_matrix_sparse, r_a_vector,
+    /// u_b_vector, max_iter)` (methods_for_global_analysis.rs:189-233) on the GPU: (u_a, iterations).  The
+    /// separation must be this model's latest.
+    pub fn find_ua_vector_iterative_pcg_jacobi_sparse(
+        &self,
+        separated_stiffness_matrix_sparse: &SeparatedStiffnessMatrixSparse,
+        r_a_vector: &Vec<f64>,
+        u_b_vector: &Vec<f64>,
+        max_iter: usize,
+    ) -> Result<(Vec<f64>, usize), String> {
+        self.pcg(separated_stiffness_matrix_sparse, r_a_vector, u_b_vector, max_iter, false)
+    }
+
+    /// `find_ua_vector_iterative_pcg_block_jacobi_sparse(...)` (methods_for_global_analysis.rs:235-275): the
+    /// node blocks of K_aa as preconditioner.
+    pub fn find_ua_vector_iterative_pcg_block_jacobi_sparse(
+        &self,
+        separated_stiffness_matrix_sparse: &SeparatedStiffnessMatrixSparse,
+        r_a_vector: &Vec<f64>,
+        u_b_vector: &Vec<f64>,
+        max_iter: usize,
+    ) -> Result<(Vec<f64>, usize), String> {
+        self.pcg(separated_stiffness_matrix_sparse, r_a_vector, u_b_vector, max_iter, true)
+    }
+
+    /// `find_r_r_vector_sparse(sep, u_a_vector, u_b_vector)` (methods_for_global_analysis.rs:306-330): the
+    /// reactions K_ba u_a + K_bb u_b - r_b at the restrained DOFs.
+    pub fn find_r_r_vector_sparse(
+        &self,
+        sep: &SeparatedStiffnessMatrixSparse,
+        u_a_vector: &Vec<f64>,
+        u_b_vector: &Vec<f64>,
+    ) -> Result<Vec<f64>, String> {
+        if u_a_vector.len() != sep.n_aa || u_b_vector.len() != sep.n_bb {
+            return Err("u_a / u_b vector sizes do not match the separation".to_string());
+        }
+        let f = self.forces_vector()?;
+        let r_b: Vec<f64> = sep.k_bb_indexes.iter().map(|&i| f[i]).collect();
+        let mut r_r = vec![0.0f64; sep.n_bb];
+        let st = unsafe {
+            ffi::fem_gpu_reactions(self.h, u_a_vector.as_ptr(), u_b_vector.as_ptr(), r_b.as_ptr(), r_r.as_mut_ptr())
+        };
+        self.check(st).map(|_| r_r)
+    }
+
+    /// `compose_global_analysis_result(k_aa_indexes, k_bb_indexes, u_a_vector, r_r_vector)`
+    /// (methods_for_global_analysis.rs:335-359): the free DOFs' displacements into the displacements
+    /// vector, the reactions into the forces vector at the restrained DOFs.
+    pub fn compose_global_analysis_result(
+        &mut self,
+        k_aa_indexes: &[usize],
+        k_bb_indexes: &[usize],
+        u_a_vector: &Vec<f64>,
+        r_r_vector: &Vec<f64>,
+    ) -> Result<(), String> {
+        if u_a_vector.len() != k_aa_indexes.len() || r_r_vector.len() != k_bb_indexes.len() {
+            return Err("u_a / r_r vector sizes do not match the index lists".to_string());
+        }
+        let mut forces = self.forces_vector()?;
+        for (k, &i) in k_aa_indexes.iter().enumerate() {
+            self.displacements[i] = u_a_vector[k];
+        }
+        for (k, &i) in k_bb_indexes.iter().enumerate() {
+            forces[i] = r_r_vector[k];
+        }
+        self.result_forces = Some(forces);
+        Ok(())
+    }
+
+    /// `extract_global_analysis_result()` (methods_for_global_analysis.rs:361-387): (node number, DOF,
+    /// displacement, load) for every DOF of every node, in node index (insertion) order.
+    pub fn extract_global_analysis_result(&self) -> Result<Vec<(u32, DOFParameter, f64, f64)>, String> {
+        let forces = match &self.result_forces {
+            Some(f) => f.clone(),
+            None => self.forces_vector()?,
+        };
+        let mut count = 0i64;
+        self.check(unsafe { ffi::fem_gpu_get_node_count(self.h, &mut count) })?;
+        let mut numbers = vec![0u32; count as usize];
+        self.check(unsafe { ffi::fem_gpu_get_index_node_numbers(self.h, numbers.as_mut_ptr()) })?;
+        let mut out = Vec::with_capacity(6 * numbers.len());
+        for (i, &number) in numbers.iter().enumerate() {
+            for p in 0..6usize {
+                out.push((number, DOFParameter::from_usize(p), self.displacements[6 * i + p], forces[6 * i + p]));
+            }
+        }
+        Ok(out)
+    }
+
+    /// `extract_elements_analysis_result()` (methods_for_element_analysis.rs:27-58) on the GPU, from the
+    /// displacements vector: (element number, [(component, value), ...]) for the trusses, then the beams,
+    /// then the plates, each in call order.
+    pub fn extract_elements_analysis_result(&self) -> Result<Vec<(u32, Vec<(ElementForceComponent, f64)>)>, String> {
+        use ElementForceComponent::*;
+        let (mut t, mut b, mut p) = (0i64, 0i64, 0i64);
+        self.check(unsafe { ffi::fem_gpu_get_element_counts(self.h, &mut t, &mut b, &mut p) })?;
+        let (t, b, p) = (t as usize, b as usize, p as usize);
+        let (mut truss, mut beam, mut plate) = (vec![0.0f64; t], vec![0.0f64; 10 * b], vec![0.0f64; 8 * p]);
+        let st = unsafe {
+            ffi::fem_gpu_element_results(
+                self.h,
+                self.displacements.as_ptr(),
+                self.displacements.len(),
+                truss.as_mut_ptr(),
+                beam.as_mut_ptr(),
+                plate.as_mut_ptr(),
+            )
+        };
+        self.check(st)?;
+        let kinds: [(usize, &[ElementForceComponent], &Vec<f64>); 3] = [
+            (t, &[ForceR], &truss),
+            (b, &[ForceR, ForceS, ForceT, MomentR, MomentS, MomentS, MomentS, MomentT, MomentT, MomentT], &beam),
+            (
+                p,
+                &[MembraneForceR, MembraneForceS, MembraneForceRS, BendingMomentR, BendingMomentS, BendingMomentRS,
+                  ShearForceRT, ShearForceST],
+                &plate,
+            ),
+        ];
+        let mut out = Vec::with_capacity(t + b + p);
+        for (kind, (n, names, values)) in kinds.iter().enumerate() {
+            let mut numbers = vec![0u32; *n];
+            self.check(unsafe { ffi::fem_gpu_get_element_numbers(self.h, kind as c_int, numbers.as_mut_ptr()) })?;
+            let w = names.len();
+            for (e, &number) in numbers.iter().enumerate() {
+                out.push((number, names.iter().copied().zip(values[w * e..w * (e + 1)].iter().copied()).collect()));
+            }
+        }
+        Ok(out)
+    }
 }
 
 impl Drop for FEM {
@@ -429,4 +756,97 @@ pub struct BeamSection {
     pub it: f64,
     pub shear_factor: f64,
     pub local_axis_1_direction: [f64; 3],
+}
+
+/// `DOFParameter` (methods_for_bc_data_handle.rs:7-29): a node's six degrees of freedom in DOF order.
+#[derive(Debug, Clone, Copy, PartialEq, Eq, Hash)]
+#[repr(u8)]
+pub enum DOFParameter {
+    X = 0,
+    Y = 1,
+    Z = 2,
+    ThX = 3,
+    ThY = 4,
+    ThZ = 5,
+}
+
+impl DOFParameter {
+    pub fn from_usize(number: usize) -> Self {
+        match number {
+            0 => DOFParameter::X,
+            1 => DOFParameter::Y,
+            2 => DOFParameter::Z,
+            3 => DOFParameter::ThX,
+            4 => DOFParameter::ThY,
+            5 => DOFParameter::ThZ,
+            _ => panic!("Incorrect dof parameter number!"),
+        }
+    }
+}
+
+/// `ElementForceComponent` (methods_for_element_analysis.rs:6-21).
+#[derive(Debug, Clone, Copy, PartialEq, Eq, Hash)]
+pub enum ElementForceComponent {
+    ForceR,
+    ForceS,
+    ForceT,
+    MembraneForceR,
+    MembraneForceS,
+    MembraneForceRS,
+    ShearForceRT,
+    ShearForceST,
+    MomentR,
+    MomentS,
+    MomentT,
+    BendingMomentR,
+    BendingMomentS,
+    BendingMomentRS,
+}
+
+/// `SeparatedStiffnessMatrixSparse` (structs/separated_stiffness_matrix_sparse.rs): the free (a) and
+/// restrained (b) DOF lists and the four blocks as (local row, local column, value) triplets.
+#[derive(Debug, Clone, PartialEq)]
+pub struct SeparatedStiffnessMatrixSparse {
+    k_aa_indexes: Vec<usize>,
+    k_bb_indexes: Vec<usize>,
+    k_aa_triplets: Vec<(usize, usize, f64)>,
+    k_ab_triplets: Vec<(usize, usize, f64)>,
+    k_ba_triplets: Vec<(usize, usize, f64)>,
+    k_bb_triplets: Vec<(usize, usize, f64)>,
+    n_aa: usize,
+    n_bb: usize,
+}
+
+impl SeparatedStiffnessMatrixSparse {
+    pub fn get_k_aa_indexes(&self) -> &Vec<usize> {
+        &self.k_aa_indexes
+    }
+
+    pub fn get_k_bb_indexes(&self) -> &Vec<usize> {
+        &self.k_bb_indexes
+    }
+
+    pub fn get_k_aa_triplets(&self) -> &Vec<(usize, usize, f64)> {
+        &self.k_aa_triplets
+    }
+
+    pub fn get_k_ab_triplets(&self) -> &Vec<(usize, usize, f64)> {
+        &self.k_ab_triplets
+    }
+
+    pub fn get_k_ba_triplets(&self) -> &Vec<(usize, usize, f64)> {
+        &self.k_ba_triplets
+    }
+
+    pub fn get_k_bb_triplets(&self) -> &Vec<(usize, usize, f64)> {
+        &self.k_bb_triplets
+    }
+
+    pub fn get_n_aa(&self) -> usize {
+        self.n_aa
+    }
+
+    pub fn get_n_bb(&self) -> usize {
+        self.n_bb
+    }
 }

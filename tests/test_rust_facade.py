@@ -57,6 +57,41 @@ REFERENCE_METHODS = {
     "get_truss_rotation_matrix_elements": ["number"],
     "get_beam_rotation_matrix_elements": ["number"],
     "get_plate_rotation_matrix_elements": ["number"],
+    # src/fem/methods_for_bc_data_handle.rs:34-39, 58-63, 103-108, 176-181
+    "add_concentrated_load": ["node_number", "dof_parameter", "value"],
+    "add_uniformly_distributed_line_load": ["beam_element_number", "dof_parameter", "value"],
+    "add_uniformly_distributed_surface_load": ["plate_element_number", "dof_parameter", "value"],
+    "add_displacement": ["node_number", "dof_parameter", "value"],
+    # src/fem/methods_for_separate_stiffness_matrix.rs:217-219, 322, 333
+    "separate_stiffness_matrix_sparse_iterative": [],
+    "compose_r_a_vector": ["k_aa_indexes"],
+    "compose_u_b_vector": ["k_bb_indexes"],
+    # src/fem/methods_for_global_analysis.rs:189-195, 235-241, 306-311, 335-341, 361
+    "find_ua_vector_iterative_pcg_jacobi_sparse": ["separated_stiffness_matrix_sparse", "r_a_vector", "u_b_vector",
+                                                   "max_iter"],
+    "find_ua_vector_iterative_pcg_block_jacobi_sparse": ["separated_stiffness_matrix_sparse", "r_a_vector",
+                                                         "u_b_vector", "max_iter"],
+    "find_r_r_vector_sparse": ["sep", "u_a_vector", "u_b_vector"],
+    "compose_global_analysis_result": ["k_aa_indexes", "k_bb_indexes", "u_a_vector", "r_r_vector"],
+    "extract_global_analysis_result": [],
+    # src/fem/methods_for_element_analysis.rs:27-29
+    "extract_elements_analysis_result": [],
+}
+
+# return types other than Result<(), String> (the crate's Vector<V> is a Vec<f64> here)
+REFERENCE_RETURNS = {
+    "create": "Self",
+    "get_truss_rotation_matrix_elements": "Result<[f64; 9], String>",
+    "get_beam_rotation_matrix_elements": "Result<[f64; 9], String>",
+    "get_plate_rotation_matrix_elements": "Result<[f64; 9], String>",
+    "separate_stiffness_matrix_sparse_iterative": "Result<SeparatedStiffnessMatrixSparse, String>",
+    "compose_r_a_vector": "Result<Vec<f64>, String>",
+    "compose_u_b_vector": "Result<Vec<f64>, String>",
+    "find_ua_vector_iterative_pcg_jacobi_sparse": "Result<(Vec<f64>, usize), String>",
+    "find_ua_vector_iterative_pcg_block_jacobi_sparse": "Result<(Vec<f64>, usize), String>",
+    "find_r_r_vector_sparse": "Result<Vec<f64>, String>",
+    "extract_global_analysis_result": "Result<Vec<(u32, DOFParameter, f64, f64)>, String>",
+    "extract_elements_analysis_result": "Result<Vec<(u32, Vec<(ElementForceComponent, f64)>)>, String>",
 }
 
 
@@ -68,13 +103,21 @@ def test_facade_keeps_reference_signatures():
         args = [a.strip() for a in m.group(1).split(",") if a.strip()]
         args = [a for a in args if not a.startswith("&")]
         assert [a.split(":")[0].strip() for a in args] == params, name
-        ret = m.group(2).strip()
-        if name == "create":
-            assert ret == "Self"
-        elif name.startswith("get_"):
-            assert ret == "Result<[f64; 9], String>", name
-        else:
-            assert ret == "Result<(), String>", name
+        ret = " ".join(m.group(2).split())
+        assert ret == REFERENCE_RETURNS.get(name, "Result<(), String>"), name
+
+
+def test_facade_keeps_reference_enums():
+    """DOFParameter and ElementForceComponent with the crate's variants (DOFParameter in DOF order)"""
+    lib = _read("src", "lib.rs")
+    for enum, variants in (("DOFParameter", ["X = 0", "Y = 1", "Z = 2", "ThX = 3", "ThY = 4", "ThZ = 5"]),
+                           ("ElementForceComponent", ["ForceR", "ForceS", "ForceT", "MembraneForceR",
+                                                      "MembraneForceS", "MembraneForceRS", "ShearForceRT",
+                                                      "ShearForceST", "MomentR", "MomentS", "MomentT",
+                                                      "BendingMomentR", "BendingMomentS", "BendingMomentRS"])):
+        m = re.search(r"pub enum " + enum + r"\s*\{(.*?)\}", lib, flags=re.S)
+        assert m, enum
+        assert [v.strip() for v in m.group(1).split(",") if v.strip()] == variants, enum
 
 
 def test_crate_links_the_library():
