@@ -9,6 +9,7 @@
 //! | here | reference |
 //! |---|---|
 //! | [`FEM::create`] | `FEM::create` (src/fem/fem.rs:34) |
+//! | [`FEM::reset`] | `reset` (src/fem/fem.rs:154-168) |
 //! | [`FEM::add_node`] | `add_node` (src/fem/methods_for_node_data_handle.rs:66) |
 //! | [`FEM::add_truss`] | `add_truss` (src/fem/methods_for_truss_data_handle.rs:49) |
 //! | [`FEM::add_beam`] | `add_beam` (src/fem/methods_for_beam_data_handle.rs:49) |
@@ -70,6 +71,10 @@ pub struct Vjp {
 pub struct FEM {
     h: *mut ffi::FemGpu,
     nodes_number: u32,
+    rel_tol: f64,
+    abs_tol: f64,
+    /// the nodes_number of create: the crate's props keep it through a reset
+    node_limit: u32,
     /// the reference's imposed_constraints: one flag per DOF (6 * nodes_number)
     imposed: Vec<u8>,
     /// the reference's displacements_vector: imposed values, then the solution once composed
@@ -95,6 +100,9 @@ impl FEM {
         FEM {
             h,
             nodes_number,
+            rel_tol,
+            abs_tol,
+            node_limit: nodes_number,
             imposed: vec![0; ndof],
             displacements: vec![0.0; ndof],
             result_forces: None,
@@ -114,6 +122,27 @@ impl FEM {
         self.nodes_number
     }
 
+    /// `reset(nodes_number)` (fem.rs:154-168): drops every node, element, load and imposed displacement and
+    /// sizes the stiffness, forces and displacements for `nodes_number` nodes (a new handle).  As in the
+    /// crate, the tolerances and the node limit stay those of create: `add_node` refuses the node past the
+    /// nodes_number given at creation even after a reset to more.  After a reset to fewer nodes the node
+    /// past the new count is refused; the crate would accept it with its DOFs outside the matrix.
+    pub fn reset(&mut self, nodes_number: u32) {
+        let mut h = ptr::null_mut();
+        let st = unsafe { ffi::fem_gpu_create(self.rel_tol, self.abs_tol, nodes_number, &mut h) };
+        assert!(st == 0 && !h.is_null(), "fem_gpu_create failed with status {st}");
+        unsafe {
+            ffi::fem_gpu_destroy(self.h);
+        }
+        let ndof = 6 * nodes_number as usize;
+        self.h = h;
+        self.nodes_number = nodes_number;
+        self.imposed = vec![0; ndof];
+        self.displacements = vec![0.0; ndof];
+        self.result_forces = None;
+        self.node_index.clear();
+    }
+
     /// `add_node(number, x, y, z)`: node index = insertion order, DOFs 6 * index + {X..ThZ}.
     pub fn add_node(&mut self, number: u32, x: f64, y: f64, z: f64) -> Result<(), String> {
         self.add_nodes(&[number], &[[x, y, z]]).map(|_| ())
@@ -122,11 +151,22 @@ impl FEM {
     /// Bulk `add_node` in call order; stops at the first failure (earlier nodes stay added).
     pub fn add_nodes(&mut self, numbers: &[u32], xyz: &[[f64; 3]]) -> Result<usize, String> {
         assert_eq!(numbers.len(), xyz.len());
+        let mut m = numbers.len();
+        if self.node_limit < self.nodes_number {
+            // reset to more nodes than at creation: the limit of create holds
+            let mut count = 0i64;
+            self.check(unsafe { ffi::fem_gpu_get_node_count(self.h, &mut count) })?;
+            m = m.min((self.node_limit as i64 - count).max(0) as usize);
+        }
         let mut n = 0usize;
-        let st = unsafe {
-            ffi::fem_gpu_add_nodes(self.h, numbers.as_ptr(), xyz.as_ptr() as *const f64, numbers.len(), &mut n)
-        };
-        self.check(st).map(|_| n)
+        if m > 0 {
+            let st = unsafe { ffi::fem_gpu_add_nodes(self.h, numbers.as_ptr(), xyz.as_ptr() as *const f64, m, &mut n) };
+            self.check(st)?;
+        }
+        if m < numbers.len() {
+            return Err(format!("Nodes number could not be greater than {}!", self.node_limit));
+        }
+        Ok(n)
     }
 
     /// `add_truss(number, node_1_number, node_2_number, young_modulus, area, optional_area_2)`.
