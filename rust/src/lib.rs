@@ -328,6 +328,40 @@ impl FEM {
         self.check(st)
     }
 
+    /// [`FEM::assemble`] with the stiffness read back into `csr`: on a new topology the pattern travels back
+    /// while the symbolic phase finishes and the values are computed, then the values follow.  `csr`'s
+    /// vectors are resized to fit (a call whose buffers turn out too small is repeated once with room, the
+    /// pattern being kept).  Returns nnz.
+    pub fn assemble_to_host(&mut self, csr: &mut Csr) -> Result<usize, String> {
+        csr.row_ptr.resize(6 * self.nodes_number as usize + 1, 0);
+        for _ in 0..2 {
+            let cap = csr.col_idx.len().min(csr.values.len());
+            let mut nnz = 0i64;
+            let st = unsafe {
+                ffi::fem_gpu_assemble_to_host(
+                    self.h,
+                    csr.row_ptr.as_mut_ptr(),
+                    csr.col_idx.as_mut_ptr(),
+                    csr.values.as_mut_ptr(),
+                    cap as i64,
+                    &mut nnz,
+                )
+            };
+            let nnz = nnz as usize;
+            if st == 0 {
+                csr.col_idx.truncate(nnz);
+                csr.values.truncate(nnz);
+                return Ok(nnz);
+            }
+            if nnz <= cap {
+                return Err(self.check(st).unwrap_err());
+            }
+            csr.col_idx.resize(nnz, 0);
+            csr.values.resize(nnz, 0.0);
+        }
+        Err("the stiffness did not fit the buffers twice".to_string())
+    }
+
     /// The assembled stiffness, read back to host memory.
     pub fn stiffness_csr(&self) -> Result<Csr, String> {
         let (mut rows, mut nnz) = (0i64, 0i64);
