@@ -617,7 +617,7 @@ class Batch:
         """One batch standing for `FEM(rel_tol, abs_tol, n)` + add_nodes + add_trusses + add_beams +
         add_plates + assemble per mesh (fem_gpu_batch_create_from_arrays): the checks of every mesh run in
         bulk on the GPU, one symbolic phase covers all meshes and one graph launch assembles them.
-        `nodes_number` (per mesh) defaults to each mesh's node count.  A failing mesh raises its first
+        `nodes_number` (per mesh, or one value for all) defaults to each mesh's node count.  A failing mesh raises its first
         failing call's error, the message prefixed by "structure i: "."""
         return cls.from_structures(cls.structures(meshes, nodes_number), rel_tol, abs_tol, library)
 
@@ -663,7 +663,12 @@ class Batch:
                     k for k in ("trusses", "beams", "plates") if getattr(m, k) is not None):
                 raise ValueError("a batch adds each mesh's trusses, then beams, then plates")
         nn = [m.nodes_number for m in meshes]
-        cap = arr(nn if nodes_number is None else nodes_number, np.uint32)
+        room = np.asarray(nn if nodes_number is None else nodes_number)
+        if room.ndim == 0:
+            room = np.full(S, room)
+        if room.shape != (S,):
+            raise ValueError(f"nodes_number: one value or one per mesh ({S}), got shape {room.shape}")
+        cap = arr(room, np.uint32)
         st = _lib.Structures()
         st.n_structures = S
         st.nodes_number = ptr(cap, c_uint32)
