@@ -42,6 +42,12 @@ class FEMError(RuntimeError):
         self.code = code
 
 
+def _require(ok, what):
+    """argument check that stays on under python -O: the C side trusts the sizes it is given"""
+    if not ok:
+        raise ValueError(what)
+
+
 def _f64(v, m):
     return np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), (m,)))
 
@@ -214,9 +220,11 @@ class FEM:
         rp = np.asarray(row_ptr)
         ci = np.asarray(col_idx)
         va = np.asarray(values)
-        assert rp.dtype == np.int64 and ci.dtype == np.int32 and va.dtype == np.float64
-        assert rp.flags.c_contiguous and ci.flags.c_contiguous and va.flags.c_contiguous
-        assert rp.size >= 6 * self.nodes_number + 1
+        _require(rp.dtype == np.int64 and ci.dtype == np.int32 and va.dtype == np.float64,
+                 "row_ptr, col_idx, values must be int64, int32, float64")
+        _require(rp.flags.c_contiguous and ci.flags.c_contiguous and va.flags.c_contiguous,
+                 "row_ptr, col_idx, values must be C-contiguous")
+        _require(rp.size >= 6 * self.nodes_number + 1, f"row_ptr needs {6 * self.nodes_number + 1} entries")
         cap = min(ci.size, va.size)
         nnz = c_int64(0)
         self._check(self._L.fem_gpu_assemble_to_host(self._h, ptr(rp, c_int64), ptr(ci, c_int32), ptr(va, c_double),
@@ -303,7 +311,8 @@ class FEM:
         lam = np.ascontiguousarray(lam, dtype=np.float64)
         if u.ndim == 1:
             u, lam = u[None], lam[None]
-        assert u.shape == lam.shape and u.shape[1] == 6 * self.nodes_number
+        _require(u.ndim == 2 and u.shape == lam.shape and u.shape[1] == 6 * self.nodes_number,
+                 f"u and lam must both be (npairs, {6 * self.nodes_number})")
         nt, nb, npl = self.element_counts()
         out = dict(truss=np.zeros((nt, 3)), beam=np.zeros((nb, 5)), plate=np.zeros((npl, 2)),
                    xyz=np.zeros((self.node_count(), 3)))
@@ -438,7 +447,7 @@ class FEM:
         GPU: the imposed displacements (from add_displacement, or `imposed`, 6 * nodes_number flags) split the
         assembled stiffness into K_aa, K_ab, K_ba, K_bb, each a CSR matrix sorted by (row, column)."""
         imp = self._imposed() if imposed is None else np.ascontiguousarray(imposed, dtype=np.uint8)
-        assert imp.shape == (6 * self.nodes_number,)
+        _require(imp.shape == (6 * self.nodes_number,), f"imposed must hold {6 * self.nodes_number} flags")
         self._check(self._L.fem_gpu_separate_sparse(self._h, ptr(imp, c_uint8)))
         n_aa, n_bb, nnz = c_int64(0), c_int64(0), (c_int64 * 4)()
         self._check(self._L.fem_gpu_get_separation_sizes(self._h, ctypes.byref(n_aa), ctypes.byref(n_bb), nnz))
@@ -459,7 +468,8 @@ class FEM:
     def _pcg(self, sep, r_a_vector, u_b_vector, max_iter, block):
         r_a = np.ascontiguousarray(r_a_vector, dtype=np.float64)
         u_b = None if u_b_vector is None else np.ascontiguousarray(u_b_vector, dtype=np.float64)
-        assert r_a.shape == (sep.n_aa,) and (u_b is None or u_b.shape == (sep.n_bb,))
+        _require(r_a.shape == (sep.n_aa,) and (u_b is None or u_b.shape == (sep.n_bb,)),
+                 f"r_a must hold {sep.n_aa} values and u_b {sep.n_bb}")
         u_a = np.zeros(sep.n_aa)
         it = c_int(0)
         self._check(self._L.fem_gpu_solve_pcg(self._h, ptr(r_a, c_double), None if u_b is None else ptr(u_b, c_double),
@@ -479,6 +489,8 @@ class FEM:
         """find_r_r_vector_sparse (methods_for_global_analysis.rs:293-330): reactions K_ba u_a + K_bb u_b - r_b"""
         u_a = np.ascontiguousarray(u_a_vector, dtype=np.float64)
         u_b = np.ascontiguousarray(u_b_vector, dtype=np.float64)
+        _require(u_a.shape == (sep.n_aa,) and u_b.shape == (sep.n_bb,),
+                 f"u_a must hold {sep.n_aa} values and u_b {sep.n_bb}")
         r_b = np.ascontiguousarray(self.forces_vector()[np.asarray(sep.k_bb_indexes, np.int64)])
         r_r = np.zeros(sep.n_bb)
         self._check(self._L.fem_gpu_reactions(self._h, ptr(u_a, c_double), ptr(u_b, c_double), ptr(r_b, c_double),

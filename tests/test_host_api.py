@@ -137,3 +137,29 @@ def test_extract_elements_analysis_result_rows():
             want.append((int(number), [(c, float(v)) for c, v in zip(names, row)]))
     assert got == want
     assert type(got[0][0]) is int and type(got[0][1][0][1]) is float
+
+
+def test_size_checks_raise_before_the_c_call():
+    """the sizes the C side trusts are checked on the host, as ValueError (not assert: they stay on under
+    python -O), before anything is handed to the library"""
+    from finite_element_method_gb300.fem import SeparatedStiffnessSparse
+
+    g = FEM(1e-12, 1e-12, 3)
+    ndof = 18
+    with pytest.raises(ValueError, match="row_ptr needs 19"):
+        g.assemble_to_host(np.zeros(ndof, np.int64), np.zeros(4, np.int32), np.zeros(4))
+    with pytest.raises(ValueError, match="int64, int32, float64"):
+        g.assemble_to_host(np.zeros(ndof + 1, np.int32), np.zeros(4, np.int32), np.zeros(4))
+    with pytest.raises(ValueError, match=r"\(npairs, 18\)"):
+        g.vjp(np.zeros((2, ndof)), np.zeros((2, ndof - 1)))
+    with pytest.raises(ValueError, match="18 flags"):
+        g.separate_stiffness_matrix_sparse_iterative(imposed=np.zeros(ndof - 6, np.uint8))
+    sep = SeparatedStiffnessSparse(np.arange(12), np.arange(12, 18), {})
+    with pytest.raises(ValueError, match="r_a must hold 12 values and u_b 6"):
+        g.find_ua_vector_iterative_pcg_jacobi_sparse(sep, np.zeros(11), np.zeros(6), 10)
+    with pytest.raises(ValueError, match="r_a must hold 12 values and u_b 6"):
+        g.find_ua_vector_iterative_pcg_block_jacobi_sparse(sep, np.zeros(12), np.zeros(5), 10)
+    g.forces_vector = lambda: np.zeros(ndof)
+    with pytest.raises(ValueError, match="u_a must hold 12 values and u_b 6"):
+        g.find_r_r_vector_sparse(sep, np.zeros(12), np.zeros(7))
+    g.close()
