@@ -833,7 +833,7 @@ pub struct BeamSection {
 }
 
 /// `DOFParameter` (methods_for_bc_data_handle.rs:7-29): a node's six degrees of freedom in DOF order.
-#[derive(Debug, Clone, Copy, PartialEq, Eq, Hash)]
+#[derive(Debug, Clone, Copy, PartialEq, Eq, PartialOrd, Ord, Hash)]
 #[repr(u8)]
 pub enum DOFParameter {
     X = 0,
@@ -859,7 +859,7 @@ impl DOFParameter {
 }
 
 /// `ElementForceComponent` (methods_for_element_analysis.rs:6-21).
-#[derive(Debug, Clone, Copy, PartialEq, Eq, Hash)]
+#[derive(Debug, Clone, Copy, PartialEq, Eq, PartialOrd, Ord, Hash)]
 pub enum ElementForceComponent {
     ForceR,
     ForceS,

@@ -128,3 +128,20 @@ def test_crate_links_the_library():
     assert 'links = "fem_gpu"' in cargo and 'build = "build.rs"' in cargo
     build = _read("build.rs")
     assert "rustc-link-lib=dylib=fem_gpu" in build
+
+
+def test_integration_tests_call_only_facade_methods():
+    """rust/tests/*.rs (the crate's own integration tests through the facade) call methods that lib.rs
+    defines, with the reference's enums"""
+    lib = _read("src", "lib.rs")
+    defined = set(re.findall(r"pub fn (\w+)", lib))
+    tests_dir = os.path.join(RUST, "tests")
+    files = sorted(f for f in os.listdir(tests_dir) if f.endswith(".rs"))
+    assert files
+    for f in files:
+        src = _read("tests", f)
+        called = set(re.findall(r"\b(?:model|sep)\.(\w+)\(", src)) | set(re.findall(r"FEM::(\w+)\(", src))
+        assert called and called <= defined, (f, called - defined)
+        for enum in set(re.findall(r"\b(DOFParameter|ElementForceComponent)::(\w+)", src)):
+            assert re.search(r"pub enum " + enum[0] + r"\s*\{[^}]*\b" + enum[1] + r"\b", lib) or \
+                enum[1] in defined, enum
