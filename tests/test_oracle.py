@@ -240,3 +240,22 @@ def test_golden_element_matrices(oracle):
         assert err < 1e-13, (c["name"], err)
         # entries that are exactly zero in the reference formulas are exactly zero in the oracle
         np.testing.assert_array_equal(got[ref == 0.0], 0.0, err_msg=c["name"])
+
+
+@pytest.mark.parametrize("threads", [1, 3, 4])
+def test_parallel_port_matches_the_eager_oracle(oracle, threads):
+    """The reference arm's multi-threaded port (orc_assemble_parallel: CSR rows partitioned over threads,
+    each row's entries summed in element call order) gives the eager oracle's CSR bit for bit: beams and
+    plates sharing nodes, a truss lattice, a plate mesh."""
+    from finite_element_method_gb300 import meshes
+
+    for m in (meshes.adjoint_model(frame=(4, 4, 3), slab=(30, 30), seed=7), meshes.truss_lattice(5, seed=3),
+              meshes.plate_mesh(20, 15, size=3.0, seed=11)):
+        o = oracle.OracleFEM(meshes.REL_TOL, meshes.ABS_TOL, m.nodes_number)
+        meshes.load(o, m)
+        rp, ci, va = o.csr()
+        _, nnz, (prp, pci, pva) = oracle.assemble_parallel(m, threads, meshes.REL_TOL, meshes.ABS_TOL)
+        assert nnz == len(ci) > 0, m.name
+        np.testing.assert_array_equal(prp, rp, err_msg=m.name)
+        np.testing.assert_array_equal(pci, ci, err_msg=m.name)
+        np.testing.assert_array_equal(pva.view(np.uint64), va.view(np.uint64), err_msg=m.name)
