@@ -259,3 +259,25 @@ def test_parallel_port_matches_the_eager_oracle(oracle, threads):
         np.testing.assert_array_equal(prp, rp, err_msg=m.name)
         np.testing.assert_array_equal(pci, ci, err_msg=m.name)
         np.testing.assert_array_equal(pva.view(np.uint64), va.view(np.uint64), err_msg=m.name)
+
+
+@pytest.mark.parametrize("name", ["truss_tapered", "beam_i12", "plate_tilted"])
+def test_golden_fixture_is_what_its_script_computes(name):
+    """element_matrices.json holds what tests/golden/make_golden.py computes: the case is evaluated again from
+    its recorded arguments in 50-digit arithmetic and compared with the fixture digit for digit"""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    case = next(c for c in _golden()["cases"] if c["name"] == name)
+    a = case["args"]
+    if case["kind"] == "truss":
+        M = literal.truss_global_matrix(a["x1"], a["x2"], a["young"], a["area"], a.get("area_2"), bk=mg.BK)
+    elif case["kind"] == "beam":
+        M = literal.beam_global_matrix(a["x1"], a["x2"], a["young"], a["poisson"], a["area"], a["i11"], a["i22"],
+                                       a["i12"], a["it"], a["shear_factor"], a["axis"], bk=mg.BK)
+    else:
+        M = literal.plate_global_matrix(a["x1"], a["x2"], a["x3"], a["x4"], a["young"], a["poisson"],
+                                        a["thickness"], a["shear_factor"], bk=mg.BK)
+    assert mg.mstr(M) == case["matrix"]
