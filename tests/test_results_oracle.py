@@ -196,3 +196,30 @@ def test_mesh_results_match_element_calls():
                 got = fo.plate_results(*(X[i] for i in nd), pl["young"][e], pl["poisson"][e], pl["thickness"][e],
                                        pl["shear_factor"][e], np.concatenate([disp[6 * i:6 * i + 6] for i in nd]))
                 assert np.array_equal(got, out1["plate"][e])
+
+
+@pytest.mark.parametrize("name", ["truss_tapered_1", "beam_i12_0", "plate_tilted_1"])
+def test_golden_fixture_is_what_its_script_computes(name):
+    """element_results.json holds what tests/golden/make_results_golden.py computes: the case is evaluated
+    again from its recorded arguments and displacements in 50-digit arithmetic, values and scales digit for
+    digit"""
+    import importlib.util
+
+    from oracle import literal
+
+    spec = importlib.util.spec_from_file_location(
+        "make_results_golden", os.path.join(os.path.dirname(GOLDEN), "make_results_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    with open(GOLDEN) as f:
+        case = next(c for c in json.load(f)["cases"] if c["name"] == name)
+    a, u = case["args"], case["u"]
+    if case["kind"] == "truss":
+        v, s = literal.truss_results(a["x1"], a["x2"], a["young"], a["area"], a.get("area_2"), u, bk=mg.BK)
+    elif case["kind"] == "beam":
+        v, s = literal.beam_results(a["x1"], a["x2"], a["young"], a["poisson"], a["area"], a["i11"], a["i22"],
+                                    a["i12"], a["it"], a["shear_factor"], a["axis"], u, bk=mg.BK)
+    else:
+        v, s = literal.plate_results(a["x1"], a["x2"], a["x3"], a["x4"], a["young"], a["poisson"], a["thickness"],
+                                     a["shear_factor"], u, bk=mg.BK)
+    assert mg.strs(v) == case["values"] and mg.strs(s) == case["scale"]
