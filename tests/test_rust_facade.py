@@ -145,3 +145,22 @@ def test_integration_tests_call_only_facade_methods():
         for enum in set(re.findall(r"\b(DOFParameter|ElementForceComponent)::(\w+)", src)):
             assert re.search(r"pub enum " + enum[0] + r"\s*\{[^}]*\b" + enum[1] + r"\b", lib) or \
                 enum[1] in defined, enum
+
+
+def test_integration_notes_declare_entry_points_as_the_header():
+    """the Rust declarations shown in INTEGRATION.md (the binding a maintainer would add to the reference
+    crate) name real entry points with the header's parameter and return types, in order"""
+    def decls(text):
+        out = {}
+        for m in re.finditer(r"fn (fem_gpu_\w+)\((.*?)\)\s*->\s*([^;]+);", text, flags=re.S):
+            types = [p.split(":", 1)[1].strip() for p in m.group(2).split(",") if p.strip()]
+            out[m.group(1)] = (types, " ".join(m.group(3).split()))
+        return out
+
+    with open(os.path.join(ROOT, "INTEGRATION.md")) as f:
+        shown = decls(f.read())
+    ffi = decls(_read("src", "ffi.rs"))
+    assert len(shown) >= 20
+    for name, sig in shown.items():
+        assert name in ffi, name
+        assert sig == ffi[name], (name, sig, ffi[name])
