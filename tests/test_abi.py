@@ -71,3 +71,41 @@ def test_structures_layout_matches_header():
     assert [f for _, f in fields] == [f for f, _ in _lib.Structures._fields_]
     sizes = {"size_t": ctypes.sizeof(ctypes.c_size_t)}
     assert ctypes.sizeof(_lib.Structures) == sum(sizes.get(t, ctypes.sizeof(ctypes.c_void_p)) for t, _ in fields)
+
+
+def test_python_binding_types_match_header():
+    """every ctypes signature has the header's argument and return types: scalars exactly (a size_t bound
+    as a 32-bit int would truncate), pointers as c_void_p or a pointer to the header's element type"""
+    import sys
+    from ctypes import (POINTER, c_char_p, c_double, c_float, c_int, c_int32, c_int64, c_size_t, c_uint8, c_uint32,
+                        c_void_p)
+
+    sys.path.insert(0, os.path.join(ROOT, "rust"))
+    import gen_ffi
+
+    scalar = {"double": c_double, "uint32_t": c_uint32, "size_t": c_size_t, "int": c_int, "int64_t": c_int64}
+    elem = {"double": c_double, "float": c_float, "int64_t": c_int64, "int32_t": c_int32, "uint32_t": c_uint32,
+            "uint8_t": c_uint8, "size_t": c_size_t, "int": c_int}
+
+    def matches(decl, ct):
+        t = decl.replace("const", "").replace(" ", "")
+        base = t.rstrip("*")
+        stars = len(t) - len(base)
+        if stars == 0:
+            return ct is scalar[base]
+        if base == "char" and stars == 1:
+            return ct is c_char_p
+        if ct is c_void_p:
+            return True
+        if stars == 1:
+            return base in elem and ct is POINTER(elem[base])
+        return stars == 2 and ct is POINTER(c_void_p)
+
+    protos = gen_ffi.prototypes()
+    assert len(protos) == len(_lib.SIGNATURES)
+    for ret, name, params in protos:
+        res, args = _lib.SIGNATURES[name]
+        assert matches(ret, res), (name, ret, res)
+        assert len(args) == len(params), name
+        for (decl, pname), ct in zip(params, args):
+            assert matches(decl, ct), (name, pname, decl, ct)
