@@ -109,3 +109,13 @@ def test_python_binding_types_match_header():
         assert len(args) == len(params), name
         for (decl, pname), ct in zip(params, args):
             assert matches(decl, ct), (name, pname, decl, ct)
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """without the CUDA library there is no fallback: loading it raises"""
+    import pytest
+
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib._build, "LIB_PATH", str(tmp_path / "libfem_gpu.so"))
+    with pytest.raises(RuntimeError, match="CUDA assembly library not found"):
+        _lib.load(build_if_missing=False)
