@@ -119,3 +119,23 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib._build, "LIB_PATH", str(tmp_path / "libfem_gpu.so"))
     with pytest.raises(RuntimeError, match="CUDA assembly library not found"):
         _lib.load(build_if_missing=False)
+
+
+def test_product_never_imports_the_oracle():
+    """the package's Python modules import nothing from oracle/ (the oracle is the checker, never the path),
+    and its CUDA/C++ sources include nothing from there"""
+    import ast
+
+    pkg = os.path.join(ROOT, "finite_element_method_gb300")
+    for path in glob.glob(os.path.join(pkg, "**", "*.py"), recursive=True):
+        tree = ast.parse(open(path).read(), path)
+        for node in ast.walk(tree):
+            if isinstance(node, ast.Import):
+                names = [a.name for a in node.names]
+            elif isinstance(node, ast.ImportFrom):
+                names = [node.module or ""]
+            else:
+                continue
+            assert not any(n == "oracle" or n.startswith("oracle.") for n in names), (path, names)
+    for path in glob.glob(os.path.join(pkg, "csrc", "*")):
+        assert "oracle" not in "".join(re.findall(r'#include\s*[<"][^>"]*[>"]', open(path).read())), path
