@@ -37,7 +37,8 @@
 //! Beyond the reference: bulk `add_*s` forms (arrays in call order, stopping at
 //! the first failing item like a loop of single calls), [`FEM::vjp`], the
 //! adjoint vector-Jacobian product in the role of a `torch.autograd.Function`
-//! backward, and [`Batch`], many structures assembled together.
+//! backward, and [`Batch`], many structures assembled together (their calls
+//! recorded in a [`Structures`]: one `create` + `add_*` sequence each).
 
 pub mod ffi;
 
@@ -766,6 +767,13 @@ impl Batch {
         Ok(batch)
     }
 
+    /// The batch of the structures whose calls `structures` recorded (see [`Structures`]).  The call is
+    /// synchronous: nothing reads the recorded arrays after it returns.
+    pub fn from_calls(rel_tol: f64, abs_tol: f64, structures: &mut Structures) -> Result<Batch, String> {
+        let layout = structures.layout();
+        Batch::from_structures(rel_tol, abs_tol, &layout)
+    }
+
     fn message(&self) -> String {
         if self.b.is_null() {
             return "batch creation failed".to_string();
@@ -922,5 +930,170 @@ impl SeparatedStiffnessMatrixSparse {
 
     pub fn get_n_bb(&self) -> usize {
         self.n_bb
+    }
+}
+
+/// The calls of many plain sequences, recorded for one [`Batch`]: [`Structures::create`] starts a
+/// structure (the `FEM::create(rel_tol, abs_tol, nodes_number)` of its sequence), then its `add_node`,
+/// `add_truss`, `add_beam` and `add_plate` calls follow with the reference's arguments.  The batch applies
+/// each structure's calls as its sequence would, kind by kind: nodes, trusses, beams, plates, each kind in
+/// call order.
+#[derive(Debug, Clone, Default)]
+pub struct Structures {
+    nodes_number: Vec<u32>,
+    /// per structure: nodes, trusses, beams, plates
+    counts: Vec<[usize; 4]>,
+    node_numbers: Vec<u32>,
+    xyz: Vec<f64>,
+    truss_numbers: Vec<u32>,
+    truss_nodes: Vec<u32>,
+    truss_young: Vec<f64>,
+    truss_area: Vec<f64>,
+    /// NaN: no second area
+    truss_area2: Vec<f64>,
+    beam_numbers: Vec<u32>,
+    beam_nodes: Vec<u32>,
+    /// young, poisson, area, i11, i22, i12, it, shear_factor
+    beam_props: [Vec<f64>; 8],
+    beam_axis: Vec<f64>,
+    plate_numbers: Vec<u32>,
+    plate_nodes: Vec<u32>,
+    /// young, poisson, thickness, shear_factor
+    plate_props: [Vec<f64>; 4],
+    /// per kind, the structures' offsets (made by `layout`)
+    offsets: [Vec<usize>; 4],
+}
+
+impl Structures {
+    pub fn new() -> Self {
+        Self::default()
+    }
+
+    /// Starts the next structure: the `FEM::create(rel_tol, abs_tol, nodes_number)` of its sequence.
+    pub fn create(&mut self, nodes_number: u32) {
+        self.nodes_number.push(nodes_number);
+        self.counts.push([0; 4]);
+    }
+
+    fn count(&mut self, kind: usize) -> &mut usize {
+        let c = self.counts.last_mut().expect("Structures::create starts a structure");
+        &mut c[kind]
+    }
+
+    pub fn add_node(&mut self, number: u32, x: f64, y: f64, z: f64) {
+        *self.count(0) += 1;
+        self.node_numbers.push(number);
+        self.xyz.extend_from_slice(&[x, y, z]);
+    }
+
+    pub fn add_truss(
+        &mut self,
+        number: u32,
+        node_1_number: u32,
+        node_2_number: u32,
+        young_modulus: f64,
+        area: f64,
+        optional_area_2: Option<f64>,
+    ) {
+        *self.count(1) += 1;
+        self.truss_numbers.push(number);
+        self.truss_nodes.extend_from_slice(&[node_1_number, node_2_number]);
+        self.truss_young.push(young_modulus);
+        self.truss_area.push(area);
+        self.truss_area2.push(optional_area_2.unwrap_or(f64::NAN));
+    }
+
+    pub fn add_beam(&mut self, number: u32, node_1_number: u32, node_2_number: u32, section: &BeamSection) {
+        *self.count(2) += 1;
+        self.beam_numbers.push(number);
+        self.beam_nodes.extend_from_slice(&[node_1_number, node_2_number]);
+        let s = section;
+        let values = [s.young_modulus, s.poisson_ratio, s.area, s.i11, s.i22, s.i12, s.it, s.shear_factor];
+        for (column, v) in self.beam_props.iter_mut().zip(values) {
+            column.push(v);
+        }
+        self.beam_axis.extend_from_slice(&s.local_axis_1_direction);
+    }
+
+    #[allow(clippy::too_many_arguments)]
+    pub fn add_plate(
+        &mut self,
+        number: u32,
+        node_1_number: u32,
+        node_2_number: u32,
+        node_3_number: u32,
+        node_4_number: u32,
+        young_modulus: f64,
+        poisson_ratio: f64,
+        thickness: f64,
+        shear_factor: f64,
+    ) {
+        *self.count(3) += 1;
+        self.plate_numbers.push(number);
+        self.plate_nodes.extend_from_slice(&[node_1_number, node_2_number, node_3_number, node_4_number]);
+        for (column, v) in self.plate_props.iter_mut().zip([young_modulus, poisson_ratio, thickness, shear_factor]) {
+            column.push(v);
+        }
+    }
+
+    /// Structures recorded so far.
+    pub fn len(&self) -> usize {
+        self.counts.len()
+    }
+
+    pub fn is_empty(&self) -> bool {
+        self.counts.is_empty()
+    }
+
+    /// The C layout (`fem_gpu_structures_t`): offsets from the per-structure counts, pointers into this
+    /// builder's arrays, valid while the builder is neither changed nor dropped; kinds without elements
+    /// are NULL.
+    fn layout(&mut self) -> ffi::FemGpuStructures {
+        for kind in 0..4 {
+            let mut off = Vec::with_capacity(self.counts.len() + 1);
+            let mut run = 0usize;
+            off.push(run);
+            for c in &self.counts {
+                run += c[kind];
+                off.push(run);
+            }
+            self.offsets[kind] = off;
+        }
+        fn p<T>(v: &[T]) -> *const T {
+            if v.is_empty() { ptr::null() } else { v.as_ptr() }
+        }
+        let has = |n: &Vec<u32>, off: &Vec<usize>| if n.is_empty() { ptr::null() } else { off.as_ptr() };
+        ffi::FemGpuStructures {
+            n_structures: self.counts.len(),
+            nodes_number: p(&self.nodes_number),
+            node_off: self.offsets[0].as_ptr(),
+            node_numbers: p(&self.node_numbers),
+            xyz: p(&self.xyz),
+            truss_off: has(&self.truss_numbers, &self.offsets[1]),
+            truss_numbers: p(&self.truss_numbers),
+            truss_nodes: p(&self.truss_nodes),
+            truss_young: p(&self.truss_young),
+            truss_area: p(&self.truss_area),
+            truss_area2: p(&self.truss_area2),
+            beam_off: has(&self.beam_numbers, &self.offsets[2]),
+            beam_numbers: p(&self.beam_numbers),
+            beam_nodes: p(&self.beam_nodes),
+            beam_young: p(&self.beam_props[0]),
+            beam_poisson: p(&self.beam_props[1]),
+            beam_area: p(&self.beam_props[2]),
+            beam_i11: p(&self.beam_props[3]),
+            beam_i22: p(&self.beam_props[4]),
+            beam_i12: p(&self.beam_props[5]),
+            beam_it: p(&self.beam_props[6]),
+            beam_shear_factor: p(&self.beam_props[7]),
+            beam_local_axis: p(&self.beam_axis),
+            plate_off: has(&self.plate_numbers, &self.offsets[3]),
+            plate_numbers: p(&self.plate_numbers),
+            plate_nodes: p(&self.plate_nodes),
+            plate_young: p(&self.plate_props[0]),
+            plate_poisson: p(&self.plate_props[1]),
+            plate_thickness: p(&self.plate_props[2]),
+            plate_shear_factor: p(&self.plate_props[3]),
+        }
     }
 }

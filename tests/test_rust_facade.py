@@ -140,7 +140,8 @@ def test_integration_tests_call_only_facade_methods():
     assert files
     for f in files:
         src = _read("tests", f)
-        called = set(re.findall(r"\b(?:model|sep)\.(\w+)\(", src)) | set(re.findall(r"FEM::(\w+)\(", src))
+        called = set(re.findall(r"\b(?:model|sep|rec|batch)\.(\w+)\(", src)) | \
+            set(re.findall(r"\b(?:FEM|Batch|Structures)::(\w+)\(", src))
         assert called and called <= defined, (f, called - defined)
         for enum in set(re.findall(r"\b(DOFParameter|ElementForceComponent)::(\w+)", src)):
             assert re.search(r"pub enum " + enum[0] + r"\s*\{[^}]*\b" + enum[1] + r"\b", lib) or \
@@ -164,3 +165,12 @@ def test_integration_notes_declare_entry_points_as_the_header():
     for name, sig in shown.items():
         assert name in ffi, name
         assert sig == ffi[name], (name, sig, ffi[name])
+
+
+def test_structures_builder_fills_every_field():
+    """Structures::layout sets every field of the generated fem_gpu_structures_t, in its order"""
+    ffi = _read("src", "ffi.rs")
+    fields = re.findall(r"pub (\w+): ", re.search(r"pub struct FemGpuStructures \{(.*?)\}", ffi, re.S).group(1))
+    lib = _read("src", "lib.rs")
+    init = re.search(r"^\s*ffi::FemGpuStructures \{\n(.*?)\n\s*\}", lib, re.S | re.M).group(1)
+    assert re.findall(r"^\s*(\w+):", init, re.M) == fields
