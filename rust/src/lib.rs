@@ -795,8 +795,8 @@ impl Batch {
         self.len() == 0
     }
 
-    /// One more numeric pass of every structure (after changed coordinates or properties are not
-    /// supported: rebuild the batch).
+    /// One more numeric pass of every structure.  The structures' coordinates and properties are those
+    /// recorded at creation; for changed ones, build a new batch.
     pub fn assemble(&mut self) -> Result<(), String> {
         let st = unsafe { ffi::fem_gpu_batch_assemble(self.b) };
         self.check(st)
